@@ -1,0 +1,251 @@
+/*
+ * qmc.h -- C ABI of the GB300 walker-ensemble QMC library (libqmc_gb300.so).
+ *
+ * The library replaces the per-configuration Rust trait calls of rust_qmc's
+ * Slater-Jastrow walker path with batched calls over W walkers resident in
+ * GPU memory.  Every entry point below names the reference interface it
+ * replaces (paths are relative to the rust_qmc source tree).
+ *
+ * Conventions
+ *  - Plain C types only; no pointer is retained after a call returns.
+ *  - Host buffers are owned by the caller; device state lives behind handles.
+ *  - Every function returns a qmc_status (0 = success).  The library never
+ *    aborts or traps; a CUDA error is reported as QMC_ERR_CUDA.
+ *  - Positions are double precision, W x n_elec x 3, electrons in the
+ *    caller's (reference) order.  Internally electrons are regrouped into
+ *    contiguous spin sectors (spin +1 first, each sector in ascending caller
+ *    index); per-electron outputs are returned in the caller's order.
+ *  - psi is reported as (log|psi|, sign) instead of the reference's raw psi;
+ *    gradients are grad_i psi / psi, Laplacians lap_i psi / psi.
+ *  - One context = one CUDA stream; calls on one context are serialised.
+ *
+ * Random numbers: Philox4x32-10 keyed by the 64-bit seed, counter
+ *   c0 = walker id, c1 = step (low 32 bits), c2 = electron / sub-index,
+ *   c3 = tag | (step bits 32..47) << 16,  tag 1 proposal, 2 accept,
+ *   3 initial position, 4 branching.
+ * Trajectories therefore depend only on (seed, walker id, step), never on the
+ * launch geometry.
+ */
+#ifndef QMC_GB300_H
+#define QMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    QMC_OK = 0,
+    QMC_ERR_ARG = 1,          /* bad argument / size mismatch (reference: assert_eq! panics) */
+    QMC_ERR_CUDA = 2,         /* CUDA runtime error, no device, or extension unusable */
+    QMC_ERR_TIMEOUT = 3,      /* a bounded device wait gave up */
+    QMC_ERR_SINGULAR = 4,     /* a Slater matrix was singular (reference: identity fallback) */
+    QMC_ERR_POPULATION = 5,   /* DMC population left [N/4, 4N] */
+    QMC_ERR_NONFINITE = 6,    /* NaN/Inf ratio, energy or position */
+    QMC_ERR_UNSUPPORTED = 7,  /* no compiled kernel for this system shape */
+    QMC_ERR_NOMEM = 8
+};
+
+/* ---- enumerations -------------------------------------------------------- */
+enum { QMC_FP64 = 0, QMC_FP32_REFINE = 1 };          /* walker working precision */
+enum { QMC_BASIS_GTO = 0, QMC_BASIS_STO = 1 };       /* contracted Gaussians / Slater-type */
+enum { QMC_JAS_NONE = 0, QMC_JAS_PADE_F = 1, QMC_JAS_PADE_EEN = 2 };
+enum {
+    QMC_MOVE_ALL_GAUSS = 0,   /* all-electron Gaussian, src/sampling/vmc.rs:95-119 */
+    QMC_MOVE_ALL_BOX = 1,     /* all-electron uniform box of side `step` */
+    QMC_MOVE_ONE_GAUSS = 2,   /* single-electron Gaussian of width `step` */
+    QMC_MOVE_ONE_DRIFT = 3    /* single-electron Langevin, src/sampling/vmc.rs:339-394 */
+};
+enum {
+    QMC_QUIRK_J2_GRAD = 1,    /* Jastrow2 gradient prefactor F/(2(1+r/F)^2 r), src/correlation/jastrow.rs:102 */
+    QMC_QUIRK_J2_LAP = 2      /* Jastrow2 per-pair Laplacian without cross terms, :110-125 */
+};
+
+/* ---- system description (MultiWfn + EnergyCalculator data) ------------- */
+/*
+ * Replaces the constructors of H2MoleculeMO (src/systems/hydrogen.rs:28-35),
+ * Lithium (src/systems/lithium.rs:9-19), MethaneGTO (src/systems/methane.rs:
+ * 600-685) and BenzeneGTO (src/systems/benzene.rs:48-112).
+ *
+ * MO k = sum_a mo_coef[k*n_ao + a] * chi_a.  Electron e's Slater column is MO
+ * occ[e]; a spin sector's columns follow its electrons' order (the reference's
+ * STOSlaterDet uses orbital j for electron j, MethaneGTO uses MOs 0..n-1).
+ * Jastrow parameters for QMC_JAS_PADE_EEN, jas[] =
+ *   { b_anti, b_para, a_anti, a_para, B_0, B_1, A_0, A_1 }
+ *   u = sum_{i<j} a_s r/(1+b_s r) - sum_{i,I} A_sp Z_I r/(1+B_sp r),
+ *   s = spin class of the pair, sp = nuc_species[I];
+ * the reference Jastrow3 is b_anti=b_para=b_ee, A=1, B_0=B_1=b_en.
+ * QMC_JAS_PADE_F is u = sum_{i<j} -F/(2(1+r/F)) (Jastrow1 / Jastrow2).
+ * Optimisable parameters (OptimizableWfn) are jas[0..7] then rot_angle[0..n_rot-1]:
+ * angle q mixes MO rot_occ[q] with MO rot_virt[q]:
+ *   phi_occ <- cos(t) phi_occ + sin(t) phi_virt.
+ */
+typedef struct {
+    int n_elec;
+    const int* spins;            /* [n_elec] +1 / -1 */
+    int n_nuc;
+    const double* nuc_pos;       /* [n_nuc*3] */
+    const double* nuc_charge;    /* [n_nuc] */
+    const int* nuc_species;      /* [n_nuc] 0/1, or NULL */
+    int basis_kind;
+    int n_ao;
+    const int* ao_nuc;           /* [n_ao] centre of each AO */
+    const int* ao_l;             /* [n_ao] 0 = s, 1 = p */
+    const int* ao_m;             /* [n_ao] p component 0/1/2 = x/y/z */
+    const int* ao_prim_off;      /* [n_ao+1] primitive ranges */
+    const double* prim_exp;
+    const double* prim_coef;
+    const int* prim_pow;         /* Slater-type r^n powers; NULL for Gaussians */
+    int n_mo;
+    const double* mo_coef;       /* [n_mo*n_ao] */
+    const int* occ;              /* [n_elec] */
+    int jastrow_kind;
+    double jas_F;
+    double jas[8];
+    int n_rot;
+    const int* rot_occ;
+    const int* rot_virt;
+    const double* rot_angle;
+    int quirks;
+    const int* init_nuc;         /* [n_elec] initial centre per electron, -1 = origin; NULL = all origin */
+    double init_sigma;           /* width of the initial Gaussian (MultiWfn::initialize) */
+    double box_L;                /* must be 0: open boundary conditions */
+    int reserved[4];
+} qmc_system_desc;
+
+/* Parameters of a sampling run (MCMCParams src/sampling/vmc.rs:13-21,
+ * DDVMCParams :197-226, ISDMCParams src/sampling/is_dmc.rs:51-86). */
+typedef struct {
+    int n_walkers;
+    int n_steps;                 /* production steps (sweeps for single-electron moves) */
+    int n_burnin;
+    int move_kind;               /* QMC_MOVE_* */
+    double step;                 /* Gaussian width / box side */
+    double tau;                  /* drift-diffusion / DMC time step */
+    double max_drift;            /* |tau F| cap */
+    int precision;               /* QMC_FP64 / QMC_FP32_REFINE */
+    int refresh_every;           /* FP64 inverse recompute + E_L measurement period (sweeps) */
+    double e_ref_damping;        /* DMC kappa */
+    int reserved[6];
+} qmc_run_params;
+
+typedef struct {
+    double energy;
+    double error;
+    double autocorrelation_time;
+    double acceptance_rate;
+    double variance;
+    int n_samples;
+    int status_flags;
+    double avg_population;
+    double reserved[4];
+} qmc_run_result;
+
+typedef struct qmc_ctx_s* qmc_ctx_t;
+typedef struct qmc_sys_s* qmc_sys_t;
+typedef struct qmc_walkers_s* qmc_walkers_t;
+
+/* ---- context --------------------------------------------------------------- */
+int qmc_init(int device, qmc_ctx_t* out);
+int qmc_destroy(qmc_ctx_t ctx);
+const char* qmc_status_string(int status);
+int qmc_version(void);
+
+/* ---- systems ------------------------------------------------------------- */
+/* Builds device-ready tables from the description (replaces the reference
+ * constructors listed above).  QMC_ERR_UNSUPPORTED if no kernel is compiled
+ * for the (n_elec, n_up, n_nuc, basis, Jastrow) shape. */
+int qmc_system_create(qmc_ctx_t ctx, const qmc_system_desc* desc, qmc_sys_t* out);
+/* Validates a description without touching a device; *shape (may be NULL)
+ * receives the compiled kernel shape it maps to. */
+int qmc_system_check(const qmc_system_desc* desc, int* shape);
+int qmc_system_destroy(qmc_sys_t sys);
+/* OptimizableWfn::num_params/get_params/set_params, src/wavefunction/traits.rs:98-106 */
+int qmc_system_num_params(qmc_sys_t sys, int* P);
+int qmc_system_get_params(qmc_sys_t sys, double* p, int P);
+int qmc_system_set_params(qmc_sys_t sys, const double* p, int P);
+/* ForceCalculator::num_nuclei/set_nuclei, src/sampling/traits.rs:22-31 */
+int qmc_system_set_nuclei(qmc_sys_t sys, const double* R, int n_nuc);
+
+/* ---- batched evaluation (MultiWfn / EnergyCalculator / OptimizableWfn /
+ *      ForceCalculator methods for W configurations at once) ---------------- */
+/* MultiWfn::evaluate/derivative/laplacian (src/wavefunction/traits.rs:53-59)
+ * and EnergyCalculator::local_energy (src/sampling/traits.rs:6-8).
+ * precision QMC_FP64 evaluates in double; QMC_FP32_REFINE evaluates orbitals,
+ * determinants and E_L in single precision (the moving-walker form).
+ * Any output pointer may be NULL. */
+int qmc_eval_batch(qmc_sys_t sys, int W, const double* pos, int precision,
+                   double* logabs, int* sign, double* grad_ln, double* lap_over_psi,
+                   double* e_local);
+
+/* OptimizableWfn::log_derivatives (src/wavefunction/traits.rs:114;
+ * src/systems/methane.rs:1212-1219): O [W x P] plus E_L [W]; optionally the
+ * FP64 compensated SR sums over the batch: S [P x P] = <O O^T> - <O><O>^T,
+ * f [P] = <E O> - <E><O>, e_mean (any may be NULL). */
+int qmc_logderiv_batch(qmc_sys_t sys, int W, const double* pos, double* O, double* e_local,
+                       double* S, double* f, double* e_mean);
+
+/* ForceCalculator::hellmann_feynman_force and wfn_nuclear_gradient
+ * (src/sampling/traits.rs:38,50; src/systems/methane.rs:1007-1101,1241-1272):
+ * F_hf [W x n_nuc x 3], omega = d ln|psi| / dR_I [W x n_nuc x 3]. */
+int qmc_forces_batch(qmc_sys_t sys, int W, const double* pos, double* F_hf, double* omega);
+
+/* ---- resident walker ensembles (the sampler state: Vec<MCMCState>,
+ *      DDWalkerState, ISDMCWalker in the reference) ------------------------- */
+int qmc_walkers_create(qmc_sys_t sys, int W, int precision, qmc_walkers_t* out);
+int qmc_walkers_destroy(qmc_walkers_t wk);
+/* MultiWfn::initialize for every walker, seeded (tag 3 draws). */
+int qmc_walkers_init(qmc_walkers_t wk, uint64_t seed);
+/* Host <-> device positions (W x n_elec x 3, caller order). */
+int qmc_walkers_set_positions(qmc_walkers_t wk, const double* pos);
+int qmc_walkers_get_positions(qmc_walkers_t wk, double* pos);
+/* FP64 rebuild of every walker's inverse Slater matrices and log|psi| from its
+ * positions, plus the FP64 local energy.  e_local [W] may be NULL (kept on
+ * the device); e_sum receives the FP64 compensated sum (may be NULL). */
+int qmc_walkers_refresh(qmc_walkers_t wk, double* e_local, double* e_sum);
+/* n_sweeps Monte Carlo steps for all walkers (one launch):
+ * src/sampling/vmc.rs:95-119 (all-electron), :339-394 (single-electron).
+ * Sweep indices step0 .. step0+n_sweeps-1 key the random stream.
+ * accepted (may be NULL) receives the number of accepted proposals. */
+int qmc_walkers_sweep(qmc_walkers_t wk, int move_kind, int n_sweeps, uint64_t step0,
+                      double step, double tau, double max_drift, uint64_t seed,
+                      long long* accepted);
+/* Per-walker E_L [W] (device values from the last refresh) and logabs/sign. */
+int qmc_walkers_get_state(qmc_walkers_t wk, double* logabs, int* sign, double* e_local);
+/* Bitwise OR of the per-walker status flags raised since the last call
+ * (1 singular, 2 non-finite); cleared on read. */
+int qmc_walkers_status(qmc_walkers_t wk, int* flags);
+
+/* ---- drivers --------------------------------------------------------------- */
+/* VMC run: MCMCSimulation::run (src/sampling/vmc.rs:69-92) for all-electron
+ * moves, DriftDiffusionVMC::run (:405-484) for single-electron moves.  With
+ * single-electron moves E_L is measured (FP64) every refresh_every sweeps.
+ * energies (may be NULL) receives the per-measurement mean energies
+ * (capacity n_steps). */
+int qmc_vmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed,
+                qmc_run_result* result, double* energies);
+
+/* ---- timing helpers (no reference counterpart; used by the benchmark) ---- */
+/* Records CUDA event `slot` (0..15) on the context's stream. */
+int qmc_ctx_event_record(qmc_ctx_t ctx, int slot);
+/* Milliseconds between two recorded events (synchronises on `b`). */
+int qmc_ctx_event_elapsed(qmc_ctx_t ctx, int a, int b, float* ms);
+int qmc_ctx_synchronize(qmc_ctx_t ctx);
+/* Writes a device buffer larger than L2 to evict cached walker state. */
+int qmc_ctx_flush_l2(qmc_ctx_t ctx);
+/* Counts of kernel launches issued by this context since creation. */
+int qmc_ctx_launch_count(qmc_ctx_t ctx, long long* n);
+/* Measured FMA throughput of this GPU's CUDA cores (FP32 and FP64), the
+ * compute roofline of the walker kernels. */
+int qmc_ctx_measure_peaks(qmc_ctx_t ctx, double* fp32_tflops, double* fp64_tflops);
+/* Page-locked host buffers for asynchronous host<->device copies. */
+int qmc_host_alloc(size_t bytes, void** out);
+int qmc_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QMC_GB300_H */

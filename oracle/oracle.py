@@ -1,0 +1,133 @@
+"""ctypes wrapper of oracle/build/libqmc_oracle.so (test infrastructure).
+
+Takes the product's SystemSpec objects only as plain data (the descriptor
+layout is shared with include/qmc.h; tests check the sizes agree).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_u32p = C.POINTER(C.c_uint32)
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        l = C.CDLL(path)
+        vp = C.c_void_p
+        l.orc_desc_size.restype = C.c_int
+        l.orc_philox.argtypes = [_u32p, _u32p, _u32p]
+        l.orc_eval.argtypes = [vp, C.c_int, _dp, _dp, _ip, _dp, _dp, _dp, C.c_int]
+        l.orc_jastrow.argtypes = [vp, _dp, _dp, _dp, _dp]
+        l.orc_logderiv.argtypes = [vp, C.c_int, _dp, _dp, C.c_int]
+        l.orc_forces.argtypes = [vp, C.c_int, _dp, _dp, _dp, C.c_int]
+        l.orc_forces_fd.argtypes = [vp, C.c_int, _dp, C.c_double, _dp]
+        l.orc_init.argtypes = [vp, C.c_int, C.c_uint32, C.c_uint64, _dp]
+        l.orc_sweeps.argtypes = [vp, C.c_int, C.c_uint32, _dp, C.c_int, C.c_uint64, C.c_int, C.c_double,
+                                 C.c_double, C.c_double, C.c_uint64, _ip, _dp, C.c_int]
+        _lib = l
+    return _lib
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+def threads_default():
+    return os.cpu_count() or 1
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox(c, k, o)
+    return tuple(int(x) for x in o)
+
+
+def evaluate(spec, pos, threads=None):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    W, N = pos.shape[0], spec.n_elec
+    d = spec.desc()
+    out = dict(logabs=np.zeros(W), sign=np.zeros(W, np.int32), grad=np.zeros((W, N, 3)), lap=np.zeros((W, N)),
+               e_local=np.zeros(W))
+    lib().orc_eval(C.byref(d), W, _d(pos), _d(out["logabs"]), _i(out["sign"]), _d(out["grad"]), _d(out["lap"]),
+                   _d(out["e_local"]), threads or threads_default())
+    return out
+
+
+def jastrow(spec, r):
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    d = spec.desc()
+    J = C.c_double()
+    g = np.zeros((spec.n_elec, 3))
+    l = np.zeros(spec.n_elec)
+    lib().orc_jastrow(C.byref(d), _d(r), C.byref(J), _d(g), _d(l))
+    return J.value, g, l
+
+
+def log_derivatives(spec, pos, threads=None):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    W = pos.shape[0]
+    O = np.zeros((W, spec.n_params))
+    d = spec.desc()
+    lib().orc_logderiv(C.byref(d), W, _d(pos), _d(O), threads or threads_default())
+    return O
+
+
+def forces(spec, pos, threads=None):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    W = pos.shape[0]
+    F = np.zeros((W, spec.n_nuc, 3))
+    Om = np.zeros((W, spec.n_nuc, 3))
+    d = spec.desc()
+    lib().orc_forces(C.byref(d), W, _d(pos), _d(F), _d(Om), threads or threads_default())
+    return F, Om
+
+
+def nuclear_gradient_fd(spec, pos, h=1e-5):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    W = pos.shape[0]
+    Om = np.zeros((W, spec.n_nuc, 3))
+    d = spec.desc()
+    lib().orc_forces_fd(C.byref(d), W, _d(pos), h, _d(Om))
+    return Om
+
+
+def init_positions(spec, W, seed, walker0=0):
+    pos = np.zeros((W, spec.n_elec, 3))
+    d = spec.desc()
+    lib().orc_init(C.byref(d), W, walker0, seed, _d(pos))
+    return pos
+
+
+def sweeps(spec, pos, n_sweeps, sweep0, move_kind, seed, step=0.3, tau=0.01, max_drift=1.0, walker0=0,
+           threads=None, want_energy=True):
+    """Reference-algorithm Monte Carlo sweeps; returns (pos, accepted, e_local)."""
+    pos = np.array(pos, dtype=np.float64, copy=True)
+    W = pos.shape[0]
+    acc = np.zeros(W, np.int32)
+    el = np.zeros(W) if want_energy else None
+    d = spec.desc()
+    lib().orc_sweeps(C.byref(d), W, walker0, _d(pos), n_sweeps, sweep0, move_kind, step, tau, max_drift, seed,
+                     _i(acc), _d(el), threads or threads_default())
+    return pos, acc, el

@@ -1,0 +1,17 @@
+"""rust_qmc_gb300 -- GB300 (sm_103a) walker-ensemble Slater-Jastrow QMC.
+
+A from-scratch GPU implementation of the walker path of rust_qmc (VMC
+Metropolis and drift-diffusion sampling, local energies, parameter and
+nuclear derivatives) behind the C ABI of include/qmc.h.  This package is the
+ctypes face of that library plus the system builders; all numerical work
+runs in libqmc_gb300.so.
+"""
+from . import _lib
+from ._lib import QMCError, load_library
+from .api import Context, PinnedArray, System, Walkers, vmc_run
+from .systems import (SystemSpec, h2_mo, lithium_atom, methane_gto, methane_minimal, jastrow3_params,
+                      reference_params_from_general, seeded_orthonormal, philox4x32, SEED_BASE)
+
+__all__ = ["QMCError", "load_library", "Context", "PinnedArray", "System", "Walkers", "vmc_run", "SystemSpec",
+           "h2_mo", "lithium_atom", "methane_gto", "methane_minimal", "jastrow3_params",
+           "reference_params_from_general", "seeded_orthonormal", "philox4x32", "SEED_BASE", "_lib"]

@@ -1,0 +1,292 @@
+"""Python face of the C ABI, shaped like the reference's traits.
+
+``System`` exposes the batched calls (``eval_batch``, ``logderiv_batch``,
+``forces_batch``) and, for drop-in use one configuration at a time, the
+reference trait methods with their value conventions:
+
+  MultiWfn (src/wavefunction/traits.rs:48-91)
+      evaluate(r) -> psi, derivative(r) -> grad_i psi, laplacian(r) -> lap_i psi
+  EnergyCalculator (src/sampling/traits.rs:6-8)
+      local_energy(r)
+  OptimizableWfn (src/wavefunction/traits.rs:98-115)
+      num_params(), get_params(), set_params(p), log_derivatives(r)
+  ForceCalculator (src/sampling/traits.rs:20-56)
+      num_nuclei(), get_nuclei(), get_charges(), set_nuclei(R),
+      hellmann_feynman_force(r), wfn_nuclear_gradient(r)
+
+``Walkers`` is the device-resident ensemble (the samplers' walker vectors).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+class Context:
+    """One CUDA device + stream (qmc_init / qmc_destroy)."""
+
+    def __init__(self, device=0):
+        self.lib = L.load_library()
+        h = C.c_void_p()
+        L.check(self.lib.qmc_init(device, C.byref(h)), "qmc_init")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def record(self, slot):
+        L.check(self.lib.qmc_ctx_event_record(self.h, slot), "qmc_ctx_event_record")
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_float()
+        L.check(self.lib.qmc_ctx_event_elapsed(self.h, a, b, C.byref(ms)), "qmc_ctx_event_elapsed")
+        return float(ms.value)
+
+    def synchronize(self):
+        L.check(self.lib.qmc_ctx_synchronize(self.h), "qmc_ctx_synchronize")
+
+    def flush_l2(self):
+        L.check(self.lib.qmc_ctx_flush_l2(self.h), "qmc_ctx_flush_l2")
+
+    def measure_peaks(self):
+        """(FP32, FP64) FMA TFLOP/s measured on this GPU."""
+        a, b = C.c_double(), C.c_double()
+        L.check(self.lib.qmc_ctx_measure_peaks(self.h, C.byref(a), C.byref(b)), "qmc_ctx_measure_peaks")
+        return a.value, b.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        L.check(self.lib.qmc_ctx_launch_count(self.h, C.byref(n)), "qmc_ctx_launch_count")
+        return int(n.value)
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory (qmc_host_alloc)."""
+
+    def __init__(self, lib, shape, dtype=np.float64):
+        self.lib = lib
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        L.check(lib.qmc_host_alloc(n, C.byref(p)), "qmc_host_alloc")
+        self.ptr = p
+        buf = (C.c_char * n).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.lib.qmc_host_free(self.ptr)
+            self.ptr = None
+
+
+class System:
+    """A system handle (qmc_system_create) built from a SystemSpec."""
+
+    def __init__(self, ctx, spec):
+        self.ctx, self.spec, self.lib = ctx, spec, ctx.lib
+        self._desc = spec.desc()
+        h = C.c_void_p()
+        L.check(self.lib.qmc_system_create(ctx.h, C.byref(self._desc), C.byref(h)), "qmc_system_create")
+        self.h = h
+        self.N = spec.n_elec
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qmc_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- batched ------------------------------------------------------------
+    def _pos(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        if pos.ndim == 2:
+            pos = pos[None]
+        if pos.shape[1:] != (self.N, 3):
+            raise ValueError("positions must be W x %d x 3" % self.N)
+        return pos
+
+    def eval_batch(self, pos, precision=L.QMC_FP64):
+        pos = self._pos(pos)
+        W = pos.shape[0]
+        out = dict(logabs=np.zeros(W), sign=np.zeros(W, np.int32), grad=np.zeros((W, self.N, 3)),
+                   lap=np.zeros((W, self.N)), e_local=np.zeros(W))
+        L.check(self.lib.qmc_eval_batch(self.h, W, _d(pos), precision, _d(out["logabs"]), _i(out["sign"]),
+                                        _d(out["grad"]), _d(out["lap"]), _d(out["e_local"])), "qmc_eval_batch")
+        return out
+
+    def logderiv_batch(self, pos, sums=False):
+        pos = self._pos(pos)
+        W, P = pos.shape[0], self.num_params()
+        O, E = np.zeros((W, P)), np.zeros(W)
+        S = np.zeros((P, P)) if sums else None
+        f = np.zeros(P) if sums else None
+        em = C.c_double()
+        L.check(self.lib.qmc_logderiv_batch(self.h, W, _d(pos), _d(O), _d(E), _d(S), _d(f),
+                                            C.byref(em) if sums else None), "qmc_logderiv_batch")
+        if sums:
+            return O, E, S, f, em.value
+        return O, E
+
+    def forces_batch(self, pos):
+        pos = self._pos(pos)
+        W = pos.shape[0]
+        F = np.zeros((W, self.spec.n_nuc, 3))
+        Om = np.zeros((W, self.spec.n_nuc, 3))
+        L.check(self.lib.qmc_forces_batch(self.h, W, _d(pos), _d(F), _d(Om)), "qmc_forces_batch")
+        return F, Om
+
+    # -- OptimizableWfn -------------------------------------------------------
+    def num_params(self):
+        P = C.c_int()
+        L.check(self.lib.qmc_system_num_params(self.h, C.byref(P)), "qmc_system_num_params")
+        return P.value
+
+    def get_params(self):
+        p = np.zeros(self.num_params())
+        L.check(self.lib.qmc_system_get_params(self.h, _d(p), len(p)), "qmc_system_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        L.check(self.lib.qmc_system_set_params(self.h, _d(p), len(p)), "qmc_system_set_params")
+        self.spec = self.spec.with_params(p)
+
+    def log_derivatives(self, r):
+        return self.logderiv_batch(r)[0][0]
+
+    # -- MultiWfn / EnergyCalculator (single configuration) -------------------
+    def evaluate(self, r):
+        o = self.eval_batch(r)
+        return float(o["sign"][0] * np.exp(o["logabs"][0]))
+
+    def derivative(self, r):
+        o = self.eval_batch(r)
+        return o["grad"][0] * (o["sign"][0] * np.exp(o["logabs"][0]))
+
+    def laplacian(self, r):
+        o = self.eval_batch(r)
+        return o["lap"][0] * (o["sign"][0] * np.exp(o["logabs"][0]))
+
+    def local_energy(self, r):
+        return float(self.eval_batch(r)["e_local"][0])
+
+    # -- ForceCalculator -------------------------------------------------------
+    def num_nuclei(self):
+        return self.spec.n_nuc
+
+    def get_nuclei(self):
+        return self.spec.nuc_pos.copy()
+
+    def get_charges(self):
+        return self.spec.nuc_charge.copy()
+
+    def set_nuclei(self, R):
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(-1)
+        L.check(self.lib.qmc_system_set_nuclei(self.h, _d(R), len(R) // 3), "qmc_system_set_nuclei")
+        self.spec = self.spec.with_nuclei(R)
+
+    def hellmann_feynman_force(self, r):
+        return self.forces_batch(r)[0][0]
+
+    def wfn_nuclear_gradient(self, r):
+        return self.forces_batch(r)[1][0]
+
+
+class Walkers:
+    """Device-resident walker ensemble (qmc_walkers_*)."""
+
+    def __init__(self, system, W, precision=L.QMC_FP64):
+        self.sys, self.lib, self.W, self.precision = system, system.lib, W, precision
+        h = C.c_void_p()
+        L.check(self.lib.qmc_walkers_create(system.h, W, precision, C.byref(h)), "qmc_walkers_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qmc_walkers_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, seed):
+        L.check(self.lib.qmc_walkers_init(self.h, seed), "qmc_walkers_init")
+
+    def set_positions(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        L.check(self.lib.qmc_walkers_set_positions(self.h, _d(pos)), "qmc_walkers_set_positions")
+
+    def set_positions_ptr(self, ptr):
+        L.check(self.lib.qmc_walkers_set_positions(self.h, C.cast(ptr, _dp)), "qmc_walkers_set_positions")
+
+    def get_positions(self):
+        pos = np.zeros((self.W, self.sys.N, 3))
+        L.check(self.lib.qmc_walkers_get_positions(self.h, _d(pos)), "qmc_walkers_get_positions")
+        return pos
+
+    def refresh(self, want_energies=False):
+        el = np.zeros(self.W) if want_energies else None
+        s = C.c_double()
+        L.check(self.lib.qmc_walkers_refresh(self.h, _d(el), C.byref(s)), "qmc_walkers_refresh")
+        return (s.value, el) if want_energies else s.value
+
+    def refresh_async(self):
+        L.check(self.lib.qmc_walkers_refresh(self.h, None, None), "qmc_walkers_refresh")
+
+    def sweep(self, move_kind, n_sweeps, step0, seed, step=0.3, tau=0.01, max_drift=1.0, count=True):
+        acc = C.c_longlong()
+        L.check(self.lib.qmc_walkers_sweep(self.h, move_kind, n_sweeps, step0, step, tau, max_drift, seed,
+                                           C.byref(acc) if count else None), "qmc_walkers_sweep")
+        return acc.value if count else None
+
+    def state(self):
+        la, sg, el = np.zeros(self.W), np.zeros(self.W, np.int32), np.zeros(self.W)
+        L.check(self.lib.qmc_walkers_get_state(self.h, _d(la), _i(sg), _d(el)), "qmc_walkers_get_state")
+        return la, sg, el
+
+    def status(self):
+        f = C.c_int()
+        L.check(self.lib.qmc_walkers_status(self.h, C.byref(f)), "qmc_walkers_status")
+        return f.value
+
+
+def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0, tau=0.01,
+            max_drift=1.0, precision=L.QMC_FP64, refresh_every=64, seed=1):
+    """MCMCSimulation::run / DriftDiffusionVMC::run on the device."""
+    p = L.RunParams()
+    p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = n_walkers, n_steps, n_burnin, move_kind
+    p.step, p.tau, p.max_drift, p.precision, p.refresh_every = step, tau, max_drift, precision, refresh_every
+    res = L.RunResult()
+    energies = np.zeros(n_steps)
+    L.check(system.lib.qmc_vmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_vmc_run")
+    return dict(energy=res.energy, error=res.error, autocorrelation_time=res.autocorrelation_time,
+                acceptance_rate=res.acceptance_rate, variance=res.variance, n_samples=res.n_samples,
+                status_flags=res.status_flags, energies=energies[:res.n_samples])

@@ -1,0 +1,788 @@
+// qmc_api.cpp -- C ABI of libqmc_gb300 (declared in include/qmc.h): context,
+// system tables, resident walker ensembles, batched evaluation and the VMC
+// driver.  All numerical work runs in the CUDA kernels of qmc_kernels.cu;
+// this file only validates arguments, lays data out for the device and
+// orchestrates launches.  There is no CPU fallback: without a usable CUDA
+// device every entry point that needs one returns QMC_ERR_CUDA.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <new>
+#include <vector>
+#include <cuda_runtime.h>
+#include "../../include/qmc.h"
+#include "qmc_internal.h"
+
+using namespace qmc;
+
+namespace qmc {
+int launch_step_all_recorded(const HostSys& hs, DevWalkers& dw, int move_kind, int n, uint64_t s0, double step,
+                             uint64_t seed, double* partial, cudaStream_t st);
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+int launch_scatter_positions(const double* src, DevWalkers& dw, const int* d_perm, int N, cudaStream_t st);
+int launch_gather_positions(const DevWalkers& dw, double* dst, const int* d_perm, int N, cudaStream_t st);
+int measure_fma_peak(int fp64, double* tflops, cudaStream_t st);
+}
+
+struct qmc_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[16] = {};
+    void* flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    long long launches0 = 0;
+};
+
+struct qmc_walkers_s;
+
+struct qmc_sys_s {
+    qmc_ctx_s* ctx = nullptr;
+    HostSys hs;
+    int* d_perm = nullptr;                 // internal -> caller electron index (device)
+    qmc_walkers_s* scratch[2] = {nullptr, nullptr};   // batch-evaluation walker sets per precision
+};
+
+struct qmc_walkers_s {
+    qmc_sys_s* sys = nullptr;
+    DevWalkers dw;
+    double* d_stage = nullptr;             // caller-order positions [W][N][3]
+    double* d_out = nullptr;               // generic device output scratch
+    size_t d_out_cap = 0;
+    unsigned long long acc_host = 0;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) {
+    if (e == cudaSuccess) return QMC_OK;
+    std::fprintf(stderr, "qmc_gb300: %s\n", cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? QMC_ERR_NOMEM : QMC_ERR_CUDA;
+}
+
+#define CK(x) do { int _rc = (x); if (_rc) return _rc; } while (0)
+#define CU(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return cuda_rc(_e); } while (0)
+
+// Build the device-ready host description; validates every field.
+int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
+    if (!d || d->n_elec <= 0 || d->n_elec > 64 || !d->spins || d->n_nuc <= 0 || d->n_nuc > 32) return QMC_ERR_ARG;
+    if (!d->nuc_pos || !d->nuc_charge || d->n_ao <= 0 || !d->ao_nuc || !d->ao_l || !d->ao_m || !d->ao_prim_off) return QMC_ERR_ARG;
+    if (!d->prim_exp || !d->prim_coef || d->n_mo <= 0 || !d->mo_coef || !d->occ) return QMC_ERR_ARG;
+    if (d->box_L != 0.0) return QMC_ERR_UNSUPPORTED;
+    if (d->basis_kind != QMC_BASIS_GTO && d->basis_kind != QMC_BASIS_STO) return QMC_ERR_ARG;
+    if (d->jastrow_kind < 0 || d->jastrow_kind > 2) return QMC_ERR_ARG;
+    if (d->n_rot < 0 || d->n_rot > 16 || (d->n_rot && (!d->rot_occ || !d->rot_virt || !d->rot_angle))) return QMC_ERR_ARG;
+    hs = HostSys();
+    hs.N = d->n_elec;
+    hs.spins.assign(d->spins, d->spins + hs.N);
+    for (int e = 0; e < hs.N; ++e) {
+        if (hs.spins[e] != 1 && hs.spins[e] != -1) return QMC_ERR_ARG;
+        if (hs.spins[e] > 0) hs.n_up++; else hs.n_dn++;
+    }
+    for (int sig = 0; sig < 2; ++sig)
+        for (int e = 0; e < hs.N; ++e)
+            if ((hs.spins[e] > 0) == (sig == 0)) hs.perm.push_back(e);
+    hs.n_nuc = d->n_nuc;
+    hs.R.assign(d->nuc_pos, d->nuc_pos + 3 * hs.n_nuc);
+    hs.Z.assign(d->nuc_charge, d->nuc_charge + hs.n_nuc);
+    for (int I = 0; I < hs.n_nuc; ++I) {
+        int sp = d->nuc_species ? d->nuc_species[I] : 0;
+        if (sp < 0 || sp > 1) return QMC_ERR_ARG;
+        hs.species.push_back(sp);
+    }
+    hs.basis = d->basis_kind;
+    hs.n_ao = d->n_ao;
+    hs.n_mo = d->n_mo;
+    int np = d->ao_prim_off[hs.n_ao];
+    if (d->ao_prim_off[0] != 0 || np <= 0) return QMC_ERR_ARG;
+    for (int a = 0; a < hs.n_ao; ++a) {
+        if (d->ao_prim_off[a + 1] <= d->ao_prim_off[a]) return QMC_ERR_ARG;
+        if (d->ao_nuc[a] < 0 || d->ao_nuc[a] >= hs.n_nuc) return QMC_ERR_ARG;
+        if (d->ao_l[a] < 0 || d->ao_l[a] > 1 || d->ao_m[a] < 0 || d->ao_m[a] > 2) return QMC_ERR_ARG;
+        if (d->basis_kind == QMC_BASIS_STO && d->ao_l[a] != 0) return QMC_ERR_ARG;
+    }
+    // group AOs into shells (same centre, exponents and powers)
+    std::vector<int> used(hs.n_ao, 0);
+    auto prim_exps = [&](int a) { return std::vector<double>(d->prim_exp + d->ao_prim_off[a], d->prim_exp + d->ao_prim_off[a + 1]); };
+    auto prim_pows = [&](int a) {
+        if (!d->prim_pow) return std::vector<int>(d->ao_prim_off[a + 1] - d->ao_prim_off[a], 0);
+        return std::vector<int>(d->prim_pow + d->ao_prim_off[a], d->prim_pow + d->ao_prim_off[a + 1]);
+    };
+    auto prim_coefs = [&](int a) { return std::vector<double>(d->prim_coef + d->ao_prim_off[a], d->prim_coef + d->ao_prim_off[a + 1]); };
+    for (int a = 0; a < hs.n_ao; ++a) {
+        if (used[a]) continue;
+        std::vector<double> ex = prim_exps(a);
+        std::vector<int> pw = prim_pows(a);
+        for (int p : pw) if (p < 0 || p > 6) return QMC_ERR_ARG;
+        // find an existing shell with the same key and room
+        HostShell* sh = nullptr;
+        for (auto& s : hs.shells)
+            if (s.nuc == d->ao_nuc[a] && s.exps == ex && s.pows == pw) {
+                if (d->ao_l[a] == 0 && (s.s_ao[0] < 0 || s.s_ao[1] < 0)) { sh = &s; break; }
+                if (d->ao_l[a] == 1 && s.p_ao[0] < 0) { sh = &s; break; }
+            }
+        if (!sh) {
+            hs.shells.emplace_back();
+            sh = &hs.shells.back();
+            sh->nuc = d->ao_nuc[a];
+            sh->exps = ex;
+            sh->pows = pw;
+        }
+        if (d->ao_l[a] == 0) {
+            int slot = sh->s_ao[0] < 0 ? 0 : 1;
+            sh->s_ao[slot] = a;
+            sh->s_coef[slot] = prim_coefs(a);
+            used[a] = 1;
+        } else {
+            // gather the x, y, z members of this p triplet
+            std::vector<double> cf = prim_coefs(a);
+            int trip[3] = {-1, -1, -1};
+            for (int b = a; b < hs.n_ao; ++b) {
+                if (used[b] || d->ao_l[b] != 1 || d->ao_nuc[b] != d->ao_nuc[a]) continue;
+                if (prim_exps(b) != ex || prim_coefs(b) != cf) continue;
+                int m = d->ao_m[b];
+                if (trip[m] < 0) trip[m] = b;
+            }
+            if (trip[0] < 0 || trip[1] < 0 || trip[2] < 0) return QMC_ERR_ARG;
+            for (int m = 0; m < 3; ++m) { sh->p_ao[m] = trip[m]; used[trip[m]] = 1; }
+            sh->p_coef = cf;
+        }
+    }
+    std::stable_sort(hs.shells.begin(), hs.shells.end(), [](const HostShell& x, const HostShell& y) { return x.nuc < y.nuc; });
+    hs.ao_int.assign(hs.n_ao, -1);
+    int nxt = 0;
+    for (auto& s : hs.shells) {
+        for (int k = 0; k < 2; ++k) if (s.s_ao[k] >= 0) hs.ao_int[s.s_ao[k]] = nxt++;
+        if (s.p_ao[0] >= 0) for (int m = 0; m < 3; ++m) hs.ao_int[s.p_ao[m]] = nxt++;
+    }
+    if (nxt != hs.n_ao) return QMC_ERR_ARG;
+    hs.C0.assign(d->mo_coef, d->mo_coef + (size_t)hs.n_mo * hs.n_ao);
+    hs.occ.assign(d->occ, d->occ + hs.N);
+    for (int e = 0; e < hs.N; ++e) if (hs.occ[e] < 0 || hs.occ[e] >= hs.n_mo) return QMC_ERR_ARG;
+    hs.jk = d->jastrow_kind;
+    hs.F = d->jas_F;
+    if (hs.jk == QMC_JAS_PADE_F && !(hs.F > 0)) return QMC_ERR_ARG;
+    for (int i = 0; i < 8; ++i) hs.jas[i] = d->jas[i];
+    for (int q = 0; q < d->n_rot; ++q) {
+        if (d->rot_occ[q] < 0 || d->rot_occ[q] >= hs.n_mo || d->rot_virt[q] < 0 || d->rot_virt[q] >= hs.n_mo) return QMC_ERR_ARG;
+        hs.rot_occ.push_back(d->rot_occ[q]);
+        hs.rot_virt.push_back(d->rot_virt[q]);
+        hs.rot_angle.push_back(d->rot_angle[q]);
+    }
+    for (int q = 0; q < d->n_rot; ++q)
+        for (int q2 = 0; q2 < q; ++q2) if (hs.rot_occ[q] == hs.rot_occ[q2]) return QMC_ERR_ARG;
+    hs.quirks = d->quirks;
+    if (d->init_nuc) hs.init_nuc.assign(d->init_nuc, d->init_nuc + hs.N);
+    else hs.init_nuc.assign(hs.N, -1);
+    for (int e = 0; e < hs.N; ++e) if (hs.init_nuc[e] >= hs.n_nuc) return QMC_ERR_ARG;
+    hs.init_sigma = d->init_sigma;
+    hs.v_nn = 0.0;
+    for (int I = 0; I < hs.n_nuc; ++I)
+        for (int J = I + 1; J < hs.n_nuc; ++J) {
+            double dx = hs.R[3 * I] - hs.R[3 * J], dy = hs.R[3 * I + 1] - hs.R[3 * J + 1], dz = hs.R[3 * I + 2] - hs.R[3 * J + 2];
+            hs.v_nn += hs.Z[I] * hs.Z[J] / std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    // shape
+    hs.shape = -1;
+    if (hs.N == 2 && hs.n_up == 1 && hs.n_nuc == 2 && hs.basis == QMC_BASIS_STO && hs.jk == QMC_JAS_PADE_F) hs.shape = SHAPE_H2;
+    if (hs.N == 3 && hs.n_up == 2 && hs.n_nuc == 1 && hs.basis == QMC_BASIS_STO && hs.jk == QMC_JAS_PADE_F) hs.shape = SHAPE_LI;
+    if (hs.N == 10 && hs.n_up == 5 && hs.n_nuc == 5 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN) hs.shape = SHAPE_CH4;
+    if (hs.shape < 0) return QMC_ERR_UNSUPPORTED;
+    return QMC_OK;
+}
+
+int alloc_walkers(qmc_sys_s* sys, int W, int prec, qmc_walkers_s** out) {
+    if (W <= 0 || (prec != QMC_FP64 && prec != QMC_FP32_REFINE)) return QMC_ERR_ARG;
+    cudaSetDevice(sys->ctx->device);
+    qmc_walkers_s* wk = new (std::nothrow) qmc_walkers_s();
+    if (!wk) return QMC_ERR_NOMEM;
+    wk->sys = sys;
+    DevWalkers& dw = wk->dw;
+    const HostSys& hs = sys->hs;
+    dw.W = W;
+    dw.Wcap = ((W + 127) / 128) * 128;
+    dw.prec = prec;
+    size_t ts = prec == QMC_FP64 ? 8 : 4;
+    int nm = nmax_of_shape(hs.shape);
+    size_t Wc = dw.Wcap;
+    int nblk = (int)((Wc + 63) / 64);
+    dw.partial_cap = 2 * nblk + 64;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&dw.pos, ts * 3 * hs.N * Wc);
+    if (e == cudaSuccess) e = cudaMalloc(&dw.dinv, ts * 2 * nm * nm * Wc);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.logabs, 8 * Wc);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.sign, 4 * Wc);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.el, 8 * Wc);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.flags, 4);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.acc, 8);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dw.partial, 8 * (size_t)dw.partial_cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&wk->d_stage, 8 * 3 * (size_t)hs.N * Wc);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.flags, 0, 4, sys->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, sys->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, sys->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.dinv, 0, ts * 2 * nm * nm * Wc, sys->ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
+        cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(wk->d_stage);
+        delete wk;
+        return cuda_rc(e);
+    }
+    *out = wk;
+    return QMC_OK;
+}
+
+void free_walkers(qmc_walkers_s* wk) {
+    if (!wk) return;
+    DevWalkers& dw = wk->dw;
+    cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
+    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(wk->d_stage); cudaFree(wk->d_out);
+    delete wk;
+}
+
+int ensure_out(qmc_walkers_s* wk, size_t doubles) {
+    if (wk->d_out_cap >= doubles) return QMC_OK;
+    cudaFree(wk->d_out);
+    wk->d_out = nullptr;
+    wk->d_out_cap = 0;
+    CU(cudaMalloc((void**)&wk->d_out, doubles * 8));
+    wk->d_out_cap = doubles;
+    return QMC_OK;
+}
+
+// A scratch walker set of at least W walkers for batched evaluation.
+int scratch_walkers(qmc_sys_s* sys, int W, int prec, qmc_walkers_s** out) {
+    qmc_walkers_s*& s = sys->scratch[prec];
+    if (s && s->dw.Wcap >= W) { s->dw.W = W; *out = s; return QMC_OK; }
+    free_walkers(s);
+    s = nullptr;
+    CK(alloc_walkers(sys, W, prec, &s));
+    *out = s;
+    return QMC_OK;
+}
+
+int upload_positions(qmc_walkers_s* wk, const double* pos) {
+    const HostSys& hs = wk->sys->hs;
+    cudaStream_t st = wk->sys->ctx->stream;
+    CU(cudaMemcpyAsync(wk->d_stage, pos, sizeof(double) * 3 * hs.N * (size_t)wk->dw.W, cudaMemcpyHostToDevice, st));
+    return launch_scatter_positions(wk->d_stage, wk->dw, wk->sys->d_perm, hs.N, st);
+}
+
+// Statistics of a per-step energy series: src/sampling/vmc.rs:141-188.
+double autocorrelation_time(const std::vector<double>& x) {
+    size_t n = x.size();
+    if (n == 0) return 1.0;
+    double mean = 0.0;
+    for (double v : x) mean += v;
+    mean /= (double)n;
+    double var = 0.0;
+    for (double v : x) var += (v - mean) * (v - mean);
+    var /= (double)n;
+    if (var == 0.0) return 1.0;
+    double tau = 1.0;
+    for (size_t t = 1; t < n / 2; ++t) {
+        double s = 0.0;
+        for (size_t i = 0; i + t < n; ++i) s += (x[i] - mean) * (x[i + t] - mean);
+        double a = s / ((double)(n - t) * var);
+        if (a < 0.0) break;
+        tau += 2.0 * a;
+    }
+    return tau;
+}
+
+double blocking_error(const std::vector<double>& x, double tau) {
+    size_t bs = (size_t)std::ceil(2.0 * tau);
+    if (bs == 0) bs = 1;
+    size_t nb = x.size() / bs;
+    if (nb < 2) return 0.0;
+    std::vector<double> m(nb, 0.0);
+    for (size_t b = 0; b < nb; ++b) {
+        for (size_t i = 0; i < bs; ++i) m[b] += x[b * bs + i];
+        m[b] /= (double)bs;
+    }
+    double mu = 0.0;
+    for (double v : m) mu += v;
+    mu /= (double)nb;
+    double var = 0.0;
+    for (double v : m) var += (v - mu) * (v - mu);
+    var /= (double)(nb - 1);
+    return std::sqrt(var / (double)nb);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// HostSys helpers
+// ---------------------------------------------------------------------------
+std::vector<double> HostSys::effective_mo() const {
+    std::vector<double> C = C0;
+    for (size_t q = 0; q < rot_occ.size(); ++q) {
+        int k = rot_occ[q], v = rot_virt[q];
+        double c = std::cos(rot_angle[q]), s = std::sin(rot_angle[q]);
+        for (int a = 0; a < n_ao; ++a) C[(size_t)k * n_ao + a] = c * C0[(size_t)k * n_ao + a] + s * C0[(size_t)v * n_ao + a];
+    }
+    return C;
+}
+
+std::vector<double> HostSys::rotation_derivative_rows() const {
+    std::vector<double> D(rot_occ.size() * (size_t)n_ao, 0.0);
+    for (size_t q = 0; q < rot_occ.size(); ++q) {
+        int k = rot_occ[q], v = rot_virt[q];
+        double c = std::cos(rot_angle[q]), s = std::sin(rot_angle[q]);
+        for (int a = 0; a < n_ao; ++a) D[q * n_ao + a] = -s * C0[(size_t)k * n_ao + a] + c * C0[(size_t)v * n_ao + a];
+    }
+    return D;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int qmc_version(void) { return 100; }
+
+const char* qmc_status_string(int s) {
+    switch (s) {
+        case QMC_OK: return "ok";
+        case QMC_ERR_ARG: return "invalid argument";
+        case QMC_ERR_CUDA: return "CUDA error or no usable device";
+        case QMC_ERR_TIMEOUT: return "bounded device wait timed out";
+        case QMC_ERR_SINGULAR: return "singular Slater matrix";
+        case QMC_ERR_POPULATION: return "DMC population out of range";
+        case QMC_ERR_NONFINITE: return "non-finite value";
+        case QMC_ERR_UNSUPPORTED: return "no kernel compiled for this system shape";
+        case QMC_ERR_NOMEM: return "out of memory";
+    }
+    return "unknown status";
+}
+
+int qmc_init(int device, qmc_ctx_t* out) {
+    if (!out) return QMC_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) { cudaGetLastError(); return QMC_ERR_CUDA; }
+    if (device < 0 || device >= n) return QMC_ERR_ARG;
+    CU(cudaSetDevice(device));
+    qmc_ctx_s* c = new (std::nothrow) qmc_ctx_s();
+    if (!c) return QMC_ERR_NOMEM;
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) { delete c; return cuda_rc(e); }
+    c->launches0 = g_launch_count;
+    *out = c;
+    return QMC_OK;
+}
+
+int qmc_destroy(qmc_ctx_t c) {
+    if (!c) return QMC_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < 16; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->flush_buf) cudaFree(c->flush_buf);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return QMC_OK;
+}
+
+int qmc_system_create(qmc_ctx_t ctx, const qmc_system_desc* desc, qmc_sys_t* out) {
+    if (!ctx || !desc || !out) return QMC_ERR_ARG;
+    *out = nullptr;
+    qmc_sys_s* s = new (std::nothrow) qmc_sys_s();
+    if (!s) return QMC_ERR_NOMEM;
+    s->ctx = ctx;
+    int rc = build_hostsys(desc, s->hs);
+    if (rc) { delete s; return rc; }
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMalloc((void**)&s->d_perm, sizeof(int) * s->hs.N);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->d_perm, s->hs.perm.data(), sizeof(int) * s->hs.N, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { cudaFree(s->d_perm); delete s; return cuda_rc(e); }
+    *out = s;
+    return QMC_OK;
+}
+
+int qmc_system_check(const qmc_system_desc* desc, int* shape) {
+    HostSys hs;
+    int rc = build_hostsys(desc, hs);
+    if (shape) *shape = rc == QMC_OK ? hs.shape : -1;
+    return rc;
+}
+
+int qmc_system_destroy(qmc_sys_t s) {
+    if (!s) return QMC_ERR_ARG;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_walkers(s->scratch[0]);
+    free_walkers(s->scratch[1]);
+    cudaFree(s->d_perm);
+    delete s;
+    return QMC_OK;
+}
+
+int qmc_system_num_params(qmc_sys_t s, int* P) {
+    if (!s || !P) return QMC_ERR_ARG;
+    *P = s->hs.n_params();
+    return QMC_OK;
+}
+
+int qmc_system_get_params(qmc_sys_t s, double* p, int P) {
+    if (!s || !p || P != s->hs.n_params()) return QMC_ERR_ARG;
+    for (int i = 0; i < 8; ++i) p[i] = s->hs.jas[i];
+    for (size_t q = 0; q < s->hs.rot_angle.size(); ++q) p[8 + q] = s->hs.rot_angle[q];
+    return QMC_OK;
+}
+
+int qmc_system_set_params(qmc_sys_t s, const double* p, int P) {
+    if (!s || !p || P != s->hs.n_params()) return QMC_ERR_ARG;
+    for (int i = 0; i < P; ++i) if (!std::isfinite(p[i])) return QMC_ERR_ARG;
+    for (int i = 0; i < 8; ++i) s->hs.jas[i] = p[i];
+    for (size_t q = 0; q < s->hs.rot_angle.size(); ++q) s->hs.rot_angle[q] = p[8 + q];
+    return QMC_OK;
+}
+
+int qmc_system_set_nuclei(qmc_sys_t s, const double* R, int n_nuc) {
+    if (!s || !R || n_nuc != s->hs.n_nuc) return QMC_ERR_ARG;
+    for (int i = 0; i < 3 * n_nuc; ++i) if (!std::isfinite(R[i])) return QMC_ERR_ARG;
+    s->hs.R.assign(R, R + 3 * n_nuc);
+    HostSys& hs = s->hs;
+    hs.v_nn = 0.0;
+    for (int I = 0; I < hs.n_nuc; ++I)
+        for (int J = I + 1; J < hs.n_nuc; ++J) {
+            double dx = hs.R[3 * I] - hs.R[3 * J], dy = hs.R[3 * I + 1] - hs.R[3 * J + 1], dz = hs.R[3 * I + 2] - hs.R[3 * J + 2];
+            hs.v_nn += hs.Z[I] * hs.Z[J] / std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    return QMC_OK;
+}
+
+int qmc_eval_batch(qmc_sys_t s, int W, const double* pos, int precision, double* logabs, int* sign,
+                   double* grad_ln, double* lap_over_psi, double* e_local) {
+    if (!s || W <= 0 || !pos || (precision != QMC_FP64 && precision != QMC_FP32_REFINE)) return QMC_ERR_ARG;
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    qmc_walkers_s* wk;
+    CK(scratch_walkers(s, W, precision, &wk));
+    const HostSys& hs = s->hs;
+    int N = hs.N;
+    CK(upload_positions(wk, pos));
+    CK(ensure_out(wk, (size_t)W * N * 4));
+    MeasureOut mo;
+    if (grad_ln) mo.grad = wk->d_out;
+    if (lap_over_psi) mo.lap = wk->d_out + (size_t)W * N * 3;
+    CK(launch_measure(hs, wk->dw, precision == QMC_FP64 ? 0 : 1, true, mo, st));
+    std::vector<double> g(grad_ln ? (size_t)W * N * 3 : 0), l(lap_over_psi ? (size_t)W * N : 0);
+    if (grad_ln) CU(cudaMemcpyAsync(g.data(), mo.grad, 8 * g.size(), cudaMemcpyDeviceToHost, st));
+    if (lap_over_psi) CU(cudaMemcpyAsync(l.data(), mo.lap, 8 * l.size(), cudaMemcpyDeviceToHost, st));
+    if (logabs) CU(cudaMemcpyAsync(logabs, wk->dw.logabs, 8 * (size_t)W, cudaMemcpyDeviceToHost, st));
+    if (sign) CU(cudaMemcpyAsync(sign, wk->dw.sign, 4 * (size_t)W, cudaMemcpyDeviceToHost, st));
+    if (e_local) CU(cudaMemcpyAsync(e_local, wk->dw.el, 8 * (size_t)W, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (int w = 0; w < W; ++w)
+        for (int ei = 0; ei < N; ++ei) {
+            int e = hs.perm[ei];
+            if (grad_ln) for (int c = 0; c < 3; ++c) grad_ln[((size_t)w * N + e) * 3 + c] = g[((size_t)w * N + ei) * 3 + c];
+            if (lap_over_psi) lap_over_psi[(size_t)w * N + e] = l[(size_t)w * N + ei];
+        }
+    int fl = 0;
+    CU(cudaMemcpy(&fl, wk->dw.flags, 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemset(wk->dw.flags, 0, 4));
+    return QMC_OK;
+}
+
+int qmc_logderiv_batch(qmc_sys_t s, int W, const double* pos, double* O, double* e_local, double* S, double* f,
+                       double* e_mean) {
+    if (!s || W <= 0 || !pos) return QMC_ERR_ARG;
+    if (s->hs.jk != QMC_JAS_PADE_EEN) return QMC_ERR_UNSUPPORTED;
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    qmc_walkers_s* wk;
+    CK(scratch_walkers(s, W, QMC_FP64, &wk));
+    const HostSys& hs = s->hs;
+    int P = hs.n_params();
+    int M = 2 + 2 * P + P * (P + 1) / 2;
+    int nblk = std::min(1024, std::max(1, (W + 255) / 256));
+    size_t need = (size_t)W * P + (size_t)M + 2 * (size_t)M * nblk + 64;
+    CK(upload_positions(wk, pos));
+    CK(ensure_out(wk, need));
+    MeasureOut mo;
+    mo.O = wk->d_out;
+    CK(launch_measure(hs, wk->dw, 0, true, mo, st));
+    double* d_sums = wk->d_out + (size_t)W * P;
+    double* d_scr = d_sums + M;
+    if (S || f || e_mean)
+        CK(launch_sr_sums(wk->dw.el, mo.O, W, P, d_sums, d_scr, (int)(2 * (size_t)M * nblk + 64), st));
+    if (O) CU(cudaMemcpyAsync(O, mo.O, 8 * (size_t)W * P, cudaMemcpyDeviceToHost, st));
+    if (e_local) CU(cudaMemcpyAsync(e_local, wk->dw.el, 8 * (size_t)W, cudaMemcpyDeviceToHost, st));
+    std::vector<double> sums(M);
+    if (S || f || e_mean) CU(cudaMemcpyAsync(sums.data(), d_sums, 8 * (size_t)M, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (S || f || e_mean) {
+        double n = (double)W;
+        double Em = sums[0] / n;
+        if (e_mean) *e_mean = Em;
+        std::vector<double> Om(P);
+        for (int p = 0; p < P; ++p) Om[p] = sums[2 + p] / n;
+        if (f) for (int p = 0; p < P; ++p) f[p] = sums[2 + P + p] / n - Em * Om[p];
+        if (S) {
+            int m = 2 + 2 * P;
+            for (int p = 0; p < P; ++p)
+                for (int q = p; q < P; ++q) {
+                    double v = sums[m++] / n - Om[p] * Om[q];
+                    S[p * P + q] = v;
+                    S[q * P + p] = v;
+                }
+        }
+    }
+    return QMC_OK;
+}
+
+int qmc_forces_batch(qmc_sys_t s, int W, const double* pos, double* F_hf, double* omega) {
+    if (!s || W <= 0 || !pos) return QMC_ERR_ARG;
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    qmc_walkers_s* wk;
+    CK(scratch_walkers(s, W, QMC_FP64, &wk));
+    const HostSys& hs = s->hs;
+    size_t per = (size_t)W * hs.n_nuc * 3;
+    CK(upload_positions(wk, pos));
+    CK(ensure_out(wk, 2 * per));
+    MeasureOut mo;
+    if (F_hf) mo.fhf = wk->d_out;
+    if (omega) mo.omega = wk->d_out + per;
+    CK(launch_measure(hs, wk->dw, 0, true, mo, st));
+    if (F_hf) CU(cudaMemcpyAsync(F_hf, mo.fhf, 8 * per, cudaMemcpyDeviceToHost, st));
+    if (omega) CU(cudaMemcpyAsync(omega, mo.omega, 8 * per, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return QMC_OK;
+}
+
+int qmc_walkers_create(qmc_sys_t s, int W, int precision, qmc_walkers_t* out) {
+    if (!s || !out) return QMC_ERR_ARG;
+    *out = nullptr;
+    return alloc_walkers(s, W, precision, out);
+}
+
+int qmc_walkers_destroy(qmc_walkers_t wk) {
+    if (!wk) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStreamSynchronize(wk->sys->ctx->stream);
+    free_walkers(wk);
+    return QMC_OK;
+}
+
+int qmc_walkers_init(qmc_walkers_t wk, uint64_t seed) {
+    if (!wk) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    return launch_init(wk->sys->hs, wk->dw, seed, wk->sys->ctx->stream);
+}
+
+int qmc_walkers_set_positions(qmc_walkers_t wk, const double* pos) {
+    if (!wk || !pos) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    return upload_positions(wk, pos);
+}
+
+int qmc_walkers_get_positions(qmc_walkers_t wk, double* pos) {
+    if (!wk || !pos) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStream_t st = wk->sys->ctx->stream;
+    const HostSys& hs = wk->sys->hs;
+    CK(launch_gather_positions(wk->dw, wk->d_stage, wk->sys->d_perm, hs.N, st));
+    CU(cudaMemcpyAsync(pos, wk->d_stage, sizeof(double) * 3 * hs.N * (size_t)wk->dw.W, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return QMC_OK;
+}
+
+int qmc_walkers_refresh(qmc_walkers_t wk, double* e_local, double* e_sum) {
+    if (!wk) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStream_t st = wk->sys->ctx->stream;
+    MeasureOut mo;
+    CK(launch_measure(wk->sys->hs, wk->dw, 0, true, mo, st));
+    if (e_local) CU(cudaMemcpyAsync(e_local, wk->dw.el, 8 * (size_t)wk->dw.W, cudaMemcpyDeviceToHost, st));
+    if (e_sum) CU(cudaMemcpyAsync(e_sum, wk->dw.partial + wk->dw.partial_cap - 1, 8, cudaMemcpyDeviceToHost, st));
+    if (e_local || e_sum) CU(cudaStreamSynchronize(st));
+    return QMC_OK;
+}
+
+int qmc_walkers_sweep(qmc_walkers_t wk, int move_kind, int n_sweeps, uint64_t step0, double step, double tau,
+                      double max_drift, uint64_t seed, long long* accepted) {
+    if (!wk || n_sweeps < 0 || move_kind < 0 || move_kind > 3) return QMC_ERR_ARG;
+    if ((move_kind == QMC_MOVE_ONE_DRIFT) && !(tau > 0 && max_drift > 0)) return QMC_ERR_ARG;
+    if (move_kind != QMC_MOVE_ONE_DRIFT && !(step > 0)) return QMC_ERR_ARG;
+    if (n_sweeps == 0) { if (accepted) *accepted = 0; return QMC_OK; }
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStream_t st = wk->sys->ctx->stream;
+    if (accepted) CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+    CK(launch_sweep(wk->sys->hs, wk->dw, move_kind, n_sweeps, step0, step, tau, max_drift, seed, st));
+    if (accepted) {
+        unsigned long long a = 0;
+        CU(cudaMemcpyAsync(&a, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        *accepted = (long long)a;
+    }
+    return QMC_OK;
+}
+
+int qmc_walkers_get_state(qmc_walkers_t wk, double* logabs, int* sign, double* e_local) {
+    if (!wk) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStream_t st = wk->sys->ctx->stream;
+    size_t W = wk->dw.W;
+    if (logabs) CU(cudaMemcpyAsync(logabs, wk->dw.logabs, 8 * W, cudaMemcpyDeviceToHost, st));
+    if (sign) CU(cudaMemcpyAsync(sign, wk->dw.sign, 4 * W, cudaMemcpyDeviceToHost, st));
+    if (e_local) CU(cudaMemcpyAsync(e_local, wk->dw.el, 8 * W, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return QMC_OK;
+}
+
+int qmc_walkers_status(qmc_walkers_t wk, int* flags) {
+    if (!wk || !flags) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    cudaStream_t st = wk->sys->ctx->stream;
+    int f = 0;
+    CU(cudaMemcpyAsync(&f, wk->dw.flags, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemsetAsync(wk->dw.flags, 0, 4, st));
+    CU(cudaStreamSynchronize(st));
+    *flags = f;
+    return QMC_OK;
+}
+
+int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies) {
+    if (!s || !p || !res) return QMC_ERR_ARG;
+    if (p->n_walkers <= 0 || p->n_steps <= 0 || p->n_burnin < 0 || p->move_kind < 0 || p->move_kind > 3) return QMC_ERR_ARG;
+    std::memset(res, 0, sizeof(*res));
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    qmc_walkers_s* wk = nullptr;
+    CK(alloc_walkers(s, p->n_walkers, p->precision, &wk));
+    struct Guard { qmc_walkers_s* w; ~Guard() { if (w) { cudaStreamSynchronize(w->sys->ctx->stream); free_walkers(w); } } } guard{wk};
+    const HostSys& hs = s->hs;
+    CK(launch_init(hs, wk->dw, seed, st));
+    MeasureOut none;
+    CK(launch_measure(hs, wk->dw, 0, true, none, st));
+    std::vector<double> series;
+    long long proposals = 0;
+    CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+    if (p->move_kind == QMC_MOVE_ALL_GAUSS || p->move_kind == QMC_MOVE_ALL_BOX) {
+        if (!(p->step > 0)) return QMC_ERR_ARG;
+        if (p->n_burnin) CK(launch_sweep(hs, wk->dw, p->move_kind, p->n_burnin, 0, p->step, 0, 0, seed, st));
+        CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+        int nblk = (wk->dw.W + 63) / 64;
+        double* d_part = nullptr;
+        double* d_mean = nullptr;
+        CU(cudaMalloc((void**)&d_part, 16 * (size_t)nblk * p->n_steps));
+        cudaError_t e = cudaMalloc((void**)&d_mean, 8 * (size_t)p->n_steps);
+        if (e != cudaSuccess) { cudaFree(d_part); return cuda_rc(e); }
+        int rc = launch_step_all_recorded(hs, wk->dw, p->move_kind, p->n_steps, (uint64_t)p->n_burnin, p->step, seed, d_part, st);
+        if (!rc) rc = launch_sum_partials(d_part, nblk, p->n_steps, d_mean, st);
+        series.resize(p->n_steps);
+        if (!rc) rc = cuda_rc(cudaMemcpyAsync(series.data(), d_mean, 8 * (size_t)p->n_steps, cudaMemcpyDeviceToHost, st));
+        if (!rc) rc = cuda_rc(cudaStreamSynchronize(st));
+        cudaFree(d_part);
+        cudaFree(d_mean);
+        if (rc) return rc;
+        for (double& v : series) v /= (double)wk->dw.W;
+        proposals = (long long)p->n_steps * wk->dw.W;
+    } else {
+        int every = p->refresh_every > 0 ? p->refresh_every : 1;
+        uint64_t sweep = 0;
+        for (int done = 0; done < p->n_burnin; done += every) {
+            int n = std::min(every, p->n_burnin - done);
+            CK(launch_sweep(hs, wk->dw, p->move_kind, n, sweep, p->step, p->tau, p->max_drift, seed, st));
+            sweep += n;
+            CK(launch_measure(hs, wk->dw, 0, true, none, st));
+        }
+        CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+        for (int done = 0; done < p->n_steps; done += every) {
+            int n = std::min(every, p->n_steps - done);
+            CK(launch_sweep(hs, wk->dw, p->move_kind, n, sweep, p->step, p->tau, p->max_drift, seed, st));
+            sweep += n;
+            CK(launch_measure(hs, wk->dw, 0, true, none, st));
+            double esum = 0.0;
+            CU(cudaMemcpyAsync(&esum, wk->dw.partial + wk->dw.partial_cap - 1, 8, cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            series.push_back(esum / (double)wk->dw.W);
+            proposals += (long long)n * hs.N * wk->dw.W;
+        }
+    }
+    unsigned long long acc = 0;
+    int flags = 0;
+    CU(cudaMemcpyAsync(&acc, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&flags, wk->dw.flags, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    double mean = 0.0;
+    for (double v : series) mean += v;
+    mean /= (double)series.size();
+    double var = 0.0;
+    for (double v : series) var += (v - mean) * (v - mean);
+    res->energy = mean;
+    res->variance = series.size() ? var / (double)series.size() : 0.0;
+    res->autocorrelation_time = autocorrelation_time(series);
+    res->error = blocking_error(series, res->autocorrelation_time);
+    res->acceptance_rate = proposals ? (double)acc / (double)proposals : 0.0;
+    res->n_samples = (int)series.size();
+    res->status_flags = flags;
+    if (energies) for (size_t i = 0; i < series.size(); ++i) energies[i] = series[i];
+    return QMC_OK;
+}
+
+int qmc_ctx_event_record(qmc_ctx_t c, int slot) {
+    if (!c || slot < 0 || slot >= 16) return QMC_ERR_ARG;
+    CU(cudaEventRecord(c->ev[slot], c->stream));
+    return QMC_OK;
+}
+
+int qmc_ctx_event_elapsed(qmc_ctx_t c, int a, int b, float* ms) {
+    if (!c || a < 0 || a >= 16 || b < 0 || b >= 16 || !ms) return QMC_ERR_ARG;
+    CU(cudaEventSynchronize(c->ev[b]));
+    CU(cudaEventElapsedTime(ms, c->ev[a], c->ev[b]));
+    return QMC_OK;
+}
+
+int qmc_ctx_synchronize(qmc_ctx_t c) {
+    if (!c) return QMC_ERR_ARG;
+    CU(cudaStreamSynchronize(c->stream));
+    return QMC_OK;
+}
+
+int qmc_ctx_flush_l2(qmc_ctx_t c) {
+    if (!c) return QMC_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (!c->flush_buf) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+        c->flush_bytes = std::max<size_t>((size_t)l2 * 2, (size_t)256 << 20);
+        CU(cudaMalloc(&c->flush_buf, c->flush_bytes));
+    }
+    return launch_flush(c->flush_buf, c->flush_bytes, c->stream);
+}
+
+int qmc_ctx_launch_count(qmc_ctx_t c, long long* n) {
+    if (!c || !n) return QMC_ERR_ARG;
+    *n = g_launch_count - c->launches0;
+    return QMC_OK;
+}
+
+int qmc_ctx_measure_peaks(qmc_ctx_t c, double* fp32_tflops, double* fp64_tflops) {
+    if (!c || !fp32_tflops || !fp64_tflops) return QMC_ERR_ARG;
+    cudaSetDevice(c->device);
+    CK(measure_fma_peak(0, fp32_tflops, c->stream));
+    CK(measure_fma_peak(1, fp64_tflops, c->stream));
+    return QMC_OK;
+}
+
+int qmc_host_alloc(size_t bytes, void** out) {
+    if (!out || bytes == 0) return QMC_ERR_ARG;
+    CU(cudaMallocHost(out, bytes));
+    return QMC_OK;
+}
+
+int qmc_host_free(void* p) {
+    if (!p) return QMC_ERR_ARG;
+    CU(cudaFreeHost(p));
+    return QMC_OK;
+}
+
+}  // extern "C"

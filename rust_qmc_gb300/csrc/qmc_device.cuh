@@ -1,0 +1,293 @@
+// qmc_device.cuh -- device-side system tables and the per-walker building
+// blocks of the Slater-Jastrow walker path: counter-based RNG, AO->MO
+// evaluation, Jastrow pair terms, Gauss-Jordan inverse, Sherman-Morrison
+// update.  One thread owns one walker; every per-walker array is indexed with
+// compile-time indices so it stays in registers or in the thread's own
+// shared-memory column.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qmc {
+
+enum { BASIS_GTO = 0, BASIS_STO = 1 };
+enum { JAS_NONE = 0, JAS_PADE_F = 1, JAS_PADE_EEN = 2 };
+enum { MOVE_ALL_GAUSS = 0, MOVE_ALL_BOX = 1, MOVE_ONE_GAUSS = 2, MOVE_ONE_DRIFT = 3 };
+enum { TAG_PROPOSE = 1, TAG_ACCEPT = 2, TAG_INIT = 3, TAG_BRANCH = 4 };
+enum { FLAG_SINGULAR = 1, FLAG_NONFINITE = 2 };
+
+template <int NE_, int NUP_, int NNUC_, int NSH_, int NAO_, int NPRIM_, int BASIS_, int JAS_, int NROT_>
+struct ShapeT {
+    static constexpr int NE = NE_, NUP = NUP_, NDN = NE_ - NUP_, NNUC = NNUC_;
+    static constexpr int NSH = NSH_, NAO = NAO_, NPRIM = NPRIM_, BASIS = BASIS_, JAS = JAS_;
+    static constexpr int NROT = NROT_;
+    static constexpr int NMAX = NUP_ > (NE_ - NUP_) ? NUP_ : (NE_ - NUP_);
+};
+
+// H2 LCAO (src/systems/hydrogen.rs:28-35): 2 Slater 1s AOs, 1 up + 1 down.
+using ShapeH2 = ShapeT<2, 1, 2, 2, 2, 2, BASIS_STO, JAS_PADE_F, 1>;
+// Li atom (src/systems/lithium.rs, src/main.rs:37-48): STO-7G 1s/2s, 2 up + 1 down.
+using ShapeLi = ShapeT<3, 2, 1, 1, 2, 8, BASIS_STO, JAS_PADE_F, 1>;
+// CH4 (src/systems/methane.rs:600-776): up to 17 Gaussian AOs, 5 up + 5 down.
+using ShapeCH4 = ShapeT<10, 5, 5, 12, 17, 28, BASIS_GTO, JAS_PADE_EEN, 4>;
+
+template <class SH, class T>
+struct SysT {
+    T nuc[SH::NNUC][3];
+    T Z[SH::NNUC];
+    T enA[SH::NNUC];          // A_species * Z_I (e-n Jastrow amplitude)
+    T enB[SH::NNUC];          // B_species
+    T Aspec[SH::NNUC];        // A_species (unscaled)
+    int species[SH::NNUC];
+    T F;                      // Pade-F parameter
+    T b_ee[2], a_ee[2];       // [0] antiparallel, [1] parallel
+    T qa;                     // Jastrow2 gradient prefactor quirk (F or 1)
+    int quirk_lap;            // Jastrow2 Laplacian quirk
+    T v_nn;
+    int n_rot;
+    int sh_start[SH::NNUC + 1];
+    int sh_p0[SH::NSH], sh_np[SH::NSH];
+    int sh_s0[SH::NSH], sh_s1[SH::NSH], sh_p[SH::NSH];
+    T pexp[SH::NPRIM];
+    T cs0[SH::NPRIM], cs1[SH::NPRIM], cp[SH::NPRIM];
+    int ppow[SH::NPRIM];
+    T C[2][SH::NAO][SH::NMAX];      // [sector][internal AO][column]
+    T dC[SH::NROT][SH::NAO];        // d phi / d theta rows
+    int rot_col[SH::NROT][2];       // column of the rotated MO in each sector (-1 none)
+    T init_sigma;
+    int init_nuc[SH::NE];           // internal electron order
+    int perm[SH::NE];               // internal -> caller electron index
+};
+
+// ---------------------------------------------------------------------------
+// Math helpers (float paths use the hardware approximations).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ float fexp(float x) { return __expf(x); }
+__device__ __forceinline__ double flog(double x) { return log(x); }
+__device__ __forceinline__ float flog(float x) { return __logf(x); }
+__device__ __forceinline__ double fsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float fsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double frcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float frcp(float x) { return __frcp_rn(x); }
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and the stream layout of include/qmc.h.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+__host__ __device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+        uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+        uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+        uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+        U4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+    }
+    return c;
+}
+__device__ __forceinline__ U4 rng_draw(uint64_t seed, uint32_t walker, uint64_t step, uint32_t sub, uint32_t tag) {
+    U4 c{walker, (uint32_t)step, sub, tag | ((uint32_t)((step >> 32) & 0xFFFFu) << 16)};
+    return philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+__device__ __forceinline__ double to_u01(uint32_t x, double) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+__device__ __forceinline__ float to_u01(uint32_t x, float) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ void bm(uint32_t a, uint32_t b, double& n0, double& n1) {
+    double r = sqrt(-2.0 * log(to_u01(a, 0.0)));
+    double s, c;
+    sincospi(2.0 * to_u01(b, 0.0), &s, &c);
+    n0 = r * c; n1 = r * s;
+}
+__device__ __forceinline__ void bm(uint32_t a, uint32_t b, float& n0, float& n1) {
+    float r = sqrtf(-2.0f * __logf(to_u01(a, 0.0f)));
+    float s, c;
+    __sincosf(6.28318530717958647f * to_u01(b, 0.0f), &s, &c);
+    n0 = r * c; n1 = r * s;
+}
+
+// ---------------------------------------------------------------------------
+// Orbital evaluation: phi_k(r) = sum_a C[sig][a][k] chi_a(r) for the NS
+// columns of sector SIG, optionally with gradients (MODE >= 1) and
+// Laplacians (MODE >= 2), and NR extra rows (rotation derivatives, values).
+// Shells are grouped by nucleus; each shell's primitive exponentials are
+// computed once and shared by its s-type AOs and p triplet
+// (src/systems/methane.rs:498-590 for Gaussians, src/wavefunction/slater.rs:
+// 91-145 for Slater-type radial functions).
+// ---------------------------------------------------------------------------
+template <class SH, class T, int SIG, int MODE, int NR>
+struct MOEval {
+    static constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
+    T v[SH::NMAX], gx[SH::NMAX], gy[SH::NMAX], gz[SH::NMAX], l[SH::NMAX];
+    T dv[NR > 0 ? NR : 1];
+
+    __device__ __forceinline__ void add(const SysT<SH, T>& S, int a, T chi, T ax, T ay, T az, T la) {
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            T c = S.C[SIG][a][k];
+            v[k] += c * chi;
+            if (MODE >= 1) { gx[k] += c * ax; gy[k] += c * ay; gz[k] += c * az; }
+            if (MODE >= 2) l[k] += c * la;
+        }
+#pragma unroll
+        for (int q = 0; q < NR; ++q) dv[q] += S.dC[q][a] * chi;
+    }
+
+    // NUC >= 0 restricts the sum to AOs centred on that nucleus.
+    __device__ __forceinline__ void run(const SysT<SH, T>& S, T x, T y, T z, int only_nuc = -1) {
+#pragma unroll
+        for (int k = 0; k < SH::NMAX; ++k) { v[k] = 0; gx[k] = 0; gy[k] = 0; gz[k] = 0; l[k] = 0; }
+#pragma unroll
+        for (int q = 0; q < (NR > 0 ? NR : 1); ++q) dv[q] = 0;
+#pragma unroll
+        for (int I = 0; I < SH::NNUC; ++I) {
+            if (only_nuc >= 0 && only_nuc != I) continue;
+            T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+            T r2 = dx * dx + dy * dy + dz * dz;
+            for (int sh = S.sh_start[I]; sh < S.sh_start[I + 1]; ++sh) {
+                int p0 = S.sh_p0[sh], p1 = p0 + S.sh_np[sh];
+                if (SH::BASIS == BASIS_GTO) {
+                    T a0 = 0, a1 = 0, ap = 0, b0 = 0, b1 = 0, bp = 0, c0 = 0, c1 = 0, cpp = 0;
+                    for (int p = p0; p < p1; ++p) {
+                        T al = S.pexp[p];
+                        T e = fexp(-al * r2);
+                        T e0 = S.cs0[p] * e, e1 = S.cs1[p] * e, ep = S.cp[p] * e;
+                        a0 += e0; a1 += e1; ap += ep;
+                        if (MODE >= 1) { b0 += al * e0; b1 += al * e1; bp += al * ep; }
+                        if (MODE >= 2) { c0 += al * al * e0; c1 += al * al * e1; cpp += al * al * ep; }
+                    }
+                    int s0 = S.sh_s0[sh], s1 = S.sh_s1[sh], pa = S.sh_p[sh];
+                    if (s0 >= 0) add(S, s0, a0, -2 * b0 * dx, -2 * b0 * dy, -2 * b0 * dz, -6 * b0 + 4 * r2 * c0);
+                    if (s1 >= 0) add(S, s1, a1, -2 * b1 * dx, -2 * b1 * dy, -2 * b1 * dz, -6 * b1 + 4 * r2 * c1);
+                    if (pa >= 0) {
+                        T lp = -10 * bp + 4 * r2 * cpp;
+                        // chi = x_m R(r): grad = x_m (-2 R1 dr) + e_m R0, lap = x_m(-10 R1 + 4 r^2 R2)
+                        add(S, pa + 0, dx * ap, dx * (-2 * bp * dx) + ap, dx * (-2 * bp * dy), dx * (-2 * bp * dz), dx * lp);
+                        add(S, pa + 1, dy * ap, dy * (-2 * bp * dx), dy * (-2 * bp * dy) + ap, dy * (-2 * bp * dz), dy * lp);
+                        add(S, pa + 2, dz * ap, dz * (-2 * bp * dx), dz * (-2 * bp * dy), dz * (-2 * bp * dz) + ap, dz * lp);
+                    }
+                } else {
+                    // Slater-type: R(d) = sum c d^n e^{-zeta d}
+                    T d = fsqrt(r2);
+                    T id = d > 0 ? frcp(d) : T(0);
+                    T v0 = 0, v1 = 0, d0 = 0, d1 = 0, l0 = 0, l1 = 0;
+                    for (int p = p0; p < p1; ++p) {
+                        T zt = S.pexp[p];
+                        int n = S.ppow[p];
+                        T dn = 1;
+                        for (int t = 0; t < n; ++t) dn *= d;
+                        T dn1 = dn * id, dn2 = dn1 * id;
+                        T e = fexp(-zt * d);
+                        T nf = (T)n;
+                        T val = dn * e;
+                        T rd = e * (-zt * dn + nf * dn1);
+                        T lap = e * (zt * zt * dn - 2 * zt * nf * dn1 + nf * (nf - 1) * dn2) + 2 * rd * id;
+                        v0 += S.cs0[p] * val; v1 += S.cs1[p] * val;
+                        d0 += S.cs0[p] * rd;  d1 += S.cs1[p] * rd;
+                        l0 += S.cs0[p] * lap; l1 += S.cs1[p] * lap;
+                    }
+                    int s0 = S.sh_s0[sh], s1 = S.sh_s1[sh];
+                    T ux = dx * id, uy = dy * id, uz = dz * id;
+                    if (d == 0) { l0 = 0; l1 = 0; }
+                    if (s0 >= 0) add(S, s0, v0, d0 * ux, d0 * uy, d0 * uz, l0);
+                    if (s1 >= 0) add(S, s1, v1, d1 * ux, d1 * uy, d1 * uz, l1);
+                }
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Jastrow pair functions.  Returns u, u'(r) and u'' + 2u'/r.
+// PADE_F: u = -F/(2(1+r/F))   (src/correlation/jastrow.rs:30-53, 85-125)
+// PADE_EEN e-e: u = a r/(1+b r); e-n: u = -A r/(1+B r)   (:218-321)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void pade_f(T F, T d, T& u, T& up, T& lt) {
+    T f = 1 + d / F;
+    T inv = frcp(f);
+    u = -F * T(0.5) * inv;
+    up = T(0.5) * inv * inv;
+    lt = d > 0 ? inv * inv * inv / d : T(0);
+}
+template <class T>
+__device__ __forceinline__ void pade_ab(T a, T b, T d, T& u, T& up, T& lt) {
+    T den = 1 + b * d;
+    T inv = frcp(den);
+    u = a * d * inv;
+    up = a * inv * inv;
+    lt = d > 0 ? 2 * a * inv * inv / d - 2 * a * b * inv * inv * inv : T(0);
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inverse with partial pivoting (restates the LU-based
+// determinant/try_inverse the reference calls at src/systems/methane.rs:
+// 828-829).  A is destroyed; Ainv = A^-1.  Row swaps use selects so that
+// all indices stay compile-time.
+// ---------------------------------------------------------------------------
+template <int N, class T>
+__device__ __forceinline__ bool gj_inverse(T (&A)[N][N], T (&Ainv)[N][N], double& logdet, int& sign) {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = 0; j < N; ++j) Ainv[i][j] = (i == j) ? T(1) : T(0);
+    logdet = 0.0;
+    sign = 1;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        int p = k;
+        T best = fabs(A[k][k]);
+#pragma unroll
+        for (int i = k + 1; i < N; ++i) {
+            T a = fabs(A[i][k]);
+            if (a > best) { best = a; p = i; }
+        }
+#pragma unroll
+        for (int i = k + 1; i < N; ++i) {
+            bool sw = (i == p);
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                T a = A[k][j], b = A[i][j];
+                A[k][j] = sw ? b : a; A[i][j] = sw ? a : b;
+                T c = Ainv[k][j], d = Ainv[i][j];
+                Ainv[k][j] = sw ? d : c; Ainv[i][j] = sw ? c : d;
+            }
+        }
+        if (p != k) sign = -sign;
+        T piv = A[k][k];
+        if (!(piv != T(0))) { ok = false; piv = T(1); }
+        if (piv < 0) sign = -sign;
+        logdet += log(fabs((double)piv));
+        T ip = T(1) / piv;
+#pragma unroll
+        for (int j = 0; j < N; ++j) { A[k][j] *= ip; Ainv[k][j] *= ip; }
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            if (i == k) continue;
+            T f = A[i][k];
+#pragma unroll
+            for (int j = 0; j < N; ++j) { A[i][j] -= f * A[k][j]; Ainv[i][j] -= f * Ainv[k][j]; }
+        }
+    }
+    return ok;
+}
+
+// Neumaier-compensated pair (s, c): value = s + c.
+struct Comp { double s, c; };
+__device__ __forceinline__ Comp comp_add(Comp a, Comp b) {
+    double s = a.s + b.s;
+    double e = fabs(a.s) >= fabs(b.s) ? (a.s - s) + b.s : (b.s - s) + a.s;
+    return {s, a.c + b.c + e};
+}
+
+}  // namespace qmc

@@ -1,0 +1,101 @@
+// qmc_internal.h -- host-side representation of a system and the launch
+// interface between the C ABI (qmc_api.cpp) and the CUDA kernels
+// (qmc_kernels.cu).  Not part of the public ABI.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+namespace qmc {
+
+// Kernel shapes compiled into the library.  A shape fixes the electron
+// counts and nucleus count at compile time so per-walker arrays live in
+// registers / shared memory with static indices.
+enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_COUNT = 3 };
+
+// A basis shell: primitives shared by up to two s-type AOs and one p triplet
+// (the SP shells of 6-31G share exponents between 2s and 2p; Li's STO-7G 1s
+// and 2s share exponents and powers).
+struct HostShell {
+    int nuc;
+    std::vector<double> exps;
+    std::vector<int> pows;
+    int s_ao[2] = {-1, -1};              // caller AO index of the s-type AOs
+    std::vector<double> s_coef[2];
+    int p_ao[3] = {-1, -1, -1};          // caller AO index of px, py, pz
+    std::vector<double> p_coef;
+};
+
+struct HostSys {
+    int shape = -1;
+    int N = 0, n_up = 0, n_dn = 0, n_nuc = 0, n_ao = 0, n_mo = 0;
+    std::vector<int> perm;               // internal electron index -> caller index
+    std::vector<int> spins;              // caller order
+    std::vector<double> R;               // [n_nuc*3]
+    std::vector<double> Z;
+    std::vector<int> species;
+    int basis = 0;
+    std::vector<HostShell> shells;       // sorted by nucleus
+    std::vector<int> ao_int;             // caller AO -> internal AO index (shell order)
+    std::vector<double> C0;              // caller MO coefficients [n_mo*n_ao] (caller AO order)
+    std::vector<int> occ;                // caller order
+    int jk = 0;
+    double F = 1.0;
+    double jas[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<int> rot_occ, rot_virt;
+    std::vector<double> rot_angle;
+    int quirks = 0;
+    std::vector<int> init_nuc;           // caller order
+    double init_sigma = 0.5;
+    double v_nn = 0.0;
+
+    int n_params() const { return 8 + (int)rot_occ.size(); }
+    // Effective (rotated) MO coefficients in caller AO order.
+    std::vector<double> effective_mo() const;
+    // d phi_k / d theta_q coefficient rows, one per rotation.
+    std::vector<double> rotation_derivative_rows() const;
+};
+
+// Device-resident walker arrays, structure-of-arrays with stride Wcap.
+struct DevWalkers {
+    int W = 0, Wcap = 0;
+    int prec = 0;                        // 0 FP64, 1 FP32 storage
+    void* pos = nullptr;                 // [N*3][Wcap]
+    void* dinv = nullptr;                // [2][nmax*nmax][Wcap]
+    double* logabs = nullptr;            // [Wcap]
+    int* sign = nullptr;                 // [Wcap]
+    double* el = nullptr;                // [Wcap]
+    int* flags = nullptr;                // [1] status bits (OR)
+    unsigned long long* acc = nullptr;   // [1] accepted-move counter
+    double* partial = nullptr;           // reduction scratch
+    int partial_cap = 0;
+};
+
+struct MeasureOut {
+    double* grad = nullptr;              // [W][N][3] internal order
+    double* lap = nullptr;               // [W][N]
+    double* O = nullptr;                 // [W][P]
+    double* fhf = nullptr;               // [W][n_nuc][3]
+    double* omega = nullptr;             // [W][n_nuc][3]
+};
+
+int nmax_of_shape(int shape);
+
+// Launchers (return a qmc status).  compute_prec: 0 double, 1 float.
+int launch_init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st);
+int launch_measure(const HostSys& hs, DevWalkers& dw, int compute_prec, bool write_state,
+                   const MeasureOut& out, cudaStream_t st);
+int launch_sweep(const HostSys& hs, DevWalkers& dw, int move_kind, int n_sweeps, uint64_t step0,
+                 double step, double tau, double max_drift, uint64_t seed, cudaStream_t st);
+// FP64 compensated sums.  Sums column c of X (row-major [W][ncol]) into
+// out[c]; when `products` is set also out[ncol + ...] = sum of the pairwise
+// products used by the SR matrices (see qmc_kernels.cu).
+int launch_walker_sum(const double* X, int W, int ncol, double* d_out, double* d_scratch,
+                      int scratch_cap, cudaStream_t st);
+int launch_sr_sums(const double* E, const double* O, int W, int P, double* d_out,
+                   double* d_scratch, int scratch_cap, cudaStream_t st);
+int launch_flush(void* buf, size_t bytes, cudaStream_t st);
+
+extern long long g_launch_count;
+
+}  // namespace qmc

@@ -1,0 +1,249 @@
+// qmc_kernels.cu -- shape-independent kernels (walker reductions, L2
+// flush, position scatter/gather) and the dispatch from a system's shape to
+// the per-shape kernel instantiations in qmc_shape_*.cu.
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include "qmc_internal.h"
+#include "qmc_device.cuh"
+
+namespace qmc {
+
+long long g_launch_count = 0;
+
+static int cuda_status(cudaError_t e) {
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "qmc_gb300: CUDA error %s\n", cudaGetErrorString(e));
+        return 2;
+    }
+    return 0;
+}
+
+#define QMC_DECLARE_SHAPE(NAME)                                                                               \
+    int shape_init_##NAME(const HostSys&, DevWalkers&, uint64_t, cudaStream_t);                              \
+    int shape_measure_##NAME(const HostSys&, DevWalkers&, int, bool, const MeasureOut&, cudaStream_t);       \
+    int shape_sweep_one_##NAME(const HostSys&, DevWalkers&, int, int, uint64_t, double, double, double,      \
+                               uint64_t, cudaStream_t);                                                      \
+    int shape_step_all_##NAME(const HostSys&, DevWalkers&, int, int, uint64_t, double, uint64_t, cudaStream_t,\
+                              double*);                                                                      \
+    int shape_nmax_##NAME();
+QMC_DECLARE_SHAPE(h2)
+QMC_DECLARE_SHAPE(li)
+QMC_DECLARE_SHAPE(ch4)
+
+#define QMC_SHAPE_SWITCH(shape, CALL)                  \
+    switch (shape) {                                   \
+        case SHAPE_H2: return CALL(h2);                \
+        case SHAPE_LI: return CALL(li);                \
+        case SHAPE_CH4: return CALL(ch4);              \
+    }                                                  \
+    return 7;
+
+int nmax_of_shape(int shape) {
+#define C_(n) shape_nmax_##n()
+    QMC_SHAPE_SWITCH(shape, C_)
+#undef C_
+}
+
+int launch_init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
+#define C_(n) shape_init_##n(hs, dw, seed, st)
+    QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+}
+
+int launch_measure(const HostSys& hs, DevWalkers& dw, int compute_prec, bool write_state, const MeasureOut& out,
+                   cudaStream_t st) {
+#define C_(n) shape_measure_##n(hs, dw, compute_prec, write_state, out, st)
+    QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+}
+
+int launch_sweep(const HostSys& hs, DevWalkers& dw, int move_kind, int n_sweeps, uint64_t step0, double step,
+                 double tau, double max_drift, uint64_t seed, cudaStream_t st) {
+    if (move_kind == 0 || move_kind == 1) {
+#define C_(n) shape_step_all_##n(hs, dw, move_kind, n_sweeps, step0, step, seed, st, nullptr)
+        QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+    }
+#define C_(n) shape_sweep_one_##n(hs, dw, move_kind, n_sweeps, step0, step, tau, max_drift, seed, st)
+    QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+}
+
+// All-electron steps with per-step E_L partial sums recorded.
+int launch_step_all_recorded(const HostSys& hs, DevWalkers& dw, int move_kind, int n, uint64_t s0, double step,
+                             uint64_t seed, double* partial, cudaStream_t st) {
+    if (move_kind != 0 && move_kind != 1) return 1;
+#define C_(nm) shape_step_all_##nm(hs, dw, move_kind, n, s0, step, seed, st, partial)
+    QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+}
+
+// Final reduction of block partial pairs: out[j] = sum over blocks of
+// partial[j][b] (pairs (s,c)), one thread per row j, fixed order.
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblk, int nrows, double* __restrict__ out) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nrows) return;
+    Comp acc{0.0, 0.0};
+    const double* p = partial + (size_t)j * 2 * nblk;
+    for (int b = 0; b < nblk; ++b) {
+        acc = comp_add(acc, Comp{p[2 * b], 0.0});
+        acc.c += p[2 * b + 1];
+    }
+    out[j] = acc.s + acc.c;
+}
+
+// SR sums: quantity m over the walkers of chunk b, Neumaier-compensated,
+// fixed order.  Quantities: 0 E, 1 E^2, 2..2+P-1 O_p, 2+P..2+2P-1 E O_p,
+// then O_p O_q for p <= q (row-major upper triangle).
+__device__ __forceinline__ double sr_quantity(int m, int P, const double* E, const double* O, int w) {
+    double e = E[w];
+    if (m == 0) return e;
+    if (m == 1) return e * e;
+    if (m < 2 + P) return O[(size_t)w * P + (m - 2)];
+    if (m < 2 + 2 * P) return e * O[(size_t)w * P + (m - 2 - P)];
+    int k = m - 2 - 2 * P;
+    int p = 0;
+    while (k >= P - p) { k -= P - p; ++p; }
+    int q = p + k;
+    return O[(size_t)w * P + p] * O[(size_t)w * P + q];
+}
+
+__global__ void k_sr_partials(const double* __restrict__ E, const double* __restrict__ O, int W, int P, int M,
+                              int chunk, double* __restrict__ partial, int nblk) {
+    int m = threadIdx.x;
+    int b = blockIdx.x;
+    if (m >= M) return;
+    int w0 = b * chunk, w1 = min(W, w0 + chunk);
+    Comp acc{0.0, 0.0};
+    for (int w = w0; w < w1; ++w) acc = comp_add(acc, Comp{sr_quantity(m, P, E, O, w), 0.0});
+    partial[((size_t)m * nblk + b) * 2] = acc.s;
+    partial[((size_t)m * nblk + b) * 2 + 1] = acc.c;
+}
+
+__global__ void k_flush(uint4* buf, size_t n, unsigned v) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) buf[i] = make_uint4(v, v + 1, v + 2, v + 3);
+}
+
+int launch_sr_sums(const double* E, const double* O, int W, int P, double* d_out, double* d_scratch,
+                   int scratch_cap, cudaStream_t st) {
+    int M = 2 + 2 * P + P * (P + 1) / 2;
+    int nblk = std::min(1024, std::max(1, (W + 255) / 256));
+    int chunk = (W + nblk - 1) / nblk;
+    nblk = (W + chunk - 1) / chunk;
+    if ((size_t)2 * M * nblk > (size_t)scratch_cap) return 8;
+    int tpb = ((M + 31) / 32) * 32;
+    if (tpb > 1024) return 1;
+    k_sr_partials<<<nblk, tpb, 0, st>>>(E, O, W, P, M, chunk, d_scratch, nblk);
+    ++g_launch_count;
+    k_sum_partials<<<(M + 127) / 128, 128, 0, st>>>(d_scratch, nblk, M, d_out);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+int launch_walker_sum(const double* X, int W, int ncol, double* d_out, double* d_scratch, int scratch_cap,
+                      cudaStream_t st) {
+    (void)ncol;
+    return launch_sr_sums(X, X, W, 0, d_out, d_scratch, scratch_cap, st);
+}
+
+int launch_flush(void* buf, size_t bytes, cudaStream_t st) {
+    size_t n = bytes / sizeof(uint4);
+    k_flush<<<152 * 8, 256, 0, st>>>((uint4*)buf, n, (unsigned)(g_launch_count & 0xffff));
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+template <class TS>
+__global__ void k_scatter(const double* __restrict__ src, TS* __restrict__ pos, const int* __restrict__ perm, int N,
+                          int W, int Wcap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N * W) return;
+    int ei = i / W, w = i - ei * W;
+    int e = perm[ei];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pos[(size_t)(3 * ei + c) * Wcap + w] = (TS)src[((size_t)w * N + e) * 3 + c];
+}
+
+template <class TS>
+__global__ void k_gather(const TS* __restrict__ pos, double* __restrict__ dst, const int* __restrict__ perm, int N,
+                         int W, int Wcap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N * W) return;
+    int ei = i / W, w = i - ei * W;
+    int e = perm[ei];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dst[((size_t)w * N + e) * 3 + c] = (double)pos[(size_t)(3 * ei + c) * Wcap + w];
+}
+
+int launch_scatter_positions(const double* src, DevWalkers& dw, const int* d_perm, int N, cudaStream_t st) {
+    int n = N * dw.W, tpb = 256;
+    if (dw.prec == 0) k_scatter<double><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(src, (double*)dw.pos, d_perm, N, dw.W, dw.Wcap);
+    else k_scatter<float><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(src, (float*)dw.pos, d_perm, N, dw.W, dw.Wcap);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+int launch_gather_positions(const DevWalkers& dw, double* dst, const int* d_perm, int N, cudaStream_t st) {
+    int n = N * dw.W, tpb = 256;
+    if (dw.prec == 0) k_gather<double><<<(n + tpb - 1) / tpb, tpb, 0, st>>>((const double*)dw.pos, dst, d_perm, N, dw.W, dw.Wcap);
+    else k_gather<float><<<(n + tpb - 1) / tpb, tpb, 0, st>>>((const float*)dw.pos, dst, d_perm, N, dw.W, dw.Wcap);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st) {
+    k_sum_partials<<<(nrows + 127) / 128, 128, 0, st>>>(partial, nblk, nrows, out);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+
+// FMA-chain kernels used to measure the SIMT peaks (roofline denominators for
+// the compute-bound sweep kernels).  8 independent chains per thread.
+template <class T>
+__global__ void k_fma_peak(T* out, int iters, T a, T b) {
+    T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+            x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+        }
+    }
+    T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == T(-1.2345)) out[0] = s;
+}
+
+int measure_fma_peak(int fp64, double* tflops, cudaStream_t st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* out = nullptr;
+    if (cudaMalloc(&out, 16) != cudaSuccess) return 8;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    int blocks = sms * 8, tpb = 256, iters = fp64 ? 64 : 2048;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(a, st);
+        if (fp64) k_fma_peak<double><<<blocks, tpb, 0, st>>>((double*)out, iters, 0.999999, 1e-7);
+        else k_fma_peak<float><<<blocks, tpb, 0, st>>>((float*)out, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+    }
+    g_launch_count += 2;
+    int rc = cuda_status(cudaGetLastError());
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    double flops = 2.0 * 8 * 16 * (double)iters * blocks * tpb;
+    *tflops = ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+    return rc;
+}
+
+}  // namespace qmc

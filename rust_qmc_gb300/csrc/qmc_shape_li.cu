@@ -1,0 +1,8 @@
+// qmc_shape_li.cu -- all kernels for the ShapeLi system shape.
+#include "qmc_walker_kernels.cuh"
+
+namespace qmc {
+QMC_DEFINE_SHAPE_MEASURE(li, ShapeLi)
+QMC_DEFINE_SHAPE_ONE(li, ShapeLi)
+QMC_DEFINE_SHAPE_ALL(li, ShapeLi)
+}  // namespace qmc

@@ -1,0 +1,801 @@
+// qmc_walker_kernels.cuh -- templated CUDA kernels of the walker path
+// (sm_103a), instantiated once per system shape in qmc_shape_*.cu.
+//
+//   k_init       MultiWfn::initialize for every walker (Philox, tag 3)
+//   k_measure    full evaluation from positions: AO->MO, Gauss-Jordan inverse
+//                and log-determinant, Jastrow, grad/Laplacian, E_L, optional
+//                parameter log-derivatives and nuclear forces.  In FP64 it is
+//                the refresh of the FP32 walkers (inverse + E_L every N sweeps)
+//   k_sweep_one  single-electron Metropolis / Langevin sweeps with
+//                Sherman-Morrison inverse updates, n sweeps per launch, walker
+//                state resident in shared memory for the whole launch
+//   k_step_all   all-electron Metropolis steps (H2 path of MCMCSimulation)
+#pragma once
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <vector>
+#include <algorithm>
+#include "qmc_internal.h"
+#include "qmc_device.cuh"
+
+namespace qmc {
+
+
+// ---------------------------------------------------------------------------
+// Host: fill the device table of a shape from the host description.
+// ---------------------------------------------------------------------------
+template <class SH, class T>
+static bool fill_sys(const HostSys& hs, SysT<SH, T>& S) {
+    std::memset(&S, 0, sizeof(S));
+    if (hs.N != SH::NE || hs.n_up != SH::NUP || hs.n_nuc != SH::NNUC) return false;
+    if ((int)hs.shells.size() > SH::NSH || hs.n_ao > SH::NAO || (int)hs.rot_occ.size() > SH::NROT) return false;
+    for (int I = 0; I < SH::NNUC; ++I) {
+        for (int c = 0; c < 3; ++c) S.nuc[I][c] = (T)hs.R[3 * I + c];
+        S.Z[I] = (T)hs.Z[I];
+        int sp = hs.species[I];
+        S.species[I] = sp;
+        S.Aspec[I] = (T)hs.jas[6 + sp];
+        S.enA[I] = (T)(hs.jas[6 + sp] * hs.Z[I]);
+        S.enB[I] = (T)hs.jas[4 + sp];
+    }
+    S.F = (T)hs.F;
+    S.b_ee[0] = (T)hs.jas[0]; S.b_ee[1] = (T)hs.jas[1];
+    S.a_ee[0] = (T)hs.jas[2]; S.a_ee[1] = (T)hs.jas[3];
+    S.qa = (hs.quirks & 1) ? (T)hs.F : (T)1;
+    S.quirk_lap = (hs.quirks & 2) ? 1 : 0;
+    S.v_nn = (T)hs.v_nn;
+    S.n_rot = (int)hs.rot_occ.size();
+    // shells (already sorted by nucleus)
+    int np = 0;
+    for (int I = 0; I <= SH::NNUC; ++I) S.sh_start[I] = 0;
+    for (size_t s = 0; s < hs.shells.size(); ++s) {
+        const HostShell& h = hs.shells[s];
+        S.sh_start[h.nuc + 1]++;
+        if (np + (int)h.exps.size() > SH::NPRIM) return false;
+        S.sh_p0[s] = np;
+        S.sh_np[s] = (int)h.exps.size();
+        S.sh_s0[s] = h.s_ao[0] >= 0 ? hs.ao_int[h.s_ao[0]] : -1;
+        S.sh_s1[s] = h.s_ao[1] >= 0 ? hs.ao_int[h.s_ao[1]] : -1;
+        S.sh_p[s] = h.p_ao[0] >= 0 ? hs.ao_int[h.p_ao[0]] : -1;
+        for (size_t p = 0; p < h.exps.size(); ++p) {
+            S.pexp[np] = (T)h.exps[p];
+            S.ppow[np] = h.pows.empty() ? 0 : h.pows[p];
+            S.cs0[np] = h.s_ao[0] >= 0 ? (T)h.s_coef[0][p] : (T)0;
+            S.cs1[np] = h.s_ao[1] >= 0 ? (T)h.s_coef[1][p] : (T)0;
+            S.cp[np] = h.p_ao[0] >= 0 ? (T)h.p_coef[p] : (T)0;
+            ++np;
+        }
+    }
+    for (int I = 0; I < SH::NNUC; ++I) S.sh_start[I + 1] += S.sh_start[I];
+    // MO columns per sector, internal AO order
+    std::vector<double> Ce = hs.effective_mo();
+    for (int sig = 0; sig < 2; ++sig) {
+        int col = 0;
+        for (int ei = 0; ei < hs.N; ++ei) {
+            int e = hs.perm[ei];
+            if ((hs.spins[e] > 0) != (sig == 0)) continue;
+            int k = hs.occ[e];
+            for (int a = 0; a < hs.n_ao; ++a) S.C[sig][hs.ao_int[a]][col] = (T)Ce[(size_t)k * hs.n_ao + a];
+            ++col;
+        }
+    }
+    std::vector<double> dC = hs.rotation_derivative_rows();
+    for (size_t q = 0; q < hs.rot_occ.size(); ++q) {
+        for (int a = 0; a < hs.n_ao; ++a) S.dC[q][hs.ao_int[a]] = (T)dC[q * hs.n_ao + a];
+        for (int sig = 0; sig < 2; ++sig) {
+            S.rot_col[q][sig] = -1;
+            int col = 0;
+            for (int ei = 0; ei < hs.N; ++ei) {
+                int e = hs.perm[ei];
+                if ((hs.spins[e] > 0) != (sig == 0)) continue;
+                if (hs.occ[e] == hs.rot_occ[q]) S.rot_col[q][sig] = col;
+                ++col;
+            }
+        }
+    }
+    S.init_sigma = (T)hs.init_sigma;
+    for (int ei = 0; ei < hs.N; ++ei) {
+        S.perm[ei] = hs.perm[ei];
+        S.init_nuc[ei] = hs.init_nuc[hs.perm[ei]];
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Jastrow sums for one electron e against all others (+ nuclei): u and,
+// with GRAD, grad_e u.  `pos(j, c)` returns coordinate c of electron j.
+// ---------------------------------------------------------------------------
+template <class SH, class T, int SIG, bool GRAD, class PosFn>
+__device__ __forceinline__ T jastrow_point(const SysT<SH, T>& S, PosFn pos, int e, T x, T y, T z,
+                                           T& gx, T& gy, T& gz) {
+    T u = 0;
+    gx = 0; gy = 0; gz = 0;
+    if (SH::JAS == JAS_NONE) return u;
+#pragma unroll
+    for (int j = 0; j < SH::NE; ++j) {
+        if (j == e) continue;
+        const bool para = ((j < SH::NUP) == (SIG == 0));
+        T dx = x - pos(j, 0), dy = y - pos(j, 1), dz = z - pos(j, 2);
+        T d = fsqrt(dx * dx + dy * dy + dz * dz);
+        T uu, up, lt;
+        if (SH::JAS == JAS_PADE_F) pade_f(S.F, d, uu, up, lt);
+        else pade_ab(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], d, uu, up, lt);
+        u += uu;
+        if (GRAD) {
+            T f = d > 0 ? up / d : T(0);
+            gx += f * dx; gy += f * dy; gz += f * dz;
+        }
+    }
+    if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+        for (int I = 0; I < SH::NNUC; ++I) {
+            T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+            T d = fsqrt(dx * dx + dy * dy + dz * dz);
+            T uu, up, lt;
+            pade_ab(S.enA[I], S.enB[I], d, uu, up, lt);
+            u -= uu;
+            if (GRAD) {
+                T f = d > 0 ? up / d : T(0);
+                gx -= f * dx; gy -= f * dy; gz -= f * dz;
+            }
+        }
+    }
+    if (GRAD) { gx *= S.qa; gy *= S.qa; gz *= S.qa; }
+    return u;
+}
+
+// ---------------------------------------------------------------------------
+// Full evaluation of one configuration in precision TC.
+// ---------------------------------------------------------------------------
+template <class SH, class TC, int NR>
+struct FullEval {
+    double logabs;
+    int sign;
+    bool ok;
+    TC el;
+    TC gx[SH::NE], gy[SH::NE], gz[SH::NE], lap[SH::NE];   // grad psi/psi, lap psi/psi
+    TC O[8 + (NR > 0 ? NR : 1)];
+};
+
+template <class SH, class TC, int SIG, int NR, class DinvStore>
+__device__ __forceinline__ void eval_sector(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3], double& logdet,
+                                            int& sg, bool& ok, TC (&gdx)[SH::NE], TC (&gdy)[SH::NE],
+                                            TC (&gdz)[SH::NE], TC (&ld)[SH::NE], TC* Orot,
+                                            DinvStore store, TC* omega) {
+    constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
+    if (NS == 0) return;
+    constexpr int NSa = NS > 0 ? NS : 1;
+    TC D[NSa][NSa], Gx[NSa][NSa], Gy[NSa][NSa], Gz[NSa][NSa], L[NSa][NSa];
+    TC dvr[NSa][NR > 0 ? NR : 1];
+#pragma unroll 1
+    for (int q = 0; q < NS; ++q) {
+        const int e = SIG * SH::NUP + q;
+        MOEval<SH, TC, SIG, 2, NR> m;
+        m.run(S, r[e][0], r[e][1], r[e][2]);
+#pragma unroll
+        for (int k = 0; k < NS; ++k) { D[q][k] = m.v[k]; Gx[q][k] = m.gx[k]; Gy[q][k] = m.gy[k]; Gz[q][k] = m.gz[k]; L[q][k] = m.l[k]; }
+#pragma unroll
+        for (int qq = 0; qq < NR; ++qq) dvr[q][qq] = m.dv[qq];
+    }
+    TC Di[NSa][NSa];
+    double lg;
+    int s;
+    ok = gj_inverse<NSa, TC>(D, Di, lg, s) && ok;
+    logdet += lg;
+    sg *= s;
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+#pragma unroll
+        for (int j = 0; j < NS; ++j) store(SIG, k, j, Di[k][j]);
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        const int e = SIG * SH::NUP + q;
+        TC ax = 0, ay = 0, az = 0, al = 0;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            TC w = Di[k][q];
+            ax += Gx[q][k] * w; ay += Gy[q][k] * w; az += Gz[q][k] * w; al += L[q][k] * w;
+        }
+        gdx[e] = ax; gdy[e] = ay; gdz[e] = az; ld[e] = al;
+    }
+    if (NR > 0 && Orot) {
+#pragma unroll
+        for (int qq = 0; qq < NR; ++qq) {
+            if (qq >= S.n_rot) continue;
+            int c = S.rot_col[qq][SIG];
+            TC acc = 0;
+#pragma unroll
+            for (int cc = 0; cc < NS; ++cc) {
+                if (cc != c) continue;
+#pragma unroll
+                for (int row = 0; row < NS; ++row) acc += Di[cc][row] * dvr[row][qq];
+            }
+            Orot[qq] += acc;
+        }
+    }
+    if (omega) {
+        // d ln|D| / dR_I = -sum_rows sum_k Dinv[k][row] sum_{a on I} C[k][a] grad chi_a(r_row)
+#pragma unroll 1
+        for (int q = 0; q < NS; ++q) {
+            const int e = SIG * SH::NUP + q;
+#pragma unroll
+            for (int I = 0; I < SH::NNUC; ++I) {
+                MOEval<SH, TC, SIG, 1, 0> m;
+                m.run(S, r[e][0], r[e][1], r[e][2], I);
+                TC ox = 0, oy = 0, oz = 0;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) { ox += Di[k][q] * m.gx[k]; oy += Di[k][q] * m.gy[k]; oz += Di[k][q] * m.gz[k]; }
+                omega[3 * I] -= ox; omega[3 * I + 1] -= oy; omega[3 * I + 2] -= oz;
+            }
+        }
+    }
+}
+
+// Jastrow over all pairs: u, grad_i u (true gradient), sum_j (u''+2u'/r),
+// sum_j u'^2 (for the per-pair Laplacian quirk), and parameter derivatives.
+template <class SH, class TC, bool WANT_O>
+__device__ __forceinline__ TC jastrow_full(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3], TC (&gx)[SH::NE],
+                                           TC (&gy)[SH::NE], TC (&gz)[SH::NE], TC (&lu)[SH::NE],
+                                           TC (&gsq)[SH::NE], TC* O) {
+    TC u = 0;
+#pragma unroll
+    for (int i = 0; i < SH::NE; ++i) { gx[i] = 0; gy[i] = 0; gz[i] = 0; lu[i] = 0; gsq[i] = 0; }
+    if (SH::JAS == JAS_NONE) return u;
+#pragma unroll
+    for (int i = 0; i < SH::NE; ++i)
+#pragma unroll
+        for (int j = i + 1; j < SH::NE; ++j) {
+            const bool para = ((i < SH::NUP) == (j < SH::NUP));
+            TC dx = r[i][0] - r[j][0], dy = r[i][1] - r[j][1], dz = r[i][2] - r[j][2];
+            TC d = fsqrt(dx * dx + dy * dy + dz * dz);
+            TC uu, up, lt;
+            const int c = para ? 1 : 0;
+            if (SH::JAS == JAS_PADE_F) pade_f(S.F, d, uu, up, lt);
+            else pade_ab(S.a_ee[c], S.b_ee[c], d, uu, up, lt);
+            u += uu;
+            bool skip = (SH::JAS == JAS_PADE_EEN) ? (d < TC(1e-10)) : (d == TC(0));
+            if (!skip) {
+                TC f = up / d;
+                gx[i] += f * dx; gy[i] += f * dy; gz[i] += f * dz;
+                gx[j] -= f * dx; gy[j] -= f * dy; gz[j] -= f * dz;
+                lu[i] += lt; lu[j] += lt;
+                gsq[i] += up * up; gsq[j] += up * up;
+            }
+            if (WANT_O && SH::JAS == JAS_PADE_EEN) {
+                TC den = 1 + S.b_ee[c] * d;
+                O[c] += -S.a_ee[c] * d * d / (den * den);
+                O[2 + c] += d / den;
+            }
+        }
+    if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+        for (int i = 0; i < SH::NE; ++i)
+#pragma unroll
+            for (int I = 0; I < SH::NNUC; ++I) {
+                TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
+                TC d = fsqrt(dx * dx + dy * dy + dz * dz);
+                TC uu, up, lt;
+                pade_ab(S.enA[I], S.enB[I], d, uu, up, lt);
+                u -= uu;
+                if (!(d < TC(1e-10))) {
+                    TC f = up / d;
+                    gx[i] -= f * dx; gy[i] -= f * dy; gz[i] -= f * dz;
+                    lu[i] -= lt;
+                }
+                if (WANT_O) {
+                    TC den = 1 + S.enB[I] * d;
+                    TC dB = S.Aspec[I] * S.Z[I] * d * d / (den * den);
+                    TC dA = -S.Z[I] * d / den;
+                    if (S.species[I] == 0) { O[4] += dB; O[6] += dA; }
+                    else { O[5] += dB; O[7] += dA; }
+                }
+            }
+    }
+    return u;
+}
+
+template <class SH, class TC>
+__device__ __forceinline__ TC potential(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3]) {
+    TC v = 0;
+#pragma unroll
+    for (int i = 0; i < SH::NE; ++i) {
+#pragma unroll
+        for (int I = 0; I < SH::NNUC; ++I) {
+            TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
+            v -= S.Z[I] / fsqrt(dx * dx + dy * dy + dz * dz);
+        }
+#pragma unroll
+        for (int j = i + 1; j < SH::NE; ++j) {
+            TC dx = r[i][0] - r[j][0], dy = r[i][1] - r[j][1], dz = r[i][2] - r[j][2];
+            v += TC(1) / fsqrt(dx * dx + dy * dy + dz * dz);
+        }
+    }
+    return v + S.v_nn;
+}
+
+template <class SH, class TC, int NR, class DinvStore>
+__device__ __forceinline__ void evaluate_config(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3],
+                                                FullEval<SH, TC, NR>& out, bool want_o, DinvStore store,
+                                                TC* omega) {
+    TC gjx[SH::NE], gjy[SH::NE], gjz[SH::NE], lu[SH::NE], gsq[SH::NE];
+#pragma unroll
+    for (int p = 0; p < 8 + (NR > 0 ? NR : 1); ++p) out.O[p] = 0;
+    TC u;
+    if (NR > 0 || want_o) u = jastrow_full<SH, TC, true>(S, r, gjx, gjy, gjz, lu, gsq, out.O);
+    else u = jastrow_full<SH, TC, false>(S, r, gjx, gjy, gjz, lu, gsq, out.O);
+    TC gdx[SH::NE], gdy[SH::NE], gdz[SH::NE], ld[SH::NE];
+    double logdet = 0.0;
+    int sg = 1;
+    bool ok = true;
+    eval_sector<SH, TC, 0, NR>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega);
+    eval_sector<SH, TC, 1, NR>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega);
+    TC kin = 0;
+#pragma unroll
+    for (int e = 0; e < SH::NE; ++e) {
+        TC ax = S.qa * gjx[e], ay = S.qa * gjy[e], az = S.qa * gjz[e];
+        TC lj = S.quirk_lap ? (lu[e] + gsq[e]) : (lu[e] + gjx[e] * gjx[e] + gjy[e] * gjy[e] + gjz[e] * gjz[e]);
+        TC lp = ld[e] + 2 * (gdx[e] * ax + gdy[e] * ay + gdz[e] * az) + lj;
+        out.gx[e] = gdx[e] + ax; out.gy[e] = gdy[e] + ay; out.gz[e] = gdz[e] + az;
+        out.lap[e] = lp;
+        kin += lp;
+    }
+    out.el = TC(-0.5) * kin + potential(S, r);
+    out.logabs = logdet + (double)u;
+    out.sign = sg;
+    out.ok = ok;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+template <class SH, class TS>
+__global__ void k_init(const __grid_constant__ SysT<SH, double> S, TS* __restrict__ pos, int W, int Wcap,
+                       uint64_t seed) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+#pragma unroll
+    for (int e = 0; e < SH::NE; ++e) {
+        U4 x = rng_draw(seed, (uint32_t)w, 0, (uint32_t)S.perm[e], TAG_INIT);
+        double n0, n1, n2, n3;
+        bm(x.x, x.y, n0, n1);
+        bm(x.z, x.w, n2, n3);
+        int c = S.init_nuc[e];
+        double cx = c >= 0 ? S.nuc[c][0] : 0.0, cy = c >= 0 ? S.nuc[c][1] : 0.0, cz = c >= 0 ? S.nuc[c][2] : 0.0;
+        pos[(3 * e + 0) * (size_t)Wcap + w] = (TS)(cx + S.init_sigma * n0);
+        pos[(3 * e + 1) * (size_t)Wcap + w] = (TS)(cy + S.init_sigma * n1);
+        pos[(3 * e + 2) * (size_t)Wcap + w] = (TS)(cz + S.init_sigma * n2);
+    }
+}
+
+template <int TPB>
+__device__ __forceinline__ void block_partial(double v, double* partial, int* flags) {
+    __shared__ double ss[TPB], sc[TPB];
+    ss[threadIdx.x] = v;
+    sc[threadIdx.x] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int o = TPB / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            Comp a{ss[threadIdx.x], sc[threadIdx.x]}, b{ss[threadIdx.x + o], sc[threadIdx.x + o]};
+            Comp c = comp_add(a, b);
+            ss[threadIdx.x] = c.s;
+            sc[threadIdx.x] = c.c;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { partial[2 * blockIdx.x] = ss[0]; partial[2 * blockIdx.x + 1] = sc[0]; }
+}
+
+template <class SH, class TC, class TS, int TPB, int NR>
+__global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH, TC> S,
+                                                 const TS* __restrict__ pos, TS* __restrict__ dinv,
+                                                 double* __restrict__ logabs, int* __restrict__ sign,
+                                                 double* __restrict__ el, int W, int Wcap, int write_state,
+                                                 MeasureOut out, int P, double* partial, int* flags) {
+    const int w = blockIdx.x * TPB + threadIdx.x;
+    const bool act = w < W;
+    TC r[SH::NE][3];
+#pragma unroll
+    for (int e = 0; e < SH::NE; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[e][c] = act ? (TC)pos[(3 * e + c) * (size_t)Wcap + w] : TC(e + 1) * TC(0.37 + c);
+    constexpr int NM = SH::NMAX;
+    auto store = [&](int sig, int k, int j, TC v) {
+        if (act && write_state) dinv[((size_t)(sig * NM * NM + k * NM + j)) * Wcap + w] = (TS)v;
+    };
+    TC omega[3 * SH::NNUC];
+#pragma unroll
+    for (int i = 0; i < 3 * SH::NNUC; ++i) omega[i] = 0;
+    FullEval<SH, TC, NR> ev;
+    evaluate_config<SH, TC, NR>(S, r, ev, out.O != nullptr, store, (act && out.omega) ? omega : (TC*)nullptr);
+    double e_l = (double)ev.el;
+    if (act) {
+        int fl = 0;
+        if (!ev.ok) fl |= FLAG_SINGULAR;
+        if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
+        if (fl) atomicOr(flags, fl);
+        if (write_state) { logabs[w] = ev.logabs; sign[w] = ev.sign; el[w] = e_l; }
+        if (out.grad) {
+#pragma unroll
+            for (int e = 0; e < SH::NE; ++e) {
+                out.grad[((size_t)w * SH::NE + e) * 3 + 0] = ev.gx[e];
+                out.grad[((size_t)w * SH::NE + e) * 3 + 1] = ev.gy[e];
+                out.grad[((size_t)w * SH::NE + e) * 3 + 2] = ev.gz[e];
+            }
+        }
+        if (out.lap) {
+#pragma unroll
+            for (int e = 0; e < SH::NE; ++e) out.lap[(size_t)w * SH::NE + e] = ev.lap[e];
+        }
+        if (out.O) {
+            for (int p = 0; p < P; ++p) out.O[(size_t)w * P + p] = ev.O[p];
+        }
+        if (out.fhf) {
+#pragma unroll
+            for (int I = 0; I < SH::NNUC; ++I) {
+                TC fx = 0, fy = 0, fz = 0;
+#pragma unroll
+                for (int i = 0; i < SH::NE; ++i) {
+                    TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
+                    TC d = fsqrt(dx * dx + dy * dy + dz * dz);
+                    if (d > TC(1e-10)) { TC f = S.Z[I] / (d * d * d); fx += f * dx; fy += f * dy; fz += f * dz; }
+                }
+#pragma unroll
+                for (int J = 0; J < SH::NNUC; ++J) {
+                    if (J == I) continue;
+                    TC dx = S.nuc[I][0] - S.nuc[J][0], dy = S.nuc[I][1] - S.nuc[J][1], dz = S.nuc[I][2] - S.nuc[J][2];
+                    TC d = fsqrt(dx * dx + dy * dy + dz * dz);
+                    if (d > TC(1e-10)) { TC f = S.Z[I] * S.Z[J] / (d * d * d); fx -= f * dx; fy -= f * dy; fz -= f * dz; }
+                }
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 0] = fx;
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 1] = fy;
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 2] = fz;
+            }
+        }
+        if (out.omega) {
+            if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+                for (int I = 0; I < SH::NNUC; ++I)
+#pragma unroll
+                    for (int i = 0; i < SH::NE; ++i) {
+                        TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
+                        TC d = fsqrt(dx * dx + dy * dy + dz * dz);
+                        if (d < TC(1e-10)) continue;
+                        TC den = 1 + S.enB[I] * d;
+                        TC f = S.enA[I] / (d * den * den);
+                        omega[3 * I] += f * dx; omega[3 * I + 1] += f * dy; omega[3 * I + 2] += f * dz;
+                    }
+            }
+#pragma unroll
+            for (int i = 0; i < 3 * SH::NNUC; ++i) out.omega[(size_t)w * 3 * SH::NNUC + i] = omega[i];
+        }
+    }
+    if (partial) block_partial<TPB>(act ? e_l : 0.0, partial, flags);
+}
+
+// Single-electron sweeps.  Shared memory holds the block's walkers as
+// structure-of-arrays columns: positions [3 NE][TPB], inverse Slater
+// matrices [2][NMAX^2][TPB]; each thread only touches its own column, so no
+// barrier is needed.
+template <class SH, class T, int SIG, int MOVE, int TPB>
+__device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, int t, uint32_t w, uint64_t st,
+                                             uint64_t seed, T step, T tau, T maxd, int& sgn, unsigned& acc,
+                                             int& flg) {
+    constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
+    constexpr int NM = SH::NMAX;
+    auto P = [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; };
+#define DI(k, j) sd[((SIG * NM * NM) + (k) * NM + (j)) * TPB + t]
+    for (int q = 0; q < NS; ++q) {
+        const int e = SIG * SH::NUP + q;
+        T rx = P(e, 0), ry = P(e, 1), rz = P(e, 2);
+        U4 x = rng_draw(seed, w, st, (uint32_t)e, TAG_PROPOSE);
+        T n0, n1, n2, n3;
+        bm(x.x, x.y, n0, n1);
+        bm(x.z, x.w, n2, n3);
+        T nx, ny, nz, dlx = 0, dly = 0, dlz = 0;
+        T gjx, gjy, gjz;
+        T u_old;
+        if (MOVE == MOVE_ONE_DRIFT) {
+            MOEval<SH, T, SIG, 1, 0> mc;
+            mc.run(S, rx, ry, rz);
+            T ax = 0, ay = 0, az = 0;
+#pragma unroll
+            for (int k = 0; k < NS; ++k) { T d = DI(k, q); ax += mc.gx[k] * d; ay += mc.gy[k] * d; az += mc.gz[k] * d; }
+            u_old = jastrow_point<SH, T, SIG, true>(S, P, e, rx, ry, rz, gjx, gjy, gjz);
+            T Fx = 2 * (ax + gjx), Fy = 2 * (ay + gjy), Fz = 2 * (az + gjz);
+            dlx = tau * Fx; dly = tau * Fy; dlz = tau * Fz;
+            T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
+            if (m > maxd) { T s = maxd / m; dlx *= s; dly *= s; dlz *= s; }
+            T sd2 = fsqrt(2 * tau);
+            nx = rx + dlx + sd2 * n0; ny = ry + dly + sd2 * n1; nz = rz + dlz + sd2 * n2;
+        } else {
+            u_old = jastrow_point<SH, T, SIG, false>(S, P, e, rx, ry, rz, gjx, gjy, gjz);
+            nx = rx + step * n0; ny = ry + step * n1; nz = rz + step * n2;
+        }
+        MOEval<SH, T, SIG, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0, 0> mn;
+        mn.run(S, nx, ny, nz);
+        T R = 0;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) R += mn.v[k] * DI(k, q);
+        T u_new = jastrow_point<SH, T, SIG, MOVE == MOVE_ONE_DRIFT>(S, P, e, nx, ny, nz, gjx, gjy, gjz);
+        T logG = 0;
+        if (MOVE == MOVE_ONE_DRIFT) {
+            T ax = 0, ay = 0, az = 0;
+#pragma unroll
+            for (int k = 0; k < NS; ++k) { T d = DI(k, q); ax += mn.gx[k] * d; ay += mn.gy[k] * d; az += mn.gz[k] * d; }
+            T iR = R != T(0) ? T(1) / R : T(0);
+            T Fx = 2 * (ax * iR + gjx), Fy = 2 * (ay * iR + gjy), Fz = 2 * (az * iR + gjz);
+            T bx = tau * Fx, by = tau * Fy, bz = tau * Fz;
+            T m = fsqrt(bx * bx + by * by + bz * bz);
+            if (m > maxd) { T s = maxd / m; bx *= s; by *= s; bz *= s; }
+            T fx = nx - rx - dlx, fy = ny - ry - dly, fz = nz - rz - dlz;
+            T qx = rx - nx - bx, qy = ry - ny - by, qz = rz - nz - bz;
+            logG = ((fx * fx + fy * fy + fz * fz) - (qx * qx + qy * qy + qz * qz)) / (4 * tau);
+        }
+        T ratio = R * fexp(u_new - u_old);
+        T prob = ratio * ratio;
+        if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
+        U4 a = rng_draw(seed, w, st, (uint32_t)e, TAG_ACCEPT);
+        T uacc = to_u01(a.x, T(0));
+        if (prob != prob) flg |= FLAG_NONFINITE;
+        if (uacc < prob && R != T(0)) {
+            sp[(3 * e + 0) * TPB + t] = nx;
+            sp[(3 * e + 1) * TPB + t] = ny;
+            sp[(3 * e + 2) * TPB + t] = nz;
+            T iR = T(1) / R;
+            T cq[NM];
+#pragma unroll
+            for (int k = 0; k < NS; ++k) cq[k] = DI(k, q) * iR;
+#pragma unroll
+            for (int j = 0; j < NS; ++j) {
+                T tj = 0;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) tj += mn.v[k] * DI(k, j);
+#pragma unroll
+                for (int k = 0; k < NS; ++k) DI(k, j) -= cq[k] * tj;
+            }
+#pragma unroll
+            for (int k = 0; k < NS; ++k) DI(k, q) = cq[k];
+            if (R < 0) sgn = -sgn;
+            ++acc;
+        }
+    }
+#undef DI
+}
+
+template <class SH, class T, int MOVE, int TPB>
+__global__ void __launch_bounds__(TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
+                                                   T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
+                                                   int n_sweeps, uint64_t step0, T step, T tau, T maxd,
+                                                   uint64_t seed, unsigned long long* acc_out, int* flags) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    constexpr int NM = SH::NMAX;
+    T* sp = reinterpret_cast<T*>(smraw);
+    T* sd = sp + 3 * SH::NE * TPB;
+    const int t = threadIdx.x;
+    const int w = blockIdx.x * TPB + t;
+    if (w >= W) return;
+#pragma unroll
+    for (int i = 0; i < 3 * SH::NE; ++i) sp[i * TPB + t] = gpos[(size_t)i * Wcap + w];
+#pragma unroll
+    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = gdinv[(size_t)i * Wcap + w];
+    int sgn = gsign[w];
+    unsigned acc = 0;
+    int flg = 0;
+    for (int it = 0; it < n_sweeps; ++it) {
+        uint64_t st = step0 + (uint64_t)it;
+        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, sgn, acc, flg);
+        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, sgn, acc, flg);
+    }
+#pragma unroll
+    for (int i = 0; i < 3 * SH::NE; ++i) gpos[(size_t)i * Wcap + w] = sp[i * TPB + t];
+#pragma unroll
+    for (int i = 0; i < 2 * NM * NM; ++i) gdinv[(size_t)i * Wcap + w] = sd[i * TPB + t];
+    gsign[w] = sgn;
+    if (acc) atomicAdd(acc_out, (unsigned long long)acc);
+    if (flg) atomicOr(flags, flg);
+}
+
+// All-electron Metropolis steps (src/sampling/vmc.rs:95-119): every step
+// proposes all electrons, evaluates psi and E_L at the proposal from scratch,
+// accepts with min(1, psi'^2/psi^2).  Per-step block partial sums of E_L
+// (Neumaier pairs) are written to partial[step][block] when requested.
+template <class SH, class T, int MOVE, int TPB>
+__global__ void __launch_bounds__(TPB) k_step_all(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
+                                                  double* __restrict__ glog, int* __restrict__ gsign,
+                                                  double* __restrict__ gel, int W, int Wcap, int n_steps,
+                                                  uint64_t step0, T step, uint64_t seed,
+                                                  unsigned long long* acc_out, double* partial, int nblk,
+                                                  int* flags) {
+    const int t = threadIdx.x;
+    const int w = blockIdx.x * TPB + t;
+    const bool act = w < W;
+    T r[SH::NE][3];
+#pragma unroll
+    for (int e = 0; e < SH::NE; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[e][c] = act ? gpos[(size_t)(3 * e + c) * Wcap + w] : T(e + 1) * T(0.37 + c);
+    double lp = act ? glog[w] : 0.0;
+    int sg = act ? gsign[w] : 1;
+    double el = act ? gel[w] : 0.0;
+    unsigned acc = 0;
+    int flg = 0;
+    auto nostore = [](int, int, int, T) {};
+    for (int it = 0; it < n_steps; ++it) {
+        uint64_t st = step0 + (uint64_t)it;
+        T rn[SH::NE][3];
+#pragma unroll
+        for (int e = 0; e < SH::NE; ++e) {
+            U4 x = rng_draw(seed, (uint32_t)w, st, (uint32_t)e, TAG_PROPOSE);
+            if (MOVE == MOVE_ALL_GAUSS) {
+                T n0, n1, n2, n3;
+                bm(x.x, x.y, n0, n1);
+                bm(x.z, x.w, n2, n3);
+                rn[e][0] = r[e][0] + step * n0; rn[e][1] = r[e][1] + step * n1; rn[e][2] = r[e][2] + step * n2;
+            } else {
+                rn[e][0] = r[e][0] + step * (to_u01(x.x, T(0)) - T(0.5));
+                rn[e][1] = r[e][1] + step * (to_u01(x.y, T(0)) - T(0.5));
+                rn[e][2] = r[e][2] + step * (to_u01(x.z, T(0)) - T(0.5));
+            }
+        }
+        FullEval<SH, T, 0> ev;
+        evaluate_config<SH, T, 0>(S, rn, ev, false, nostore, (T*)nullptr);
+        U4 a = rng_draw(seed, (uint32_t)w, st, 0, TAG_ACCEPT);
+        double prob = exp(2.0 * (ev.logabs - lp));
+        bool accept = act && ev.ok && (to_u01(a.x, 0.0) < prob);
+        if (accept) {
+#pragma unroll
+            for (int e = 0; e < SH::NE; ++e)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) r[e][c] = rn[e][c];
+            lp = ev.logabs;
+            sg = ev.sign;
+            el = (double)ev.el;
+            ++acc;
+            if (!isfinite(el)) flg |= FLAG_NONFINITE;
+        }
+        if (partial) block_partial<TPB>(act ? el : 0.0, partial + (size_t)it * 2 * nblk, flags);
+    }
+    if (act) {
+#pragma unroll
+        for (int e = 0; e < SH::NE; ++e)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) gpos[(size_t)(3 * e + c) * Wcap + w] = r[e][c];
+        glog[w] = lp;
+        gsign[w] = sg;
+        gel[w] = el;
+        atomicAdd(acc_out, (unsigned long long)acc);
+        if (flg) atomicOr(flags, flg);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-shape launchers (instantiated by QMC_DEFINE_SHAPE in qmc_shape_*.cu).
+// ---------------------------------------------------------------------------
+static inline int cuda_status(cudaError_t e) {
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "qmc_gb300: CUDA error %s\n", cudaGetErrorString(e));
+        return 2;
+    }
+    return 0;
+}
+
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+
+template <class SH>
+struct ShapeOps {
+    static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
+        SysT<SH, double> S;
+        if (!fill_sys(hs, S)) return 7;
+        int tpb = 128, nb = (dw.W + tpb - 1) / tpb;
+        if (dw.prec == 0) k_init<SH, double><<<nb, tpb, 0, st>>>(S, (double*)dw.pos, dw.W, dw.Wcap, seed);
+        else k_init<SH, float><<<nb, tpb, 0, st>>>(S, (float*)dw.pos, dw.W, dw.Wcap, seed);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
+    template <class TC, class TS, int NR>
+    static int measure2(const HostSys& hs, DevWalkers& dw, bool write_state, const MeasureOut& out, cudaStream_t st) {
+        SysT<SH, TC> S;
+        if (!fill_sys(hs, S)) return 7;
+        constexpr int TPB = 64;
+        int nb = (dw.W + TPB - 1) / TPB;
+        double* partial = nullptr;
+        if (write_state && dw.partial && dw.partial_cap >= 2 * nb + 1) partial = dw.partial;
+        k_measure<SH, TC, TS, TPB, NR><<<nb, TPB, 0, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign,
+                                                            dw.el, dw.W, dw.Wcap, write_state ? 1 : 0, out,
+                                                            hs.n_params(), partial, dw.flags);
+        ++g_launch_count;
+        int rc = cuda_status(cudaGetLastError());
+        if (rc || !partial) return rc;
+        return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
+    }
+
+    static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
+        if (out.O) {
+            if (SH::JAS != JAS_PADE_EEN || cp != 0 || dw.prec != 0) return 7;
+            return measure2<double, double, SH::NROT>(hs, dw, ws, out, st);
+        }
+        if (cp == 0) {
+            if (dw.prec == 0) return measure2<double, double, 0>(hs, dw, ws, out, st);
+            return measure2<double, float, 0>(hs, dw, ws, out, st);
+        }
+        if (dw.prec == 1) return measure2<float, float, 0>(hs, dw, ws, out, st);
+        return 7;
+    }
+
+    template <class T, int MOVE>
+    static int sweep_one(const HostSys& hs, DevWalkers& dw, int n, uint64_t s0, double step, double tau, double maxd,
+                         uint64_t seed, cudaStream_t st) {
+        SysT<SH, T> S;
+        if (!fill_sys(hs, S)) return 7;
+        constexpr int TPB = sizeof(T) == 4 ? 128 : 64;
+        size_t smem = sizeof(T) * TPB * (3 * SH::NE + 2 * SH::NMAX * SH::NMAX);
+        auto kern = k_sweep_one<SH, T, MOVE, TPB>;
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr_set = true;
+        }
+        int nb = (dw.W + TPB - 1) / TPB;
+        kern<<<nb, TPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W, dw.Wcap, n, s0, (T)step, (T)tau,
+                                    (T)maxd, seed, dw.acc, dw.flags);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
+    template <class T, int MOVE>
+    static int step_all(const HostSys& hs, DevWalkers& dw, int n, uint64_t s0, double step, uint64_t seed,
+                        cudaStream_t st, double* partial) {
+        SysT<SH, T> S;
+        if (!fill_sys(hs, S)) return 7;
+        constexpr int TPB = 64;
+        int nb = (dw.W + TPB - 1) / TPB;
+        k_step_all<SH, T, MOVE, TPB><<<nb, TPB, 0, st>>>(S, (T*)dw.pos, dw.logabs, dw.sign, dw.el, dw.W, dw.Wcap, n,
+                                                          s0, (T)step, seed, dw.acc, partial, nb, dw.flags);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
+    template <bool ALL>
+    static int sweep_part(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,
+                          double maxd, uint64_t seed, cudaStream_t st, double* partial) {
+        bool all = (mk == MOVE_ALL_GAUSS || mk == MOVE_ALL_BOX);
+        if (all != ALL) return 1;
+        if (ALL) {
+            if (dw.prec == 0) return mk == MOVE_ALL_BOX ? step_all<double, MOVE_ALL_BOX>(hs, dw, n, s0, step, seed, st, partial)
+                                                        : step_all<double, MOVE_ALL_GAUSS>(hs, dw, n, s0, step, seed, st, partial);
+            return mk == MOVE_ALL_BOX ? step_all<float, MOVE_ALL_BOX>(hs, dw, n, s0, step, seed, st, partial)
+                                      : step_all<float, MOVE_ALL_GAUSS>(hs, dw, n, s0, step, seed, st, partial);
+        }
+        if (dw.prec == 0) return mk == MOVE_ONE_DRIFT ? sweep_one<double, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                                      : sweep_one<double, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st);
+        return mk == MOVE_ONE_DRIFT ? sweep_one<float, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                    : sweep_one<float, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st);
+    }
+};
+
+#define QMC_DEFINE_SHAPE_MEASURE(NAME, SHAPE)                                                                  \
+    int shape_init_##NAME(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {               \
+        return ShapeOps<SHAPE>::init(hs, dw, seed, st);                                                       \
+    }                                                                                                         \
+    int shape_measure_##NAME(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out,       \
+                             cudaStream_t st) {                                                               \
+        return ShapeOps<SHAPE>::measure(hs, dw, cp, ws, out, st);                                             \
+    }                                                                                                         \
+    int shape_nmax_##NAME() { return SHAPE::NMAX; }
+
+#define QMC_DEFINE_SHAPE_ONE(NAME, SHAPE)                                                                      \
+    int shape_sweep_one_##NAME(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step,   \
+                               double tau, double maxd, uint64_t seed, cudaStream_t st) {                     \
+        return ShapeOps<SHAPE>::template sweep_part<false>(hs, dw, mk, n, s0, step, tau, maxd, seed, st, nullptr);                 \
+    }
+
+#define QMC_DEFINE_SHAPE_ALL(NAME, SHAPE)                                                                      \
+    int shape_step_all_##NAME(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step,    \
+                              uint64_t seed, cudaStream_t st, double* partial) {                              \
+        return ShapeOps<SHAPE>::template sweep_part<true>(hs, dw, mk, n, s0, step, 0.0, 0.0, seed, st, partial);                  \
+    }
+
+}  // namespace qmc

@@ -1,0 +1,88 @@
+"""CPU tests of the C ABI library: it builds, loads, exports every symbol
+include/qmc.h declares, validates system descriptions on the host, and
+reports the absence of a GPU as an error instead of falling back."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import rust_qmc_gb300 as Q
+from rust_qmc_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "qmc.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(qmc_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_expected_surface():
+    names = header_functions()
+    for n in ["qmc_init", "qmc_system_create", "qmc_eval_batch", "qmc_logderiv_batch", "qmc_forces_batch",
+              "qmc_walkers_sweep", "qmc_walkers_refresh", "qmc_vmc_run"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(qmc_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", L.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\s[TW]\s+(\w+)$", out, re.M))
+    missing = [n for n in header_functions() if n not in exported]
+    assert not missing, missing
+    # and the ctypes prototypes cover the same set
+    assert set(header_functions()) == set(L.PROTOTYPES), set(header_functions()) ^ set(L.PROTOTYPES)
+
+
+def test_status_strings(qmc_lib):
+    assert qmc_lib.qmc_version() >= 100
+    for code in range(9):
+        assert qmc_lib.qmc_status_string(code)
+    assert b"unknown" in qmc_lib.qmc_status_string(99)
+
+
+@pytest.mark.parametrize("builder,shape", [(lambda: Q.h2_mo(), 0), (lambda: Q.lithium_atom(), 1),
+                                           (lambda: Q.methane_gto(), 2), (lambda: Q.methane_minimal(), 2)])
+def test_system_check_maps_shapes(qmc_lib, builder, shape):
+    spec = builder()
+    d = spec.desc()
+    got = C.c_int(-9)
+    assert qmc_lib.qmc_system_check(C.byref(d), C.byref(got)) == L.QMC_OK
+    assert got.value == shape
+
+
+def test_system_check_rejects_bad_descriptions(qmc_lib):
+    spec = Q.methane_minimal()
+    bad = spec.copy()
+    bad.spins = np.array([1] * 5 + [2] * 5, np.int32)
+    assert qmc_lib.qmc_system_check(C.byref(bad.desc()), None) == L.QMC_ERR_ARG
+    bad = spec.copy()
+    bad.occ = np.array([0, 1, 2, 3, 99] * 2, np.int32)
+    assert qmc_lib.qmc_system_check(C.byref(bad.desc()), None) == L.QMC_ERR_ARG
+    bad = spec.copy()
+    bad.ao_m = bad.ao_m.copy()
+    bad.ao_m[3] = 0  # p triplet no longer complete
+    assert qmc_lib.qmc_system_check(C.byref(bad.desc()), None) == L.QMC_ERR_ARG
+    # an electron count with no compiled kernel is unsupported, not an error
+    odd = Q.h2_mo()
+    odd.spins = np.array([1, 1], np.int32)
+    assert qmc_lib.qmc_system_check(C.byref(odd.desc()), None) == L.QMC_ERR_UNSUPPORTED
+    assert qmc_lib.qmc_system_check(None, None) == L.QMC_ERR_ARG
+
+
+def _gpu_visible():
+    try:
+        return subprocess.run(["nvidia-smi", "-L"], capture_output=True, timeout=20).returncode == 0
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_gpu_visible(), reason="a GPU is present; covered by the gpu tests")
+def test_no_gpu_is_an_error_not_a_fallback(qmc_lib):
+    h = C.c_void_p()
+    assert qmc_lib.qmc_init(0, C.byref(h)) == L.QMC_ERR_CUDA
+    assert not h.value
+    with pytest.raises(Q.QMCError):
+        Q.Context(0)

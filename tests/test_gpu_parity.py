@@ -1,0 +1,236 @@
+"""GPU parity of the CUDA walker path against the FP64 oracle, through the C ABI.
+
+Tolerances (stated per test):
+  * FP64 kernels vs oracle: 1e-10 relative on log|psi|, drift, Laplacian,
+    E_L (absolute 1e-10 * max(1, |E_L|)).
+  * FP32 working precision vs oracle: E_L measured by the FP64 refresh of
+    FP32 walkers must be within 1e-6 Ha of the oracle at the same (float)
+    configuration.
+  * Trajectories: the counter-based Philox stream makes FP64 GPU sweeps and
+    the oracle's reference-algorithm sweeps follow the same chain; positions
+    agree to 1e-9 and accepted-move counts exactly.
+"""
+import numpy as np
+import pytest
+
+import rust_qmc_gb300 as Q
+from rust_qmc_gb300 import _lib as L
+from tests.helpers import random_configs
+
+pytestmark = pytest.mark.gpu
+
+BUILDERS = {
+    "h2": lambda: Q.h2_mo(),
+    "li_ref": lambda: Q.lithium_atom(reference_quirks=True),
+    "li_fixed": lambda: Q.lithium_atom(reference_quirks=False),
+    "ch4_gto": lambda: Q.methane_gto(),
+    "ch4_min": lambda: Q.methane_minimal(),
+}
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b)))
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_eval_batch_fp64_matches_oracle(ctx, oracle, name):
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 257, seed=1)
+    g = sysh.eval_batch(cfg, L.QMC_FP64)
+    o = oracle.evaluate(spec, cfg)
+    assert np.array_equal(g["sign"], o["sign"])
+    assert rel(g["logabs"], o["logabs"]) < 1e-10
+    assert rel(g["grad"], o["grad"]) < 1e-10
+    assert rel(g["lap"], o["lap"]) < 1e-10
+    assert rel(g["e_local"], o["e_local"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["h2", "li_ref", "ch4_gto", "ch4_min"])
+def test_eval_batch_fp32_close_to_oracle(ctx, oracle, name):
+    """The single-precision evaluation used by moving walkers: ratios and
+    drift to ~1e-4 relative (FP32 orbitals near carbon cores lose digits)."""
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 128, seed=2).astype(np.float32).astype(np.float64)
+    g = sysh.eval_batch(cfg, L.QMC_FP32_REFINE)
+    o = oracle.evaluate(spec, cfg)
+    assert np.mean(g["sign"] == o["sign"]) > 0.98
+    ok = g["sign"] == o["sign"]
+    assert np.median(np.abs(g["logabs"] - o["logabs"])[ok]) < 1e-4
+    assert np.median(np.abs(g["e_local"] - o["e_local"]) / np.maximum(1, np.abs(o["e_local"]))) < 1e-3
+
+
+@pytest.mark.parametrize("precision", [L.QMC_FP64, L.QMC_FP32_REFINE])
+def test_init_matches_oracle(ctx, oracle, precision):
+    spec = Q.methane_minimal()
+    sysh = Q.System(ctx, spec)
+    wk = Q.Walkers(sysh, 300, precision)
+    wk.init(seed=1234)
+    got = wk.get_positions()
+    want = oracle.init_positions(spec, 300, seed=1234)
+    if precision == L.QMC_FP32_REFINE:
+        want = want.astype(np.float32).astype(np.float64)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 if precision == L.QMC_FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("name", ["ch4_min", "ch4_gto", "li_ref"])
+def test_fp32_walkers_refresh_energy_within_1e6(ctx, oracle, name):
+    """FP32 walkers after sweeps: the FP64 refresh E_L equals the oracle's
+    E_L of the same (float) configuration to <= 1e-6 Ha."""
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    W = 512
+    wk = Q.Walkers(sysh, W, L.QMC_FP32_REFINE)
+    wk.init(seed=77)
+    wk.refresh()
+    wk.sweep(L.QMC_MOVE_ONE_GAUSS, 16, 0, seed=5, step=0.3)
+    _, el = wk.refresh(want_energies=True)
+    pos = wk.get_positions()
+    o = oracle.evaluate(spec, pos)
+    err = np.abs(el - o["e_local"])
+    assert np.max(err) <= 1e-6, np.max(err)
+
+
+@pytest.mark.parametrize("name,move", [("ch4_min", L.QMC_MOVE_ONE_GAUSS), ("ch4_min", L.QMC_MOVE_ONE_DRIFT),
+                                       ("ch4_gto", L.QMC_MOVE_ONE_DRIFT), ("li_ref", L.QMC_MOVE_ONE_GAUSS),
+                                       ("li_ref", L.QMC_MOVE_ONE_DRIFT), ("h2", L.QMC_MOVE_ONE_GAUSS)])
+def test_fp64_single_electron_trajectory_matches_oracle(ctx, oracle, name, move):
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    W, n = 64, 4
+    wk = Q.Walkers(sysh, W, L.QMC_FP64)
+    wk.init(seed=31)
+    wk.refresh()
+    pos0 = wk.get_positions()
+    acc = wk.sweep(move, n, 10, seed=4242, step=0.3, tau=0.02, max_drift=1.0)
+    got = wk.get_positions()
+    want, acc_o, _ = oracle.sweeps(spec, pos0, n, 10, move, 4242, step=0.3, tau=0.02, max_drift=1.0,
+                                   want_energy=False)
+    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
+    assert same.mean() >= 0.98, same.mean()
+    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))
+    assert acc > 0
+
+
+@pytest.mark.parametrize("move", [L.QMC_MOVE_ALL_BOX, L.QMC_MOVE_ALL_GAUSS])
+def test_fp64_all_electron_trajectory_matches_oracle(ctx, oracle, move):
+    spec = Q.h2_mo()
+    sysh = Q.System(ctx, spec)
+    W, n = 128, 20
+    wk = Q.Walkers(sysh, W, L.QMC_FP64)
+    wk.init(seed=8)
+    wk.refresh()
+    pos0 = wk.get_positions()
+    acc = wk.sweep(move, n, 0, seed=99, step=1.0)
+    got = wk.get_positions()
+    want, acc_o, el_o = oracle.sweeps(spec, pos0, n, 0, move, 99, step=1.0)
+    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
+    assert same.mean() >= 0.98
+    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))
+    _, _, el = wk.state()
+    np.testing.assert_allclose(el[same], el_o[same], rtol=1e-10, atol=1e-10)
+
+
+def test_refresh_restores_inverse_after_long_fp32_run(ctx, oracle):
+    """Sherman-Morrison drift in FP32 over 64 sweeps stays small enough that
+    acceptance matches the FP64 chain statistically, and the refresh E_L is
+    the oracle's."""
+    spec = Q.methane_minimal()
+    sysh = Q.System(ctx, spec)
+    W = 4096
+    wk = Q.Walkers(sysh, W, L.QMC_FP32_REFINE)
+    wk.init(seed=3)
+    wk.refresh()
+    acc = wk.sweep(L.QMC_MOVE_ONE_GAUSS, 64, 0, seed=17, step=0.3)
+    assert 0.2 < acc / (64 * 10 * W) < 0.95
+    s, el = wk.refresh(want_energies=True)
+    assert np.all(np.isfinite(el))
+    assert abs(s - el.sum()) < 1e-6 * max(1.0, abs(s))
+    assert wk.status() & 1 == 0
+
+
+@pytest.mark.parametrize("name", ["ch4_min", "ch4_gto"])
+def test_logderiv_batch_matches_oracle(ctx, oracle, name):
+    spec = BUILDERS[name]()
+    if name == "ch4_min":
+        spec = spec.with_params(np.concatenate([spec.jas, [0.1, -0.2, 0.05, 0.3]]))
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 1000, seed=6)
+    O, E, S, f, em = sysh.logderiv_batch(cfg, sums=True)
+    Oo = oracle.log_derivatives(spec, cfg)
+    Eo = oracle.evaluate(spec, cfg)["e_local"]
+    assert rel(O, Oo) < 1e-10
+    assert rel(E, Eo) < 1e-10
+    n = len(E)
+    Om = Oo.mean(0)
+    S_ref = Oo.T @ Oo / n - np.outer(Om, Om)
+    f_ref = (Eo[:, None] * Oo).mean(0) - Eo.mean() * Om
+    np.testing.assert_allclose(S, S_ref, rtol=1e-9, atol=1e-9 * np.abs(S_ref).max())
+    np.testing.assert_allclose(f, f_ref, rtol=1e-8, atol=1e-8 * np.abs(f_ref).max())
+    assert abs(em - Eo.mean()) < 1e-9 * max(1, abs(em))
+
+
+@pytest.mark.parametrize("name", ["h2", "ch4_min", "ch4_gto"])
+def test_forces_match_oracle_and_fd(ctx, oracle, name):
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 64, seed=12)
+    F, Om = sysh.forces_batch(cfg)
+    Fo, Omo = oracle.forces(spec, cfg)
+    assert rel(F, Fo) < 1e-10
+    assert rel(Om, Omo) < 1e-10
+    fd = oracle.nuclear_gradient_fd(spec, cfg[:8], h=1e-5)
+    np.testing.assert_allclose(Om[:8], fd, rtol=1e-5, atol=1e-6)
+
+
+def test_trait_surface_single_configuration(ctx, oracle):
+    """MultiWfn/EnergyCalculator/OptimizableWfn/ForceCalculator methods with
+    the reference's value conventions (psi, grad psi, lap psi)."""
+    spec = Q.methane_gto()
+    sysh = Q.System(ctx, spec)
+    r = random_configs(spec, 1, seed=40)[0]
+    o = oracle.evaluate(spec, r)
+    psi = o["sign"][0] * np.exp(o["logabs"][0])
+    assert abs(sysh.evaluate(r) - psi) <= 1e-10 * abs(psi)
+    np.testing.assert_allclose(sysh.derivative(r), o["grad"][0] * psi, rtol=1e-9, atol=1e-12 * abs(psi))
+    np.testing.assert_allclose(sysh.laplacian(r), o["lap"][0] * psi, rtol=1e-9, atol=1e-12 * abs(psi))
+    assert abs(sysh.local_energy(r) - o["e_local"][0]) < 1e-9
+    p = sysh.get_params()
+    p2 = p.copy()
+    p2[0] += 0.1
+    sysh.set_params(p2)
+    assert np.allclose(sysh.get_params(), p2)
+    assert abs(sysh.local_energy(r) - oracle.evaluate(spec.with_params(p2), r)["e_local"][0]) < 1e-9
+    R = spec.nuc_pos.copy()
+    R[1] += 0.05
+    sysh.set_nuclei(R)
+    o2 = oracle.evaluate(spec.with_params(p2).with_nuclei(R), r)
+    assert abs(sysh.local_energy(r) - o2["e_local"][0]) < 1e-9
+    with pytest.raises(Q.QMCError):
+        sysh.set_params(np.zeros(3))
+
+
+def test_vmc_run_h2_box_moves(ctx):
+    """MCMCSimulation on H2 (all-electron uniform box of 1.0 bohr): energy
+    in the LCAO-Jastrow range and the error bar from blocking."""
+    sysh = Q.System(ctx, Q.h2_mo())
+    r = Q.vmc_run(sysh, n_walkers=1024, n_steps=400, n_burnin=100, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0,
+                  seed=5)
+    assert -1.20 < r["energy"] < -1.10, r
+    assert 0 < r["error"] < 0.01
+    assert 0.3 < r["acceptance_rate"] < 0.95
+    assert r["n_samples"] == 400
+
+
+def test_vmc_run_precisions_agree_ch4(ctx):
+    """FP32+refine and FP64 chains give statistically indistinguishable
+    energies (combined 4 sigma)."""
+    sysh = Q.System(ctx, Q.methane_minimal())
+    res = {}
+    for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
+        res[prec] = Q.vmc_run(sysh, n_walkers=8192, n_steps=256, n_burnin=64, move_kind=L.QMC_MOVE_ONE_GAUSS,
+                              step=0.3, precision=prec, refresh_every=8, seed=11 + prec)
+    a, b = res[L.QMC_FP64], res[L.QMC_FP32_REFINE]
+    sig = np.hypot(max(a["error"], 1e-6), max(b["error"], 1e-6))
+    assert abs(a["energy"] - b["energy"]) < 4 * sig + 1e-3 * abs(a["energy"]), (a, b)

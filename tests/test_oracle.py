@@ -1,0 +1,199 @@
+"""CPU checks that pin the oracle to the reference.
+
+The reference (a Rust crate) cannot be built here, so the oracle is pinned by
+the reference's own golden scalars, its finite-difference self-consistency
+tests, its range checks, and the published Philox known-answer vectors.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import rust_qmc_gb300 as Q
+from tests.helpers import fd_grad_lap, random_configs
+
+
+# Philox4x32-10 known-answer vectors (Random123 distribution, kat_vectors).
+KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,want", KAT)
+def test_philox_known_answers(oracle, ctr, key, want):
+    assert oracle.philox(ctr, key) == want
+    assert Q.philox4x32(ctr, key) == want
+
+
+def test_descriptor_layout_matches_abi(oracle):
+    import ctypes
+    assert oracle.lib().orc_desc_size() == ctypes.sizeof(Q._lib.SystemDesc)
+
+
+def test_jastrow1_golden(oracle):
+    # src/lib.rs:31-56: Jastrow1(F=1) at r1=0, r2=(1,0,0)
+    spec = Q.h2_mo(F=1.0)
+    r = np.array([[0.0, 0, 0], [1.0, 0, 0]])
+    J, g, _ = oracle.jastrow(spec, r)
+    assert abs(J - 0.7788007831) < 1e-8
+    assert abs(g[0, 0] - (-0.09735009789)) < 1e-6 and abs(g[1, 0] - 0.09735009789) < 1e-6
+    assert np.all(np.abs(g[:, 1:]) < 1e-12)
+
+
+def test_jastrow1_symmetry_translation(oracle):
+    # src/lib.rs:69-85
+    spec = Q.h2_mo(F=1.0)
+    r = np.array([[0.5, 0.5, 0.5], [-0.5, -0.5, -0.5]])
+    J1, g, _ = oracle.jastrow(spec, r)
+    J2, _, _ = oracle.jastrow(spec, r[::-1].copy())
+    assert abs(J1 - J2) < 1e-12
+    assert np.linalg.norm(g[0] + g[1]) < 1e-12
+
+
+@pytest.mark.parametrize("builder", ["h2", "li_fixed", "ch4_gto", "ch4_min"])
+def test_oracle_analytic_vs_fd(oracle, builder):
+    """Analytic gradient/Laplacian vs central differences (src/lib.rs:88-267,
+    src/systems/methane.rs:1310-1337), on seeded configurations."""
+    spec = {"h2": lambda: Q.h2_mo(), "li_fixed": lambda: Q.lithium_atom(reference_quirks=False),
+            "ch4_gto": lambda: Q.methane_gto(), "ch4_min": lambda: Q.methane_minimal()}[builder]()
+    cfgs = random_configs(spec, 3, seed=11)
+    ev = oracle.evaluate(spec, cfgs)
+    for w in range(3):
+        g, l = fd_grad_lap(oracle, spec, cfgs[w], h=2e-5)
+        np.testing.assert_allclose(ev["grad"][w], g, rtol=1e-5, atol=1e-5 * (1 + np.abs(g).max()))
+        np.testing.assert_allclose(ev["lap"][w], l, rtol=1e-3, atol=1e-3 * (1 + np.abs(l).max()))
+
+
+def test_lithium_quirks_reproduce_reference_formulas(oracle):
+    """With the Jastrow2 quirks on, grad J2 / J2 carries F/(2(1+r/F)^2 r) per
+    pair (src/correlation/jastrow.rs:102) and lap J2 / J2 the per-pair sum
+    without cross terms (:110-125)."""
+    spec = Q.lithium_atom(F=2.0, reference_quirks=True)
+    r = random_configs(spec, 1, seed=5)[0]
+    J, g, l = oracle.jastrow(spec, r)
+    F = 2.0
+    gw = np.zeros((3, 3))
+    lw = np.zeros(3)
+    u = 0.0
+    for i in range(3):
+        for j in range(i + 1, 3):
+            rij = r[i] - r[j]
+            d = np.linalg.norm(rij)
+            f = 1 + d / F
+            u += -F / (2 * f)
+            gi = F / (2 * f * f * d) * rij
+            gw[i] += gi
+            gw[j] -= gi
+            comp = (2 * f * f) ** -2 + 1 / (d * f ** 3)
+            lw[i] += comp
+            lw[j] += comp
+    assert abs(J - math.exp(u)) < 1e-14
+    np.testing.assert_allclose(g, J * gw, rtol=1e-12)
+    np.testing.assert_allclose(l, J * lw, rtol=1e-12)
+
+
+@pytest.mark.parametrize("builder", ["ch4_gto", "ch4_min"])
+def test_log_derivatives_vs_fd(oracle, builder):
+    """O_p = d ln|psi| / dp vs central differences (src/systems/methane.rs:
+    1340-1373), all 8 Jastrow parameters and the MO-rotation angles."""
+    spec = Q.methane_gto(2.0, 3.0) if builder == "ch4_gto" else Q.methane_minimal()
+    if builder == "ch4_min":
+        spec = spec.with_params(np.concatenate([spec.jas, [0.1, -0.2, 0.05, 0.3]]))
+    r = random_configs(spec, 2, seed=3)
+    O = oracle.log_derivatives(spec, r)
+    p0 = spec.params()
+    h = 1e-5
+    for k in range(spec.n_params):
+        pp, pm = p0.copy(), p0.copy()
+        pp[k] += h
+        pm[k] -= h
+        lp = oracle.evaluate(spec.with_params(pp), r)["logabs"]
+        lm = oracle.evaluate(spec.with_params(pm), r)["logabs"]
+        fd = (lp - lm) / (2 * h)
+        np.testing.assert_allclose(O[:, k], fd, rtol=1e-6, atol=1e-7)
+
+
+def test_reference_four_parameter_derivatives(oracle):
+    """MethaneGTO's d_ln_j_d_{bee,ben,a_anti,a_para} (src/correlation/
+    jastrow.rs:326-391) are sums of the generalised derivatives, checked by FD
+    with b_anti=b_para and B0=B1 tied as in the reference."""
+    spec = Q.methane_gto(2.0, 3.0)
+    r = random_configs(spec, 1, seed=9)
+    O = oracle.log_derivatives(spec, r)[0]
+    ref4 = [O[0] + O[1], O[4] + O[5], O[2], O[3]]
+    p = Q.reference_params_from_general(spec.params())
+    h = 1e-5
+    for k in range(4):
+        pp, pm = list(p), list(p)
+        pp[k] += h
+        pm[k] -= h
+        sp = spec.with_params(Q.jastrow3_params(pp[0], pp[1], pp[2], pp[3]))
+        sm = spec.with_params(Q.jastrow3_params(pm[0], pm[1], pm[2], pm[3]))
+        fd = (oracle.evaluate(sp, r)["logabs"][0] - oracle.evaluate(sm, r)["logabs"][0]) / (2 * h)
+        assert abs(ref4[k] - fd) <= 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("builder", ["h2", "ch4_gto", "ch4_min"])
+def test_nuclear_gradient_vs_fd(oracle, builder):
+    """Analytic d ln|psi| / dR_I (src/systems/methane.rs:1007-1101) vs the FD
+    form of src/systems/hydrogen.rs:260-290."""
+    spec = {"h2": lambda: Q.h2_mo(), "ch4_gto": lambda: Q.methane_gto(), "ch4_min": lambda: Q.methane_minimal()}[builder]()
+    r = random_configs(spec, 2, seed=21)
+    _, Om = oracle.forces(spec, r)
+    fd = oracle.nuclear_gradient_fd(spec, r, h=1e-5)
+    np.testing.assert_allclose(Om, fd, rtol=1e-5, atol=1e-6)
+
+
+def test_hf_force_sum_rule(oracle):
+    """HF forces (src/systems/methane.rs:1241-1272): the nuclear-nuclear part
+    is antisymmetric, so sum_I F_I equals the total electron-nucleus pull."""
+    spec = Q.methane_gto()
+    r = random_configs(spec, 1, seed=4)
+    F, _ = oracle.forces(spec, r)
+    tot = np.zeros(3)
+    for I in range(spec.n_nuc):
+        for i in range(spec.n_elec):
+            d = r[0, i] - spec.nuc_pos[I]
+            tot += spec.nuc_charge[I] * d / np.linalg.norm(d) ** 3
+    np.testing.assert_allclose(F[0].sum(axis=0), tot, rtol=1e-12, atol=1e-12)
+
+
+def test_methane_ranges():
+    """src/systems/methane.rs:1284-1307: C-H 2.05 bohr, tetrahedral, V_nn in (10, 20)."""
+    spec = Q.methane_gto()
+    R = spec.nuc_pos
+    for h in range(1, 5):
+        assert abs(np.linalg.norm(R[h] - R[0]) - 2.05) < 1e-12
+    hh = [np.linalg.norm(R[i] - R[j]) for i in range(1, 5) for j in range(i + 1, 5)]
+    assert max(hh) - min(hh) < 1e-12
+    assert 10.0 < spec.v_nn() < 20.0
+
+
+def test_synthetic_mo_orthonormal():
+    spec = Q.methane_minimal()
+    M = spec.mo_coef
+    np.testing.assert_allclose(M @ M.T, np.eye(9), atol=1e-13)
+    assert spec.n_params == 12
+
+
+def test_oracle_init_matches_layout(oracle):
+    """Initial positions: electron e at N(R_init(e), sigma) from the tag-3
+    Philox stream (src/systems/methane.rs:1105-1120 placement)."""
+    spec = Q.methane_gto()
+    pos = oracle.init_positions(spec, 4, seed=123)
+    x = Q.philox4x32((2, 0, 7, 3), (123, 0))
+    u1, u2 = (x[0] + 0.5) / 2 ** 32, (x[1] + 0.5) / 2 ** 32
+    n0 = math.sqrt(-2 * math.log(u1)) * math.cos(2 * math.pi * u2)
+    assert abs(pos[2, 7, 0] - (spec.nuc_pos[1, 0] + 0.5 * n0)) < 1e-12
+
+
+def test_oracle_sweeps_deterministic(oracle):
+    spec = Q.methane_minimal()
+    pos = oracle.init_positions(spec, 8, seed=7)
+    a = oracle.sweeps(spec, pos, 3, 0, 2, seed=99, step=0.3, threads=1)
+    b = oracle.sweeps(spec, pos, 3, 0, 2, seed=99, step=0.3, threads=4)
+    np.testing.assert_array_equal(a[0], b[0])
+    assert a[1].sum() > 0

@@ -18,6 +18,8 @@
  *  - psi is reported as (log|psi|, sign) instead of the reference's raw psi;
  *    gradients are grad_i psi / psi, Laplacians lap_i psi / psi.
  *  - One context = one CUDA stream; calls on one context are serialised.
+ *  - Handles are destroyed children first: walker sets, then systems, then
+ *    the context (a parent's destroy invalidates the children's handles).
  *
  * Random numbers: Philox4x32-10 keyed by the 64-bit seed, counter
  *   c0 = walker id, c1 = step (low 32 bits), c2 = electron / sub-index,

@@ -17,6 +17,7 @@ reference trait methods with their value conventions:
 ``Walkers`` is the device-resident ensemble (the samplers' walker vectors).
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -39,11 +40,15 @@ class Context:
 
     def __init__(self, device=0):
         self.lib = L.load_library()
+        self._children = weakref.WeakSet()
         h = C.c_void_p()
         L.check(self.lib.qmc_init(device, C.byref(h)), "qmc_init")
         self.h = h
 
     def close(self):
+        """Destroys the context; systems and walkers made from it close first."""
+        for ch in list(getattr(self, "_children", ())):
+            ch.close()
         if getattr(self, "h", None):
             self.lib.qmc_destroy(self.h)
             self.h = None
@@ -104,13 +109,18 @@ class System:
 
     def __init__(self, ctx, spec):
         self.ctx, self.spec, self.lib = ctx, spec, ctx.lib
+        self._children = weakref.WeakSet()
         self._desc = spec.desc()
         h = C.c_void_p()
         L.check(self.lib.qmc_system_create(ctx.h, C.byref(self._desc), C.byref(h)), "qmc_system_create")
         self.h = h
         self.N = spec.n_elec
+        ctx._children.add(self)
 
     def close(self):
+        """Destroys the system; walker sets made from it close first."""
+        for ch in list(getattr(self, "_children", ())):
+            ch.close()
         if getattr(self, "h", None):
             self.lib.qmc_system_destroy(self.h)
             self.h = None
@@ -225,6 +235,7 @@ class Walkers:
         h = C.c_void_p()
         L.check(self.lib.qmc_walkers_create(system.h, W, precision, C.byref(h)), "qmc_walkers_create")
         self.h = h
+        system._children.add(self)
 
     def close(self):
         if getattr(self, "h", None):

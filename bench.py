@@ -343,7 +343,7 @@ def main():
             traffic = None
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_hbm, "unit": "GB/s",
                 "frac": achieved_gbs / peak_hbm, "traffic": traffic, "peak_source": peak_kind,
-                "kernel": "k_sweep_one<CH4,float,ONE_GAUSS>",
+                "kernel": "k_sweep_one<ShapeCH4Min,float,ONE_GAUSS,64>",
                 "note": "state bytes per launch / launch time; the kernel keeps walkers in shared memory "
                         "for all 64 sweeps and is bound by FP32/SFU issue, see roofline_fp32"}
     roofline_fp32 = {"bound": "fp32_simt", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",

@@ -25,6 +25,11 @@
  *   c0 = walker id, c1 = step (low 32 bits), c2 = electron / sub-index,
  *   c3 = tag | (step bits 32..47) << 16,  tag 1 proposal, 2 accept,
  *   3 initial position, 4 branching.
+ * A single-electron move uses one call (tag 1, c2 = internal electron
+ * index): the low 24 bits of words 0-3 are two Box-Muller pairs (three
+ * displacement components used), the top bytes of words 0-2 the acceptance
+ * uniform.  All-electron steps draw tag 1 per electron (32-bit uniforms) and
+ * tag 2 once for acceptance.
  * Trajectories therefore depend only on (seed, walker id, step), never on the
  * launch geometry.
  */

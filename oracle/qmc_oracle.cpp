@@ -121,6 +121,7 @@ U4 draw(uint64_t seed, uint32_t walker, uint64_t step, uint32_t sub, uint32_t ta
     return philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 inline double u01(uint32_t x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+inline double u24(uint32_t x) { return ((double)x + 0.5) * (1.0 / 16777216.0); }
 // Box-Muller (Box & Muller 1958): two uniforms -> two standard normals.
 inline void box_muller(uint32_t a, uint32_t b, double& n0, double& n1) {
     double r = std::sqrt(-2.0 * std::log(u01(a)));
@@ -777,10 +778,20 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
             }
             for (int q = 0; q < N; ++q) {
                 int e = order[q];
+                // one Philox call per single-electron move: 24-bit uniforms
+                // (words 0-3, low 24 bits) for two Box-Muller pairs, and the
+                // top bytes of words 0-2 for the acceptance uniform
                 U4 x = draw(seed, wid, st, (uint32_t)q, TAG_PROPOSE);
                 double n0, n1, n2, n3;
-                box_muller(x.v[0], x.v[1], n0, n1);
-                box_muller(x.v[2], x.v[3], n2, n3);
+                {
+                    double r = std::sqrt(-2.0 * std::log(u24(x.v[0] & 0xFFFFFFu)));
+                    double t = 6.283185307179586476925286766559 * u24(x.v[1] & 0xFFFFFFu);
+                    n0 = r * std::cos(t); n1 = r * std::sin(t);
+                    r = std::sqrt(-2.0 * std::log(u24(x.v[2] & 0xFFFFFFu)));
+                    t = 6.283185307179586476925286766559 * u24(x.v[3] & 0xFFFFFFu);
+                    n2 = r * std::cos(t); n3 = r * std::sin(t);
+                }
+                double uacc = u24((x.v[0] >> 24) | ((x.v[1] >> 24) << 8) | ((x.v[2] >> 24) << 16));
                 V3 eta{n0, n1, n2};
                 std::vector<V3> rn = r;
                 double logG = 0.0;
@@ -800,8 +811,7 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
                 double lpn = log_psi(s, rn, sgn, okn);
                 if (!okn) continue;
                 double prob = std::exp(2.0 * (lpn - lp) + logG);
-                U4 a = draw(seed, wid, st, (uint32_t)q, TAG_ACCEPT);
-                if (u01(a.v[0]) < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
+                if (uacc < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
             }
         }
         for (int i = 0; i < N; ++i) {

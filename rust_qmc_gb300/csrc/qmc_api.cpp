@@ -187,7 +187,8 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
     hs.shape = -1;
     if (hs.N == 2 && hs.n_up == 1 && hs.n_nuc == 2 && hs.basis == QMC_BASIS_STO && hs.jk == QMC_JAS_PADE_F) hs.shape = SHAPE_H2;
     if (hs.N == 3 && hs.n_up == 2 && hs.n_nuc == 1 && hs.basis == QMC_BASIS_STO && hs.jk == QMC_JAS_PADE_F) hs.shape = SHAPE_LI;
-    if (hs.N == 10 && hs.n_up == 5 && hs.n_nuc == 5 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN) hs.shape = SHAPE_CH4;
+    if (hs.N == 10 && hs.n_up == 5 && hs.n_nuc == 5 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN)
+        hs.shape = layout_matches_ch4min(hs) ? SHAPE_CH4MIN : SHAPE_CH4;
     if (hs.shape < 0) return QMC_ERR_UNSUPPORTED;
     return QMC_OK;
 }

@@ -6,6 +6,7 @@
 // shared-memory column.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace qmc {
@@ -16,12 +17,27 @@ enum { MOVE_ALL_GAUSS = 0, MOVE_ALL_BOX = 1, MOVE_ONE_GAUSS = 2, MOVE_ONE_DRIFT 
 enum { TAG_PROPOSE = 1, TAG_ACCEPT = 2, TAG_INIT = 3, TAG_BRANCH = 4 };
 enum { FLAG_SINGULAR = 1, FLAG_NONFINITE = 2 };
 
-template <int NE_, int NUP_, int NNUC_, int NSH_, int NAO_, int NPRIM_, int BASIS_, int JAS_, int NROT_>
+// Compile-time basis layout of the 9-function CH4 workload: shell s sits on
+// nucleus nuc(s), has np(s) primitives and is kind 1 (one s AO) or kind 2
+// (an s AO plus a p triplet sharing exponents).  Shells are ordered by
+// nucleus; AO and primitive indices are the prefix sums the host uses.
+struct LayoutCH4Min {
+    static constexpr int NSHELL = 6;
+    __host__ __device__ static constexpr int nuc(int s) { return s < 2 ? 0 : s - 1; }
+    __host__ __device__ static constexpr int np(int) { return 3; }
+    __host__ __device__ static constexpr int kind(int s) { return s == 1 ? 2 : 1; }
+    __host__ __device__ static constexpr int p0(int s) { return 3 * s; }
+    __host__ __device__ static constexpr int ao0(int s) { return s < 2 ? s : s + 3; }
+};
+
+template <int NE_, int NUP_, int NNUC_, int NSH_, int NAO_, int NPRIM_, int BASIS_, int JAS_, int NROT_,
+          class LAYOUT_ = void>
 struct ShapeT {
     static constexpr int NE = NE_, NUP = NUP_, NDN = NE_ - NUP_, NNUC = NNUC_;
     static constexpr int NSH = NSH_, NAO = NAO_, NPRIM = NPRIM_, BASIS = BASIS_, JAS = JAS_;
     static constexpr int NROT = NROT_;
     static constexpr int NMAX = NUP_ > (NE_ - NUP_) ? NUP_ : (NE_ - NUP_);
+    using Layout = LAYOUT_;
 };
 
 // H2 LCAO (src/systems/hydrogen.rs:28-35): 2 Slater 1s AOs, 1 up + 1 down.
@@ -30,6 +46,8 @@ using ShapeH2 = ShapeT<2, 1, 2, 2, 2, 2, BASIS_STO, JAS_PADE_F, 1>;
 using ShapeLi = ShapeT<3, 2, 1, 1, 2, 8, BASIS_STO, JAS_PADE_F, 1>;
 // CH4 (src/systems/methane.rs:600-776): up to 17 Gaussian AOs, 5 up + 5 down.
 using ShapeCH4 = ShapeT<10, 5, 5, 12, 17, 28, BASIS_GTO, JAS_PADE_EEN, 4>;
+// The 9-function CH4 workload with its basis layout fixed at compile time.
+using ShapeCH4Min = ShapeT<10, 5, 5, 6, 9, 18, BASIS_GTO, JAS_PADE_EEN, 4, LayoutCH4Min>;
 
 template <class SH, class T>
 struct SysT {
@@ -39,7 +57,7 @@ struct SysT {
     T enB[SH::NNUC];          // B_species
     T Aspec[SH::NNUC];        // A_species (unscaled)
     int species[SH::NNUC];
-    T F;                      // Pade-F parameter
+    T F, invF;                // Pade-F parameter and 1/F
     T b_ee[2], a_ee[2];       // [0] antiparallel, [1] parallel
     T qa;                     // Jastrow2 gradient prefactor quirk (F or 1)
     int quirk_lap;            // Jastrow2 Laplacian quirk
@@ -100,6 +118,25 @@ __device__ __forceinline__ U4 rng_draw(uint64_t seed, uint32_t walker, uint64_t 
     U4 c{walker, (uint32_t)step, sub, tag | ((uint32_t)((step >> 32) & 0xFFFFu) << 16)};
     return philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
+// A single-electron move takes one Philox call: four 24-bit uniforms feed two
+// Box-Muller pairs (three displacement components are used) and the top
+// bytes of words 0-2 form the 24-bit acceptance uniform.
+__device__ __forceinline__ double u24(uint32_t k, double) { return ((double)k + 0.5) * (1.0 / 16777216.0); }
+__device__ __forceinline__ float u24(uint32_t k, float) { return ((float)k + 0.5f) * (1.0f / 16777216.0f); }
+template <class T>
+struct MoveDraw { T n0, n1, n2, uacc; };
+__device__ __forceinline__ void bm24(uint32_t a, uint32_t b, double& n0, double& n1) {
+    double r = sqrt(-2.0 * log(u24(a, 0.0)));
+    double s, c;
+    sincospi(2.0 * u24(b, 0.0), &s, &c);
+    n0 = r * c; n1 = r * s;
+}
+__device__ __forceinline__ void bm24(uint32_t a, uint32_t b, float& n0, float& n1) {
+    float r = sqrtf(-2.0f * __logf(u24(a, 0.0f)));
+    float s, c;
+    __sincosf(6.28318530717958647f * u24(b, 0.0f), &s, &c);
+    n0 = r * c; n1 = r * s;
+}
 __device__ __forceinline__ double to_u01(uint32_t x, double) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
 __device__ __forceinline__ float to_u01(uint32_t x, float) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 __device__ __forceinline__ void bm(uint32_t a, uint32_t b, double& n0, double& n1) {
@@ -113,6 +150,18 @@ __device__ __forceinline__ void bm(uint32_t a, uint32_t b, float& n0, float& n1)
     float s, c;
     __sincosf(6.28318530717958647f * to_u01(b, 0.0f), &s, &c);
     n0 = r * c; n1 = r * s;
+}
+
+template <class T>
+__device__ __forceinline__ MoveDraw<T> move_draw(uint64_t seed, uint32_t walker, uint64_t step, uint32_t e) {
+    U4 x = rng_draw(seed, walker, step, e, TAG_PROPOSE);
+    MoveDraw<T> d;
+    T n3;
+    bm24(x.x & 0xFFFFFFu, x.y & 0xFFFFFFu, d.n0, d.n1);
+    bm24(x.z & 0xFFFFFFu, x.w & 0xFFFFFFu, d.n2, n3);
+    uint32_t ua = (x.x >> 24) | ((x.y >> 24) << 8) | ((x.z >> 24) << 16);
+    d.uacc = u24(ua, T(0));
+    return d;
 }
 
 // ---------------------------------------------------------------------------
@@ -142,12 +191,58 @@ struct MOEval {
         for (int q = 0; q < NR; ++q) dv[q] += S.dC[q][a] * chi;
     }
 
-    // NUC >= 0 restricts the sum to AOs centred on that nucleus.
+    // GTO shell: accumulate one shell's s AO (index a) and optional p triplet.
+    __device__ __forceinline__ void gto_shell(const SysT<SH, T>& S, int a, bool has_p, T a0, T b0, T c0, T ap,
+                                              T bp, T cpp, T dx, T dy, T dz, T r2) {
+        add(S, a, a0, -2 * b0 * dx, -2 * b0 * dy, -2 * b0 * dz, -6 * b0 + 4 * r2 * c0);
+        if (has_p) {
+            T lp = -10 * bp + 4 * r2 * cpp;
+            add(S, a + 1, dx * ap, dx * (-2 * bp * dx) + ap, dx * (-2 * bp * dy), dx * (-2 * bp * dz), dx * lp);
+            add(S, a + 2, dy * ap, dy * (-2 * bp * dx), dy * (-2 * bp * dy) + ap, dy * (-2 * bp * dz), dy * lp);
+            add(S, a + 3, dz * ap, dz * (-2 * bp * dx), dz * (-2 * bp * dy), dz * (-2 * bp * dz) + ap, dz * lp);
+        }
+    }
+
+    // only_nuc >= 0 restricts the sum to AOs centred on that nucleus.
     __device__ __forceinline__ void run(const SysT<SH, T>& S, T x, T y, T z, int only_nuc = -1) {
 #pragma unroll
         for (int k = 0; k < SH::NMAX; ++k) { v[k] = 0; gx[k] = 0; gy[k] = 0; gz[k] = 0; l[k] = 0; }
 #pragma unroll
         for (int q = 0; q < (NR > 0 ? NR : 1); ++q) dv[q] = 0;
+        if constexpr (!std::is_void<typename SH::Layout>::value) {
+            using LY = typename SH::Layout;
+#pragma unroll
+            for (int sh = 0; sh < LY::NSHELL; ++sh) {
+                const int I = LY::nuc(sh), p0 = LY::p0(sh), a = LY::ao0(sh);
+                const bool has_p = LY::kind(sh) == 2;
+                if (only_nuc >= 0 && only_nuc != I) continue;
+                T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+                T r2 = dx * dx + dy * dy + dz * dz;
+                T a0 = 0, b0 = 0, c0 = 0, ap = 0, bp = 0, cpp = 0;
+#pragma unroll
+                for (int p = p0; p < p0 + LY::np(sh); ++p) {
+                    T al = S.pexp[p];
+                    T e = fexp(-al * r2);
+                    T e0 = S.cs0[p] * e;
+                    a0 += e0;
+                    if (MODE >= 1) b0 += al * e0;
+                    if (MODE >= 2) c0 += al * al * e0;
+                    if (has_p) {
+                        T ep = S.cp[p] * e;
+                        ap += ep;
+                        if (MODE >= 1) bp += al * ep;
+                        if (MODE >= 2) cpp += al * al * ep;
+                    }
+                }
+                gto_shell(S, a, has_p, a0, b0, c0, ap, bp, cpp, dx, dy, dz, r2);
+            }
+        } else {
+            run_tables(S, x, y, z, only_nuc);
+        }
+    }
+
+    // Table-driven shells (runtime shell and primitive counts).
+    __device__ __forceinline__ void run_tables(const SysT<SH, T>& S, T x, T y, T z, int only_nuc) {
 #pragma unroll
         for (int I = 0; I < SH::NNUC; ++I) {
             if (only_nuc >= 0 && only_nuc != I) continue;
@@ -212,20 +307,35 @@ struct MOEval {
 // PADE_EEN e-e: u = a r/(1+b r); e-n: u = -A r/(1+B r)   (:218-321)
 // ---------------------------------------------------------------------------
 template <class T>
-__device__ __forceinline__ void pade_f(T F, T d, T& u, T& up, T& lt) {
-    T f = 1 + d / F;
-    T inv = frcp(f);
+__device__ __forceinline__ T frsqrt(T x);
+template <>
+__device__ __forceinline__ double frsqrt<double>(double x) { return rsqrt(x); }
+template <>
+__device__ __forceinline__ float frsqrt<float>(float x) { return rsqrtf(x); }
+
+// Distance and reciprocal distance from a squared distance (one rsqrt).
+template <class T>
+__device__ __forceinline__ void dist(T r2, T& d, T& rinv) {
+    rinv = r2 > T(0) ? frsqrt(r2) : T(0);
+    d = r2 * rinv;
+}
+
+// upr = u'(r)/r, lt = u'' + 2u'/r.  rinv = 1/r (0 at r = 0).
+template <class T>
+__device__ __forceinline__ void pade_f(T F, T invF, T d, T rinv, T& u, T& upr, T& lt) {
+    T inv = frcp(1 + d * invF);
     u = -F * T(0.5) * inv;
-    up = T(0.5) * inv * inv;
-    lt = d > 0 ? inv * inv * inv / d : T(0);
+    T up = T(0.5) * inv * inv;
+    upr = up * rinv;
+    lt = inv * inv * inv * rinv;
 }
 template <class T>
-__device__ __forceinline__ void pade_ab(T a, T b, T d, T& u, T& up, T& lt) {
-    T den = 1 + b * d;
-    T inv = frcp(den);
+__device__ __forceinline__ void pade_ab(T a, T b, T d, T rinv, T& u, T& upr, T& lt) {
+    T inv = frcp(1 + b * d);
     u = a * d * inv;
-    up = a * inv * inv;
-    lt = d > 0 ? 2 * a * inv * inv / d - 2 * a * b * inv * inv * inv : T(0);
+    T up = a * inv * inv;
+    upr = up * rinv;
+    lt = 2 * up * rinv - 2 * a * b * inv * inv * inv;
 }
 
 // ---------------------------------------------------------------------------

@@ -11,7 +11,7 @@ namespace qmc {
 // Kernel shapes compiled into the library.  A shape fixes the electron
 // counts and nucleus count at compile time so per-walker arrays live in
 // registers / shared memory with static indices.
-enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_COUNT = 3 };
+enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_CH4MIN = 3, SHAPE_COUNT = 4 };
 
 // A basis shell: primitives shared by up to two s-type AOs and one p triplet
 // (the SP shells of 6-31G share exponents between 2s and 2p; Li's STO-7G 1s
@@ -80,6 +80,8 @@ struct MeasureOut {
 };
 
 int nmax_of_shape(int shape);
+// True when the system's shells match the compile-time 9-function CH4 layout.
+bool layout_matches_ch4min(const HostSys& hs);
 
 // Launchers (return a qmc status).  compute_prec: 0 double, 1 float.
 int launch_init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st);

@@ -30,12 +30,32 @@ static int cuda_status(cudaError_t e) {
 QMC_DECLARE_SHAPE(h2)
 QMC_DECLARE_SHAPE(li)
 QMC_DECLARE_SHAPE(ch4)
+QMC_DECLARE_SHAPE(ch4min)
+
+// The compile-time CH4 layout has no all-electron kernels of its own.
+int shape_step_all_ch4min(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, uint64_t seed,
+                          cudaStream_t st, double* partial) {
+    return shape_step_all_ch4(hs, dw, mk, n, s0, step, seed, st, partial);
+}
+
+bool layout_matches_ch4min(const HostSys& hs) {
+    using LY = LayoutCH4Min;
+    if ((int)hs.shells.size() != LY::NSHELL || hs.n_ao != 9) return false;
+    for (int s = 0; s < LY::NSHELL; ++s) {
+        const HostShell& h = hs.shells[s];
+        if (h.nuc != LY::nuc(s) || (int)h.exps.size() != LY::np(s)) return false;
+        bool has_p = h.p_ao[0] >= 0;
+        if (h.s_ao[0] < 0 || h.s_ao[1] >= 0 || has_p != (LY::kind(s) == 2)) return false;
+    }
+    return true;
+}
 
 #define QMC_SHAPE_SWITCH(shape, CALL)                  \
     switch (shape) {                                   \
         case SHAPE_H2: return CALL(h2);                \
         case SHAPE_LI: return CALL(li);                \
         case SHAPE_CH4: return CALL(ch4);              \
+        case SHAPE_CH4MIN: return CALL(ch4min);        \
     }                                                  \
     return 7;
 
@@ -61,6 +81,7 @@ int launch_measure(const HostSys& hs, DevWalkers& dw, int compute_prec, bool wri
 int launch_sweep(const HostSys& hs, DevWalkers& dw, int move_kind, int n_sweeps, uint64_t step0, double step,
                  double tau, double max_drift, uint64_t seed, cudaStream_t st) {
     if (move_kind == 0 || move_kind == 1) {
+        if (hs.shape == SHAPE_CH4MIN) return shape_step_all_ch4(hs, dw, move_kind, n_sweeps, step0, step, seed, st, nullptr);
 #define C_(n) shape_step_all_##n(hs, dw, move_kind, n_sweeps, step0, step, seed, st, nullptr)
         QMC_SHAPE_SWITCH(hs.shape, C_)
 #undef C_
@@ -74,6 +95,7 @@ int launch_sweep(const HostSys& hs, DevWalkers& dw, int move_kind, int n_sweeps,
 int launch_step_all_recorded(const HostSys& hs, DevWalkers& dw, int move_kind, int n, uint64_t s0, double step,
                              uint64_t seed, double* partial, cudaStream_t st) {
     if (move_kind != 0 && move_kind != 1) return 1;
+    if (hs.shape == SHAPE_CH4MIN) return shape_step_all_ch4(hs, dw, move_kind, n, s0, step, seed, st, partial);
 #define C_(nm) shape_step_all_##nm(hs, dw, move_kind, n, s0, step, seed, st, partial)
     QMC_SHAPE_SWITCH(hs.shape, C_)
 #undef C_

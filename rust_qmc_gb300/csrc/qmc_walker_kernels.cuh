@@ -40,6 +40,7 @@ static bool fill_sys(const HostSys& hs, SysT<SH, T>& S) {
         S.enB[I] = (T)hs.jas[4 + sp];
     }
     S.F = (T)hs.F;
+    S.invF = (T)(1.0 / hs.F);
     S.b_ee[0] = (T)hs.jas[0]; S.b_ee[1] = (T)hs.jas[1];
     S.a_ee[0] = (T)hs.jas[2]; S.a_ee[1] = (T)hs.jas[3];
     S.qa = (hs.quirks & 1) ? (T)hs.F : (T)1;
@@ -117,28 +118,24 @@ __device__ __forceinline__ T jastrow_point(const SysT<SH, T>& S, PosFn pos, int 
         if (j == e) continue;
         const bool para = ((j < SH::NUP) == (SIG == 0));
         T dx = x - pos(j, 0), dy = y - pos(j, 1), dz = z - pos(j, 2);
-        T d = fsqrt(dx * dx + dy * dy + dz * dz);
-        T uu, up, lt;
-        if (SH::JAS == JAS_PADE_F) pade_f(S.F, d, uu, up, lt);
-        else pade_ab(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], d, uu, up, lt);
+        T d, ri;
+        dist(dx * dx + dy * dy + dz * dz, d, ri);
+        T uu, upr, lt;
+        if (SH::JAS == JAS_PADE_F) pade_f(S.F, S.invF, d, ri, uu, upr, lt);
+        else pade_ab(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], d, ri, uu, upr, lt);
         u += uu;
-        if (GRAD) {
-            T f = d > 0 ? up / d : T(0);
-            gx += f * dx; gy += f * dy; gz += f * dz;
-        }
+        if (GRAD) { gx += upr * dx; gy += upr * dy; gz += upr * dz; }
     }
     if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll
         for (int I = 0; I < SH::NNUC; ++I) {
             T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
-            T d = fsqrt(dx * dx + dy * dy + dz * dz);
-            T uu, up, lt;
-            pade_ab(S.enA[I], S.enB[I], d, uu, up, lt);
+            T d, ri;
+            dist(dx * dx + dy * dy + dz * dz, d, ri);
+            T uu, upr, lt;
+            pade_ab(S.enA[I], S.enB[I], d, ri, uu, upr, lt);
             u -= uu;
-            if (GRAD) {
-                T f = d > 0 ? up / d : T(0);
-                gx -= f * dx; gy -= f * dy; gz -= f * dz;
-            }
+            if (GRAD) { gx -= upr * dx; gy -= upr * dy; gz -= upr * dz; }
         }
     }
     if (GRAD) { gx *= S.qa; gy *= S.qa; gz *= S.qa; }
@@ -233,85 +230,71 @@ __device__ __forceinline__ void eval_sector(const SysT<SH, TC>& S, const TC (&r)
 }
 
 // Jastrow over all pairs: u, grad_i u (true gradient), sum_j (u''+2u'/r),
-// sum_j u'^2 (for the per-pair Laplacian quirk), and parameter derivatives.
+// sum_j u'^2 (for the per-pair Laplacian quirk), parameter derivatives, and
+// the Coulomb potential V_ee + V_en + V_nn from the same distances (one
+// reciprocal square root per pair).
 template <class SH, class TC, bool WANT_O>
-__device__ __forceinline__ TC jastrow_full(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3], TC (&gx)[SH::NE],
-                                           TC (&gy)[SH::NE], TC (&gz)[SH::NE], TC (&lu)[SH::NE],
-                                           TC (&gsq)[SH::NE], TC* O) {
+__device__ __forceinline__ TC jastrow_coulomb(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3], TC (&gx)[SH::NE],
+                                              TC (&gy)[SH::NE], TC (&gz)[SH::NE], TC (&lu)[SH::NE],
+                                              TC (&gsq)[SH::NE], TC* O, TC& V) {
     TC u = 0;
+    V = S.v_nn;
 #pragma unroll
     for (int i = 0; i < SH::NE; ++i) { gx[i] = 0; gy[i] = 0; gz[i] = 0; lu[i] = 0; gsq[i] = 0; }
-    if (SH::JAS == JAS_NONE) return u;
 #pragma unroll
     for (int i = 0; i < SH::NE; ++i)
 #pragma unroll
         for (int j = i + 1; j < SH::NE; ++j) {
             const bool para = ((i < SH::NUP) == (j < SH::NUP));
             TC dx = r[i][0] - r[j][0], dy = r[i][1] - r[j][1], dz = r[i][2] - r[j][2];
-            TC d = fsqrt(dx * dx + dy * dy + dz * dz);
-            TC uu, up, lt;
+            TC d, ri;
+            dist(dx * dx + dy * dy + dz * dz, d, ri);
+            V += ri;
+            if (SH::JAS == JAS_NONE) continue;
+            TC uu, upr, lt;
             const int c = para ? 1 : 0;
-            if (SH::JAS == JAS_PADE_F) pade_f(S.F, d, uu, up, lt);
-            else pade_ab(S.a_ee[c], S.b_ee[c], d, uu, up, lt);
+            if (SH::JAS == JAS_PADE_F) pade_f(S.F, S.invF, d, ri, uu, upr, lt);
+            else pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
             u += uu;
             bool skip = (SH::JAS == JAS_PADE_EEN) ? (d < TC(1e-10)) : (d == TC(0));
             if (!skip) {
-                TC f = up / d;
-                gx[i] += f * dx; gy[i] += f * dy; gz[i] += f * dz;
-                gx[j] -= f * dx; gy[j] -= f * dy; gz[j] -= f * dz;
+                gx[i] += upr * dx; gy[i] += upr * dy; gz[i] += upr * dz;
+                gx[j] -= upr * dx; gy[j] -= upr * dy; gz[j] -= upr * dz;
                 lu[i] += lt; lu[j] += lt;
+                TC up = upr * d;
                 gsq[i] += up * up; gsq[j] += up * up;
             }
             if (WANT_O && SH::JAS == JAS_PADE_EEN) {
-                TC den = 1 + S.b_ee[c] * d;
-                O[c] += -S.a_ee[c] * d * d / (den * den);
-                O[2 + c] += d / den;
+                TC inv = TC(1) / (1 + S.b_ee[c] * d);
+                O[c] += -S.a_ee[c] * d * d * inv * inv;
+                O[2 + c] += d * inv;
             }
         }
-    if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll
-        for (int i = 0; i < SH::NE; ++i)
-#pragma unroll
-            for (int I = 0; I < SH::NNUC; ++I) {
-                TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
-                TC d = fsqrt(dx * dx + dy * dy + dz * dz);
-                TC uu, up, lt;
-                pade_ab(S.enA[I], S.enB[I], d, uu, up, lt);
-                u -= uu;
-                if (!(d < TC(1e-10))) {
-                    TC f = up / d;
-                    gx[i] -= f * dx; gy[i] -= f * dy; gz[i] -= f * dz;
-                    lu[i] -= lt;
-                }
-                if (WANT_O) {
-                    TC den = 1 + S.enB[I] * d;
-                    TC dB = S.Aspec[I] * S.Z[I] * d * d / (den * den);
-                    TC dA = -S.Z[I] * d / den;
-                    if (S.species[I] == 0) { O[4] += dB; O[6] += dA; }
-                    else { O[5] += dB; O[7] += dA; }
-                }
-            }
-    }
-    return u;
-}
-
-template <class SH, class TC>
-__device__ __forceinline__ TC potential(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3]) {
-    TC v = 0;
-#pragma unroll
-    for (int i = 0; i < SH::NE; ++i) {
+    for (int i = 0; i < SH::NE; ++i)
 #pragma unroll
         for (int I = 0; I < SH::NNUC; ++I) {
             TC dx = r[i][0] - S.nuc[I][0], dy = r[i][1] - S.nuc[I][1], dz = r[i][2] - S.nuc[I][2];
-            v -= S.Z[I] / fsqrt(dx * dx + dy * dy + dz * dz);
+            TC d, ri;
+            dist(dx * dx + dy * dy + dz * dz, d, ri);
+            V -= S.Z[I] * ri;
+            if (SH::JAS != JAS_PADE_EEN) continue;
+            TC uu, upr, lt;
+            pade_ab(S.enA[I], S.enB[I], d, ri, uu, upr, lt);
+            u -= uu;
+            if (!(d < TC(1e-10))) {
+                gx[i] -= upr * dx; gy[i] -= upr * dy; gz[i] -= upr * dz;
+                lu[i] -= lt;
+            }
+            if (WANT_O) {
+                TC inv = TC(1) / (1 + S.enB[I] * d);
+                TC dB = S.Aspec[I] * S.Z[I] * d * d * inv * inv;
+                TC dA = -S.Z[I] * d * inv;
+                if (S.species[I] == 0) { O[4] += dB; O[6] += dA; }
+                else { O[5] += dB; O[7] += dA; }
+            }
         }
-#pragma unroll
-        for (int j = i + 1; j < SH::NE; ++j) {
-            TC dx = r[i][0] - r[j][0], dy = r[i][1] - r[j][1], dz = r[i][2] - r[j][2];
-            v += TC(1) / fsqrt(dx * dx + dy * dy + dz * dz);
-        }
-    }
-    return v + S.v_nn;
+    return u;
 }
 
 template <class SH, class TC, int NR, class DinvStore>
@@ -321,9 +304,9 @@ __device__ __forceinline__ void evaluate_config(const SysT<SH, TC>& S, const TC 
     TC gjx[SH::NE], gjy[SH::NE], gjz[SH::NE], lu[SH::NE], gsq[SH::NE];
 #pragma unroll
     for (int p = 0; p < 8 + (NR > 0 ? NR : 1); ++p) out.O[p] = 0;
-    TC u;
-    if (NR > 0 || want_o) u = jastrow_full<SH, TC, true>(S, r, gjx, gjy, gjz, lu, gsq, out.O);
-    else u = jastrow_full<SH, TC, false>(S, r, gjx, gjy, gjz, lu, gsq, out.O);
+    TC u, V;
+    if (NR > 0 || want_o) u = jastrow_coulomb<SH, TC, true>(S, r, gjx, gjy, gjz, lu, gsq, out.O, V);
+    else u = jastrow_coulomb<SH, TC, false>(S, r, gjx, gjy, gjz, lu, gsq, out.O, V);
     TC gdx[SH::NE], gdy[SH::NE], gdz[SH::NE], ld[SH::NE];
     double logdet = 0.0;
     int sg = 1;
@@ -340,7 +323,7 @@ __device__ __forceinline__ void evaluate_config(const SysT<SH, TC>& S, const TC 
         out.lap[e] = lp;
         kin += lp;
     }
-    out.el = TC(-0.5) * kin + potential(S, r);
+    out.el = TC(-0.5) * kin + V;
     out.logabs = logdet + (double)u;
     out.sign = sg;
     out.ok = ok;
@@ -489,10 +472,8 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
     for (int q = 0; q < NS; ++q) {
         const int e = SIG * SH::NUP + q;
         T rx = P(e, 0), ry = P(e, 1), rz = P(e, 2);
-        U4 x = rng_draw(seed, w, st, (uint32_t)e, TAG_PROPOSE);
-        T n0, n1, n2, n3;
-        bm(x.x, x.y, n0, n1);
-        bm(x.z, x.w, n2, n3);
+        MoveDraw<T> md = move_draw<T>(seed, w, st, (uint32_t)e);
+        const T n0 = md.n0, n1 = md.n1, n2 = md.n2;
         T nx, ny, nz, dlx = 0, dly = 0, dlz = 0;
         T gjx, gjy, gjz;
         T u_old;
@@ -536,10 +517,8 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
         T ratio = R * fexp(u_new - u_old);
         T prob = ratio * ratio;
         if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
-        U4 a = rng_draw(seed, w, st, (uint32_t)e, TAG_ACCEPT);
-        T uacc = to_u01(a.x, T(0));
         if (prob != prob) flg |= FLAG_NONFINITE;
-        if (uacc < prob && R != T(0)) {
+        if (md.uacc < prob && R != T(0)) {
             sp[(3 * e + 0) * TPB + t] = nx;
             sp[(3 * e + 1) * TPB + t] = ny;
             sp[(3 * e + 2) * TPB + t] = nz;
@@ -564,8 +543,10 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
 #undef DI
 }
 
+// Occupancy target: all walkers of the 65 536-walker workload resident in
+// one wave (152 SMs x 8 blocks x 64 threads), i.e. <= 128 registers/thread.
 template <class SH, class T, int MOVE, int TPB>
-__global__ void __launch_bounds__(TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
+__global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
                                                    T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
                                                    int n_sweeps, uint64_t step0, T step, T tau, T maxd,
                                                    uint64_t seed, unsigned long long* acc_out, int* flags) {
@@ -730,7 +711,7 @@ struct ShapeOps {
                          uint64_t seed, cudaStream_t st) {
         SysT<SH, T> S;
         if (!fill_sys(hs, S)) return 7;
-        constexpr int TPB = sizeof(T) == 4 ? 128 : 64;
+        constexpr int TPB = 64;
         size_t smem = sizeof(T) * TPB * (3 * SH::NE + 2 * SH::NMAX * SH::NMAX);
         auto kern = k_sweep_one<SH, T, MOVE, TPB>;
         static bool attr_set = false;

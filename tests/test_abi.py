@@ -44,7 +44,7 @@ def test_status_strings(qmc_lib):
 
 
 @pytest.mark.parametrize("builder,shape", [(lambda: Q.h2_mo(), 0), (lambda: Q.lithium_atom(), 1),
-                                           (lambda: Q.methane_gto(), 2), (lambda: Q.methane_minimal(), 2)])
+                                           (lambda: Q.methane_gto(), 2), (lambda: Q.methane_minimal(), 3)])
 def test_system_check_maps_shapes(qmc_lib, builder, shape):
     spec = builder()
     d = spec.desc()

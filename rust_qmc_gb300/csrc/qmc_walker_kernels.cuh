@@ -142,6 +142,69 @@ __device__ __forceinline__ T jastrow_point(const SysT<SH, T>& S, PosFn pos, int 
     return u;
 }
 
+// Change of u when electron e moves from (ox,oy,oz) to (nx,ny,nz): old and
+// new pair terms in one branch-free pass (the partner e itself is masked),
+// optionally with grad_e u at both positions.
+template <class SH, class T, int SIG, bool GRAD, class PosFn>
+__device__ __forceinline__ T jastrow_delta(const SysT<SH, T>& S, PosFn pos, int e, T ox, T oy, T oz, T nx, T ny,
+                                           T nz, T (&go)[3], T (&gn)[3]) {
+    T du = 0;
+    go[0] = go[1] = go[2] = gn[0] = gn[1] = gn[2] = 0;
+    if (SH::JAS == JAS_NONE) return du;
+#pragma unroll
+    for (int j = 0; j < SH::NE; ++j) {
+        const bool para = ((j < SH::NUP) == (SIG == 0));
+        const T m = (j != e) ? T(1) : T(0);
+        T xj = pos(j, 0), yj = pos(j, 1), zj = pos(j, 2);
+        T ax = ox - xj, ay = oy - yj, az = oz - zj;
+        T bx = nx - xj, by = ny - yj, bz = nz - zj;
+        T ra = ax * ax + ay * ay + az * az, rb = bx * bx + by * by + bz * bz;
+        ra = (j != e) ? ra : T(1);
+        rb = (j != e) ? rb : T(1);
+        T da, ia, db, ib;
+        dist(ra, da, ia);
+        dist(rb, db, ib);
+        T ua, upa, lta, ub, upb, ltb;
+        if (SH::JAS == JAS_PADE_F) {
+            pade_f(S.F, S.invF, da, ia, ua, upa, lta);
+            pade_f(S.F, S.invF, db, ib, ub, upb, ltb);
+        } else {
+            const int c = para ? 1 : 0;
+            pade_ab(S.a_ee[c], S.b_ee[c], da, ia, ua, upa, lta);
+            pade_ab(S.a_ee[c], S.b_ee[c], db, ib, ub, upb, ltb);
+        }
+        du += m * (ub - ua);
+        if (GRAD) {
+            upa *= m; upb *= m;
+            go[0] += upa * ax; go[1] += upa * ay; go[2] += upa * az;
+            gn[0] += upb * bx; gn[1] += upb * by; gn[2] += upb * bz;
+        }
+    }
+    if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+        for (int I = 0; I < SH::NNUC; ++I) {
+            T ax = ox - S.nuc[I][0], ay = oy - S.nuc[I][1], az = oz - S.nuc[I][2];
+            T bx = nx - S.nuc[I][0], by = ny - S.nuc[I][1], bz = nz - S.nuc[I][2];
+            T da, ia, db, ib;
+            dist(ax * ax + ay * ay + az * az, da, ia);
+            dist(bx * bx + by * by + bz * bz, db, ib);
+            T ua, upa, lta, ub, upb, ltb;
+            pade_ab(S.enA[I], S.enB[I], da, ia, ua, upa, lta);
+            pade_ab(S.enA[I], S.enB[I], db, ib, ub, upb, ltb);
+            du -= ub - ua;
+            if (GRAD) {
+                go[0] -= upa * ax; go[1] -= upa * ay; go[2] -= upa * az;
+                gn[0] -= upb * bx; gn[1] -= upb * by; gn[2] -= upb * bz;
+            }
+        }
+    }
+    if (GRAD) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { go[c] *= S.qa; gn[c] *= S.qa; }
+    }
+    return du;
+}
+
 // ---------------------------------------------------------------------------
 // Full evaluation of one configuration in precision TC.
 // ---------------------------------------------------------------------------
@@ -472,49 +535,53 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
     for (int q = 0; q < NS; ++q) {
         const int e = SIG * SH::NUP + q;
         T rx = P(e, 0), ry = P(e, 1), rz = P(e, 2);
+        T mv[NM];
         MoveDraw<T> md = move_draw<T>(seed, w, st, (uint32_t)e);
         const T n0 = md.n0, n1 = md.n1, n2 = md.n2;
         T nx, ny, nz, dlx = 0, dly = 0, dlz = 0;
-        T gjx, gjy, gjz;
-        T u_old;
+        T logG = 0, R = 0, du;
         if (MOVE == MOVE_ONE_DRIFT) {
+            // drift at the current position: grad ln D (from the current
+            // inverse) + grad u; then the Langevin proposal
             MOEval<SH, T, SIG, 1, 0> mc;
             mc.run(S, rx, ry, rz);
             T ax = 0, ay = 0, az = 0;
 #pragma unroll
             for (int k = 0; k < NS; ++k) { T d = DI(k, q); ax += mc.gx[k] * d; ay += mc.gy[k] * d; az += mc.gz[k] * d; }
-            u_old = jastrow_point<SH, T, SIG, true>(S, P, e, rx, ry, rz, gjx, gjy, gjz);
-            T Fx = 2 * (ax + gjx), Fy = 2 * (ay + gjy), Fz = 2 * (az + gjz);
+            T g0[3], g1[3];
+            jastrow_delta<SH, T, SIG, true>(S, P, e, rx, ry, rz, rx, ry, rz, g0, g1);
+            T Fx = 2 * (ax + g0[0]), Fy = 2 * (ay + g0[1]), Fz = 2 * (az + g0[2]);
             dlx = tau * Fx; dly = tau * Fy; dlz = tau * Fz;
             T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
             if (m > maxd) { T s = maxd / m; dlx *= s; dly *= s; dlz *= s; }
             T sd2 = fsqrt(2 * tau);
             nx = rx + dlx + sd2 * n0; ny = ry + dly + sd2 * n1; nz = rz + dlz + sd2 * n2;
-        } else {
-            u_old = jastrow_point<SH, T, SIG, false>(S, P, e, rx, ry, rz, gjx, gjy, gjz);
-            nx = rx + step * n0; ny = ry + step * n1; nz = rz + step * n2;
-        }
-        MOEval<SH, T, SIG, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0, 0> mn;
-        mn.run(S, nx, ny, nz);
-        T R = 0;
+            MOEval<SH, T, SIG, 1, 0> mn;
+            mn.run(S, nx, ny, nz);
 #pragma unroll
-        for (int k = 0; k < NS; ++k) R += mn.v[k] * DI(k, q);
-        T u_new = jastrow_point<SH, T, SIG, MOVE == MOVE_ONE_DRIFT>(S, P, e, nx, ny, nz, gjx, gjy, gjz);
-        T logG = 0;
-        if (MOVE == MOVE_ONE_DRIFT) {
-            T ax = 0, ay = 0, az = 0;
+            for (int k = 0; k < NS; ++k) { R += mn.v[k] * DI(k, q); mv[k] = mn.v[k]; }
+            T gn[3];
+            du = jastrow_delta<SH, T, SIG, true>(S, P, e, rx, ry, rz, nx, ny, nz, g0, gn);
+            T bx = 0, by = 0, bz = 0;
 #pragma unroll
-            for (int k = 0; k < NS; ++k) { T d = DI(k, q); ax += mn.gx[k] * d; ay += mn.gy[k] * d; az += mn.gz[k] * d; }
+            for (int k = 0; k < NS; ++k) { T d = DI(k, q); bx += mn.gx[k] * d; by += mn.gy[k] * d; bz += mn.gz[k] * d; }
             T iR = R != T(0) ? T(1) / R : T(0);
-            T Fx = 2 * (ax * iR + gjx), Fy = 2 * (ay * iR + gjy), Fz = 2 * (az * iR + gjz);
-            T bx = tau * Fx, by = tau * Fy, bz = tau * Fz;
-            T m = fsqrt(bx * bx + by * by + bz * bz);
-            if (m > maxd) { T s = maxd / m; bx *= s; by *= s; bz *= s; }
+            bx = tau * 2 * (bx * iR + gn[0]); by = tau * 2 * (by * iR + gn[1]); bz = tau * 2 * (bz * iR + gn[2]);
+            T mb = fsqrt(bx * bx + by * by + bz * bz);
+            if (mb > maxd) { T s = maxd / mb; bx *= s; by *= s; bz *= s; }
             T fx = nx - rx - dlx, fy = ny - ry - dly, fz = nz - rz - dlz;
             T qx = rx - nx - bx, qy = ry - ny - by, qz = rz - nz - bz;
             logG = ((fx * fx + fy * fy + fz * fz) - (qx * qx + qy * qy + qz * qz)) / (4 * tau);
+        } else {
+            nx = rx + step * n0; ny = ry + step * n1; nz = rz + step * n2;
+            MOEval<SH, T, SIG, 0, 0> mn;
+            mn.run(S, nx, ny, nz);
+#pragma unroll
+            for (int k = 0; k < NS; ++k) { R += mn.v[k] * DI(k, q); mv[k] = mn.v[k]; }
+            T g0[3], g1[3];
+            du = jastrow_delta<SH, T, SIG, false>(S, P, e, rx, ry, rz, nx, ny, nz, g0, g1);
         }
-        T ratio = R * fexp(u_new - u_old);
+        T ratio = R * fexp(du);
         T prob = ratio * ratio;
         if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
         if (prob != prob) flg |= FLAG_NONFINITE;
@@ -530,7 +597,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
             for (int j = 0; j < NS; ++j) {
                 T tj = 0;
 #pragma unroll
-                for (int k = 0; k < NS; ++k) tj += mn.v[k] * DI(k, j);
+                for (int k = 0; k < NS; ++k) tj += mv[k] * DI(k, j);
 #pragma unroll
                 for (int k = 0; k < NS; ++k) DI(k, j) -= cq[k] * tj;
             }

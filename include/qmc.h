@@ -252,6 +252,27 @@ int qmc_ctx_measure_peaks(qmc_ctx_t ctx, double* fp32_tflops, double* fp64_tflop
 int qmc_host_alloc(size_t bytes, void** out);
 int qmc_host_free(void* p);
 
+/* ---- allocation-free reduction (no counterpart in the reference) -------- */
+/* The FP64 compensated SR walker sums of qmc_logderiv_batch (sum E, sum E^2,
+ * sum O_p, sum E O_p, sum O_p O_q for p <= q, in that order; deterministic)
+ * over inputs that are already on the device, for callers that cannot
+ * allocate device memory: code between cudaStreamBeginCapture and
+ * cudaStreamEndCapture, hosts whose device memory belongs to another
+ * framework's allocator, latency-critical loops that cannot absorb
+ * cudaFree's implicit synchronisation.  It calls no allocator: its scratch
+ * is a static 512 KiB device array that every GPU loading the library holds
+ * until the process exits.
+ *   d_E [W], d_O [W x P] row-major, d_sums [2 + 2P + P(P+1)/2]: device pointers.
+ *   stream: a cudaStream_t, or NULL for the legacy default stream.
+ * Limits: P <= QMC_NOALLOC_MAX_PARAMS and 2 (2 + 2P + P(P+1)/2) ceil(W/256)
+ * <= 65536 (for P = 12, W <= 80640); larger sizes return QMC_ERR_ARG and a
+ * message on stderr.  The first call on each device looks up the scratch's
+ * device address (set-up); make that first call before any stream capture.
+ * All calls share the scratch: calls that overlap on the GPU (other streams,
+ * other host threads on the same device) race and must be serialised. */
+#define QMC_NOALLOC_MAX_PARAMS 16
+int qmc_sr_sums_noalloc(const double* d_E, const double* d_O, int W, int P, double* d_sums, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,7 @@ PROTOTYPES = {
     "qmc_ctx_measure_peaks": [_vp, _dp, _dp],
     "qmc_host_alloc": [C.c_size_t, C.POINTER(_vp)],
     "qmc_host_free": [_vp],
+    "qmc_sr_sums_noalloc": [_dp, _dp, C.c_int, C.c_int, _dp, _vp],
 }
 _RESTYPES = {"qmc_status_string": C.c_char_p}
 

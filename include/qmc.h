@@ -136,7 +136,8 @@ typedef struct {
     int precision;               /* QMC_FP64 / QMC_FP32_REFINE */
     int refresh_every;           /* FP64 inverse recompute + E_L measurement period (sweeps) */
     double e_ref_damping;        /* DMC kappa */
-    int reserved[6];
+    int fixed_node;              /* DMC: refuse sign-changing proposals (the reference accepts them) */
+    int reserved[5];
 } qmc_run_params;
 
 typedef struct {
@@ -226,6 +227,22 @@ int qmc_walkers_get_state(qmc_walkers_t wk, double* logabs, int* sign, double* e
  * (1 singular, 2 non-finite); cleared on read. */
 int qmc_walkers_status(qmc_walkers_t wk, int* flags);
 
+/* Walker set with room for `capacity` walkers (DMC populations grow and
+ * shrink); W is the initial population. */
+int qmc_walkers_create_dmc(qmc_sys_t sys, int W, int capacity, int precision, qmc_walkers_t* out);
+/* Current population size. */
+int qmc_walkers_count(qmc_walkers_t wk, int* W);
+/* One IS-DMC step (src/sampling/is_dmc.rs:208-302): one drift-diffusion sweep
+ * per walker (fixed-node rejection when fixed_node), E_L after the sweep (in
+ * the walkers' precision, FP64 when fp64_measure), copies
+ * m = min(floor(exp(tau (e_ref - (E_L + E_old)/2)) + xi), 3) with an FP64
+ * log-weight and a tag-4 Philox xi per (walker slot, step), and an
+ * order-stable on-device compaction.  *n_new receives the new population
+ * (0 = collapse), *e_mean its mean E_L.  QMC_ERR_POPULATION if the new
+ * population exceeds the capacity (the population is then left unchanged). */
+int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double max_drift, int fixed_node, double e_ref,
+                         uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean);
+
 /* ---- drivers --------------------------------------------------------------- */
 /* VMC run: MCMCSimulation::run (src/sampling/vmc.rs:69-92) for all-electron
  * moves, DriftDiffusionVMC::run (:405-484) for single-electron moves.  With
@@ -234,6 +251,15 @@ int qmc_walkers_status(qmc_walkers_t wk, int* flags);
  * (capacity n_steps). */
 int qmc_vmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed,
                 qmc_run_result* result, double* energies);
+
+/* ImportanceSampledDMC::run (src/sampling/is_dmc.rs:385-553) energy part:
+ * target population n_walkers (capacity 4x), n_burnin + n_steps steps of
+ * qmc_walkers_dmc_step, E_ref = <E_L> - kappa ln(N / N_target) / tau,
+ * collapse -> re-initialisation; energy = mean of the per-step mixed
+ * estimates, error by blocking (is_dmc.rs:556-607).  FP32 walkers measure
+ * E_L in FP64 every refresh_every steps. */
+int qmc_dmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed, qmc_run_result* result,
+                double* energies);
 
 /* ---- timing helpers (no reference counterpart; used by the benchmark) ---- */
 /* Records CUDA event `slot` (0..15) on the context's stream. */

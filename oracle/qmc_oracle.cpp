@@ -630,6 +630,53 @@ V3 limit_drift(V3 F, double tau, double max_drift) {   // src/sampling/vmc.rs:30
     return m > max_drift ? (max_drift / m) * d : d;
 }
 
+// One sweep of single-electron moves for one walker (move_kind 2 Gaussian,
+// 3 drift-diffusion), with the shared single-draw Philox layout.  With
+// fixed_node a proposal that changes the sign of psi is refused (the
+// reference's IS-DMC, src/sampling/is_dmc.rs:254, accepts it).
+int sweep_walker(const Sys& s, const std::vector<int>& order, std::vector<V3>& r, double& lp, int& sg, uint32_t wid,
+                 uint64_t st, int move_kind, double step, double tau, double max_drift, uint64_t seed, int fixed_node) {
+    int acc = 0;
+    int N = s.N;
+    for (int q = 0; q < N; ++q) {
+        int e = order[q];
+        U4 x = draw(seed, wid, st, (uint32_t)q, TAG_PROPOSE);
+        double n0, n1, n2, n3;
+        {
+            double rr = std::sqrt(-2.0 * std::log(u24(x.v[0] & 0xFFFFFFu)));
+            double t = 6.283185307179586476925286766559 * u24(x.v[1] & 0xFFFFFFu);
+            n0 = rr * std::cos(t); n1 = rr * std::sin(t);
+            rr = std::sqrt(-2.0 * std::log(u24(x.v[2] & 0xFFFFFFu)));
+            t = 6.283185307179586476925286766559 * u24(x.v[3] & 0xFFFFFFu);
+            n2 = rr * std::cos(t); n3 = rr * std::sin(t);
+        }
+        double uacc = u24((x.v[0] >> 24) | ((x.v[1] >> 24) << 8) | ((x.v[2] >> 24) << 16));
+        V3 eta{n0, n1, n2};
+        std::vector<V3> rn = r;
+        double logG = 0.0;
+        if (move_kind == 2) {
+            rn[e] = r[e] + step * eta;
+        } else {
+            Eval cur = evaluate_full(s, r);
+            V3 dl = limit_drift(2.0 * cur.grad[e], tau, max_drift);
+            rn[e] = r[e] + dl + std::sqrt(2.0 * tau) * eta;
+            Eval nw = evaluate_full(s, rn);
+            if (!nw.ok) continue;
+            V3 dn = limit_drift(2.0 * nw.grad[e], tau, max_drift);
+            V3 fd = rn[e] - r[e] - dl, bd = r[e] - rn[e] - dn;
+            logG = (-dot(bd, bd) + dot(fd, fd)) / (4.0 * tau);
+        }
+        int sgn;
+        bool okn;
+        double lpn = log_psi(s, rn, sgn, okn);
+        if (!okn) continue;
+        if (fixed_node && sgn != sg) continue;
+        double prob = std::exp(2.0 * (lpn - lp) + logG);
+        if (uacc < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
+    }
+    return acc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -776,43 +823,7 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
                 if (okn && u01(a.v[0]) < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
                 continue;
             }
-            for (int q = 0; q < N; ++q) {
-                int e = order[q];
-                // one Philox call per single-electron move: 24-bit uniforms
-                // (words 0-3, low 24 bits) for two Box-Muller pairs, and the
-                // top bytes of words 0-2 for the acceptance uniform
-                U4 x = draw(seed, wid, st, (uint32_t)q, TAG_PROPOSE);
-                double n0, n1, n2, n3;
-                {
-                    double r = std::sqrt(-2.0 * std::log(u24(x.v[0] & 0xFFFFFFu)));
-                    double t = 6.283185307179586476925286766559 * u24(x.v[1] & 0xFFFFFFu);
-                    n0 = r * std::cos(t); n1 = r * std::sin(t);
-                    r = std::sqrt(-2.0 * std::log(u24(x.v[2] & 0xFFFFFFu)));
-                    t = 6.283185307179586476925286766559 * u24(x.v[3] & 0xFFFFFFu);
-                    n2 = r * std::cos(t); n3 = r * std::sin(t);
-                }
-                double uacc = u24((x.v[0] >> 24) | ((x.v[1] >> 24) << 8) | ((x.v[2] >> 24) << 16));
-                V3 eta{n0, n1, n2};
-                std::vector<V3> rn = r;
-                double logG = 0.0;
-                if (move_kind == 2) {
-                    rn[e] = r[e] + step * eta;
-                } else {
-                    Eval cur = evaluate_full(s, r);
-                    V3 dl = limit_drift(2.0 * cur.grad[e], tau, max_drift);
-                    rn[e] = r[e] + dl + std::sqrt(2.0 * tau) * eta;
-                    Eval nw = evaluate_full(s, rn);
-                    if (!nw.ok) continue;
-                    V3 dn = limit_drift(2.0 * nw.grad[e], tau, max_drift);
-                    V3 fd = rn[e] - r[e] - dl, bd = r[e] - rn[e] - dn;
-                    logG = (-dot(bd, bd) + dot(fd, fd)) / (4.0 * tau);
-                }
-                int sgn; bool okn;
-                double lpn = log_psi(s, rn, sgn, okn);
-                if (!okn) continue;
-                double prob = std::exp(2.0 * (lpn - lp) + logG);
-                if (uacc < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
-            }
+            acc += sweep_walker(s, order, r, lp, sg, wid, st, move_kind, step, tau, max_drift, seed, 0);
         }
         for (int i = 0; i < N; ++i) {
             double* p = pos + ((size_t)w * N + i) * 3;
@@ -822,6 +833,75 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
         if (e_local) e_local[w] = evaluate_full(s, r).el;
     });
     return 0;
+}
+
+// Importance-sampled DMC (src/sampling/is_dmc.rs:208-302, 385-502) with the
+// shared Philox layout: per step one drift-diffusion sweep per walker
+// (walker id = its slot in the current population, step index = DMC step),
+// E_L after the sweep, copies m = min(floor(exp(tau (E_ref - (E_L + E_old)/2)) + xi), 3)
+// with xi from tag-4 draws, populations rebuilt in slot order, and
+// E_ref = <E_L> - kappa ln(N / N_target) / tau.  Stops early if the population
+// collapses or exceeds `cap`.  Returns the number of steps done; pos_out
+// receives the final population, pops/energies the per-step values.
+int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps, uint64_t step0, double tau,
+            double max_drift, int fixed_node, double kappa, int target, uint64_t seed, int cap, double* pos_out,
+            int* W_out, int* pops, double* energies, double* e_ref_io, int threads) {
+    Sys s = make_sys(d);
+    int N = s.N;
+    std::vector<int> order = visit_order(s);
+    std::vector<std::vector<V3>> R(W0);
+    std::vector<double> E(W0), lpv(W0);
+    std::vector<int> sgv(W0);
+    for (int w = 0; w < W0; ++w) R[w] = load_cfg(pos_in + (size_t)w * N * 3, N);
+    parallel_for(W0, threads, [&](int w) {
+        Eval e = evaluate_full(s, R[w]);
+        E[w] = e.el; lpv[w] = e.logabs; sgv[w] = e.sign;
+    });
+    double e_ref = *e_ref_io;
+    int t = 0;
+    for (; t < n_steps; ++t) {
+        uint64_t st = step0 + (uint64_t)t;
+        int W = (int)R.size();
+        std::vector<double> Eold = E;
+        parallel_for(W, threads, [&](int w) {
+            sweep_walker(s, order, R[w], lpv[w], sgv[w], (uint32_t)w, st, 3, 0.0, tau, max_drift, seed, fixed_node);
+            Eval e = evaluate_full(s, R[w]);
+            E[w] = e.el; lpv[w] = e.logabs; sgv[w] = e.sign;
+        });
+        std::vector<std::vector<V3>> R2;
+        std::vector<double> E2, lp2;
+        std::vector<int> sg2;
+        double esum = 0.0;
+        for (int w = 0; w < W; ++w) {
+            int m = 0;
+            if (std::isfinite(E[w]) && std::isfinite(Eold[w])) {
+                double wgt = std::exp(tau * (e_ref - 0.5 * (E[w] + Eold[w])));
+                U4 x = draw(seed, (uint32_t)w, st, 0, TAG_BRANCH);
+                double f = std::floor(wgt + u01(x.v[0]));
+                m = f >= 3.0 ? 3 : (int)f;
+                if (m < 0) m = 0;
+            }
+            for (int c = 0; c < m; ++c) {
+                R2.push_back(R[w]); E2.push_back(E[w]); lp2.push_back(lpv[w]); sg2.push_back(sgv[w]);
+                esum += E[w];
+            }
+        }
+        int Wn = (int)R2.size();
+        pops[t] = Wn;
+        if (Wn == 0 || Wn > cap) { energies[t] = 0.0; ++t; R.swap(R2); break; }
+        double em = esum / Wn;
+        energies[t] = em;
+        e_ref = em - kappa * std::log((double)Wn / (double)target) / tau;
+        R.swap(R2); E.swap(E2); lpv.swap(lp2); sgv.swap(sg2);
+    }
+    *W_out = (int)R.size();
+    for (size_t w = 0; w < R.size() && (int)w < cap; ++w)
+        for (int i = 0; i < N; ++i) {
+            double* p = pos_out + (w * N + i) * 3;
+            p[0] = R[w][i].x; p[1] = R[w][i].y; p[2] = R[w][i].z;
+        }
+    *e_ref_io = e_ref;
+    return t;
 }
 
 }  // extern "C"

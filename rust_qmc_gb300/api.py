@@ -230,10 +230,14 @@ class System:
 class Walkers:
     """Device-resident walker ensemble (qmc_walkers_*)."""
 
-    def __init__(self, system, W, precision=L.QMC_FP64):
+    def __init__(self, system, W, precision=L.QMC_FP64, capacity=None):
         self.sys, self.lib, self.W, self.precision = system, system.lib, W, precision
         h = C.c_void_p()
-        L.check(self.lib.qmc_walkers_create(system.h, W, precision, C.byref(h)), "qmc_walkers_create")
+        if capacity is None:
+            L.check(self.lib.qmc_walkers_create(system.h, W, precision, C.byref(h)), "qmc_walkers_create")
+        else:
+            L.check(self.lib.qmc_walkers_create_dmc(system.h, W, capacity, precision, C.byref(h)),
+                    "qmc_walkers_create_dmc")
         self.h = h
         system._children.add(self)
 
@@ -283,6 +287,21 @@ class Walkers:
         L.check(self.lib.qmc_walkers_get_state(self.h, _d(la), _i(sg), _d(el)), "qmc_walkers_get_state")
         return la, sg, el
 
+    def count(self):
+        n = C.c_int()
+        L.check(self.lib.qmc_walkers_count(self.h, C.byref(n)), "qmc_walkers_count")
+        self.W = n.value
+        return n.value
+
+    def dmc_step(self, tau, e_ref, seed, step, max_drift=1.0, fixed_node=True, fp64_measure=False):
+        """One IS-DMC step; returns (new population, mean E_L of it)."""
+        n, em = C.c_int(), C.c_double()
+        L.check(self.lib.qmc_walkers_dmc_step(self.h, tau, max_drift, int(bool(fixed_node)), e_ref, seed, step,
+                                              int(bool(fp64_measure)), C.byref(n), C.byref(em)),
+                "qmc_walkers_dmc_step")
+        self.W = n.value
+        return n.value, em.value
+
     def status(self):
         f = C.c_int()
         L.check(self.lib.qmc_walkers_status(self.h, C.byref(f)), "qmc_walkers_status")
@@ -301,3 +320,19 @@ def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_
     return dict(energy=res.energy, error=res.error, autocorrelation_time=res.autocorrelation_time,
                 acceptance_rate=res.acceptance_rate, variance=res.variance, n_samples=res.n_samples,
                 status_flags=res.status_flags, energies=energies[:res.n_samples])
+
+
+def dmc_run(system, *, n_walkers, n_steps, n_burnin=0, tau=0.005, max_drift=1.0, precision=L.QMC_FP64,
+            refresh_every=1, e_ref_damping=0.5, fixed_node=True, seed=1):
+    """ImportanceSampledDMC::run (energy part) on the device."""
+    p = L.RunParams()
+    p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = n_walkers, n_steps, n_burnin, L.QMC_MOVE_ONE_DRIFT
+    p.tau, p.max_drift, p.precision, p.refresh_every = tau, max_drift, precision, refresh_every
+    p.e_ref_damping, p.fixed_node = e_ref_damping, int(bool(fixed_node))
+    res = L.RunResult()
+    energies = np.zeros(n_steps)
+    L.check(system.lib.qmc_dmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_dmc_run")
+    return dict(energy=res.energy, error=res.error, autocorrelation_time=res.autocorrelation_time,
+                acceptance_rate=res.acceptance_rate, variance=res.variance, n_samples=res.n_samples,
+                status_flags=res.status_flags, avg_population=res.avg_population,
+                energies=energies[:res.n_samples])

@@ -47,6 +47,8 @@ struct qmc_sys_s {
 struct qmc_walkers_s {
     qmc_sys_s* sys = nullptr;
     DevWalkers dw;
+    DevWalkers alt;                        // DMC ping-pong population buffer
+    DevBranch br;
     double* d_stage = nullptr;             // caller-order positions [W][N][3]
     double* d_out = nullptr;               // generic device output scratch
     size_t d_out_cap = 0;
@@ -193,16 +195,15 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
     return QMC_OK;
 }
 
-int alloc_walkers(qmc_sys_s* sys, int W, int prec, qmc_walkers_s** out) {
-    if (W <= 0 || (prec != QMC_FP64 && prec != QMC_FP32_REFINE)) return QMC_ERR_ARG;
-    cudaSetDevice(sys->ctx->device);
-    qmc_walkers_s* wk = new (std::nothrow) qmc_walkers_s();
-    if (!wk) return QMC_ERR_NOMEM;
-    wk->sys = sys;
-    DevWalkers& dw = wk->dw;
-    const HostSys& hs = sys->hs;
+void free_dev(DevWalkers& dw) {
+    cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
+    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial);
+    dw = DevWalkers();
+}
+
+int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cudaStream_t st) {
     dw.W = W;
-    dw.Wcap = ((W + 127) / 128) * 128;
+    dw.Wcap = ((Wcap + 127) / 128) * 128;
     dw.prec = prec;
     size_t ts = prec == QMC_FP64 ? 8 : 4;
     int nm = nmax_of_shape(hs.shape);
@@ -218,26 +219,63 @@ int alloc_walkers(qmc_sys_s* sys, int W, int prec, qmc_walkers_s** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.flags, 4);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.acc, 8);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.partial, 8 * (size_t)dw.partial_cap);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&wk->d_stage, 8 * 3 * (size_t)hs.N * Wc);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dw.flags, 0, 4, sys->ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, sys->ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, sys->ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dw.dinv, 0, ts * 2 * nm * nm * Wc, sys->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.flags, 0, 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.el, 0, 8 * Wc, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.dinv, 0, ts * 2 * nm * nm * Wc, st);
+    if (e != cudaSuccess) { free_dev(dw); return cuda_rc(e); }
+    return QMC_OK;
+}
+
+int alloc_walkers(qmc_sys_s* sys, int W, int prec, qmc_walkers_s** out, int capacity = 0) {
+    if (W <= 0 || (prec != QMC_FP64 && prec != QMC_FP32_REFINE) || capacity < 0) return QMC_ERR_ARG;
+    cudaSetDevice(sys->ctx->device);
+    qmc_walkers_s* wk = new (std::nothrow) qmc_walkers_s();
+    if (!wk) return QMC_ERR_NOMEM;
+    wk->sys = sys;
+    const HostSys& hs = sys->hs;
+    int cap = std::max(W, capacity);
+    int rc = alloc_dev(wk->dw, hs, W, cap, prec, sys->ctx->stream);
+    if (rc) { delete wk; return rc; }
+    cudaError_t e = cudaMalloc((void**)&wk->d_stage, 8 * 3 * (size_t)hs.N * wk->dw.Wcap);
+    if (e != cudaSuccess) { free_dev(wk->dw); delete wk; return cuda_rc(e); }
+    *out = wk;
+    return QMC_OK;
+}
+
+// Lazily allocated DMC buffers: the second population buffer and the
+// branching scratch, both of the walker set's capacity.
+int ensure_dmc(qmc_walkers_s* wk) {
+    if (wk->br.cap) return QMC_OK;
+    const HostSys& hs = wk->sys->hs;
+    cudaStream_t st = wk->sys->ctx->stream;
+    CK(alloc_dev(wk->alt, hs, 0, wk->dw.Wcap, wk->dw.prec, st));
+    DevBranch& b = wk->br;
+    int cap = wk->dw.Wcap;
+    cudaError_t e = cudaMalloc((void**)&b.counts, 4 * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.offsets, 4 * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.el_old, 8 * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.stats, 8 * 4);
     if (e != cudaSuccess) {
-        cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
-        cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(wk->d_stage);
-        delete wk;
+        cudaFree(b.counts); cudaFree(b.offsets); cudaFree(b.el_old); cudaFree(b.stats);
+        b = DevBranch();
+        free_dev(wk->alt);
         return cuda_rc(e);
     }
-    *out = wk;
+    b.cap = cap;
     return QMC_OK;
 }
 
 void free_walkers(qmc_walkers_s* wk) {
     if (!wk) return;
-    DevWalkers& dw = wk->dw;
-    cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
-    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(wk->d_stage); cudaFree(wk->d_out);
+    free_dev(wk->dw);
+    if (wk->br.cap) {
+        free_dev(wk->alt);
+        cudaFree(wk->br.counts); cudaFree(wk->br.offsets); cudaFree(wk->br.el_old); cudaFree(wk->br.stats);
+    }
+    cudaFree(wk->d_stage);
+    cudaFree(wk->d_out);
     delete wk;
 }
 
@@ -308,6 +346,59 @@ double blocking_error(const std::vector<double>& x, double tau) {
     for (double v : m) var += (v - mu) * (v - mu);
     var /= (double)(nb - 1);
     return std::sqrt(var / (double)nb);
+}
+
+// Blocking error of the DMC energy series (src/sampling/is_dmc.rs:556-607).
+double dmc_block_error(const std::vector<double>& x) {
+    size_t n = x.size();
+    if (n < 20) return 0.0;
+    double mean = 0.0;
+    for (double v : x) mean += v;
+    mean /= (double)n;
+    double var = 0.0;
+    for (double v : x) var += (v - mean) * (v - mean);
+    var /= (double)n;
+    if (var < 1e-30) return 0.0;
+    double tau = autocorrelation_time(x);
+    size_t bs = (size_t)std::ceil(2.0 * tau);
+    size_t nb = x.size() / bs;
+    if (nb < 2) return std::sqrt(var * tau / (double)n);
+    return blocking_error(x, tau);
+}
+
+// One IS-DMC step on a resident population: save E_L, one drift-diffusion
+// sweep, E_L in the walkers' precision (FP64 when fp64_measure), branching
+// and compaction into the alternate buffer, swap.
+int dmc_step(qmc_walkers_s* wk, double tau, double max_drift, int fixed_node, double e_ref, uint64_t seed,
+             uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+    CK(ensure_dmc(wk));
+    const HostSys& hs = wk->sys->hs;
+    cudaStream_t st = wk->sys->ctx->stream;
+    DevWalkers& dw = wk->dw;
+    CU(cudaMemcpyAsync(wk->br.el_old, dw.el, 8 * (size_t)dw.W, cudaMemcpyDeviceToDevice, st));
+    dw.fixed_node = fixed_node;
+    int rc = launch_sweep(hs, dw, QMC_MOVE_ONE_DRIFT, 1, step, 0.0, tau, max_drift, seed, st);
+    dw.fixed_node = 0;
+    CK(rc);
+    MeasureOut none;
+    CK(launch_measure(hs, dw, (fp64_measure || dw.prec == QMC_FP64) ? 0 : 1, true, none, st));
+    CK(launch_branch(dw, wk->alt, wk->br, hs.N, nmax_of_shape(hs.shape), e_ref, tau, seed, step, st));
+    double stats[2] = {0, 0};
+    CU(cudaMemcpyAsync(stats, wk->br.stats, 16, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    int total = (int)stats[0];
+    *n_new = total;
+    *e_mean = total > 0 ? stats[1] / total : 0.0;
+    if (total > wk->alt.Wcap) return QMC_ERR_POPULATION;
+    if (total == 0) { dw.W = 0; return QMC_OK; }
+    // swap buffers (flags / accept counters stay with the walker set)
+    std::swap(dw.pos, wk->alt.pos);
+    std::swap(dw.dinv, wk->alt.dinv);
+    std::swap(dw.logabs, wk->alt.logabs);
+    std::swap(dw.sign, wk->alt.sign);
+    std::swap(dw.el, wk->alt.el);
+    dw.W = total;
+    return QMC_OK;
 }
 
 }  // namespace
@@ -564,6 +655,25 @@ int qmc_walkers_create(qmc_sys_t s, int W, int precision, qmc_walkers_t* out) {
     return alloc_walkers(s, W, precision, out);
 }
 
+int qmc_walkers_create_dmc(qmc_sys_t s, int W, int capacity, int precision, qmc_walkers_t* out) {
+    if (!s || !out || capacity < W) return QMC_ERR_ARG;
+    *out = nullptr;
+    return alloc_walkers(s, W, precision, out, capacity);
+}
+
+int qmc_walkers_count(qmc_walkers_t wk, int* W) {
+    if (!wk || !W) return QMC_ERR_ARG;
+    *W = wk->dw.W;
+    return QMC_OK;
+}
+
+int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double max_drift, int fixed_node, double e_ref,
+                         uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+    if (!wk || !n_new || !e_mean || !(tau > 0) || !(max_drift > 0) || wk->dw.W <= 0) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    return dmc_step(wk, tau, max_drift, fixed_node, e_ref, seed, step, fp64_measure, n_new, e_mean);
+}
+
 int qmc_walkers_destroy(qmc_walkers_t wk) {
     if (!wk) return QMC_ERR_ARG;
     cudaSetDevice(wk->sys->ctx->device);
@@ -726,6 +836,83 @@ int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     res->n_samples = (int)series.size();
     res->status_flags = flags;
     if (energies) for (size_t i = 0; i < series.size(); ++i) energies[i] = series[i];
+    return QMC_OK;
+}
+
+int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies) {
+    if (!s || !p || !res) return QMC_ERR_ARG;
+    if (p->n_walkers <= 0 || p->n_steps <= 0 || p->n_burnin < 0 || !(p->tau > 0) || !(p->max_drift > 0)) return QMC_ERR_ARG;
+    std::memset(res, 0, sizeof(*res));
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    const HostSys& hs = s->hs;
+    const int target = p->n_walkers;
+    qmc_walkers_s* wk = nullptr;
+    CK(alloc_walkers(s, target, p->precision, &wk, 4 * target));
+    struct Guard { qmc_walkers_s* w; ~Guard() { if (w) { cudaStreamSynchronize(w->sys->ctx->stream); free_walkers(w); } } } guard{wk};
+    const double kappa = p->e_ref_damping > 0 ? p->e_ref_damping : 0.5;
+    const int every = p->refresh_every > 0 ? p->refresh_every : 1;
+    auto reinit = [&](uint64_t key, double& e_ref) -> int {
+        wk->dw.W = target;
+        CK(launch_init(hs, wk->dw, key, st));
+        MeasureOut none;
+        CK(launch_measure(hs, wk->dw, 0, true, none, st));
+        double esum = 0.0;
+        CU(cudaMemcpyAsync(&esum, wk->dw.partial + wk->dw.partial_cap - 1, 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        e_ref = esum / target;                           // initial E_ref = <E_L>, is_dmc.rs:397-398
+        return QMC_OK;
+    };
+    double e_ref = 0.0;
+    CK(reinit(seed, e_ref));
+    CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+    std::vector<double> series;
+    double pop_sum = 0.0;
+    long long moves = 0;
+    unsigned long long acc_burn = 0;
+    int collapses = 0;
+    const int total_steps = p->n_burnin + p->n_steps;
+    for (int t = 0; t < total_steps; ++t) {
+        if (t == p->n_burnin) {
+            CU(cudaMemcpyAsync(&acc_burn, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+            CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+        }
+        int Wcur = wk->dw.W, n_new = 0;
+        double em = 0.0;
+        int fp64 = ((t + 1) % every) == 0;
+        CK(dmc_step(wk, p->tau, p->max_drift, p->fixed_node, e_ref, seed, (uint64_t)t, fp64, &n_new, &em));
+        if (t >= p->n_burnin) moves += (long long)Wcur * hs.N;
+        if (n_new == 0) {                                // collapse: re-initialise, is_dmc.rs:428-437
+            ++collapses;
+            CK(reinit(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(collapses), e_ref));
+            continue;
+        }
+        if (t >= p->n_burnin) {
+            series.push_back(em);
+            pop_sum += n_new;
+        }
+        e_ref = em - kappa * std::log((double)n_new / (double)target) / p->tau;   // is_dmc.rs:489-490
+    }
+    unsigned long long acc = 0;
+    int flags = 0;
+    CU(cudaMemcpyAsync(&acc, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&flags, wk->dw.flags, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    double mean = 0.0;
+    for (double v : series) mean += v;
+    if (!series.empty()) mean /= (double)series.size();
+    double var = 0.0;
+    for (double v : series) var += (v - mean) * (v - mean);
+    res->energy = mean;
+    res->variance = series.empty() ? 0.0 : var / (double)series.size();
+    res->autocorrelation_time = autocorrelation_time(series);
+    res->error = dmc_block_error(series);
+    res->acceptance_rate = moves ? (double)acc / (double)moves : 0.0;
+    res->n_samples = (int)series.size();
+    res->status_flags = flags | (collapses ? 4 : 0);
+    res->avg_population = p->n_steps ? pop_sum / (double)p->n_steps : 0.0;
+    if (energies) for (size_t i = 0; i < series.size(); ++i) energies[i] = series[i];
+    (void)acc_burn;
     return QMC_OK;
 }
 

@@ -69,6 +69,16 @@ struct DevWalkers {
     unsigned long long* acc = nullptr;   // [1] accepted-move counter
     double* partial = nullptr;           // reduction scratch
     int partial_cap = 0;
+    int fixed_node = 0;                  // sweeps refuse sign-changing proposals (DMC)
+};
+
+// Device buffers of the DMC branching step (population control).
+struct DevBranch {
+    int cap = 0;
+    int* counts = nullptr;               // [cap] copies per walker
+    int* offsets = nullptr;              // [cap] exclusive scan
+    double* el_old = nullptr;            // [cap] E_L before the sweep
+    double* stats = nullptr;             // [4] total copies, sum m E (compensated), flags
 };
 
 struct MeasureOut {
@@ -97,6 +107,11 @@ int launch_walker_sum(const double* X, int W, int ncol, double* d_out, double* d
 int launch_sr_sums(const double* E, const double* O, int W, int P, double* d_out,
                    double* d_scratch, int scratch_cap, cudaStream_t st);
 int launch_flush(void* buf, size_t bytes, cudaStream_t st);
+// DMC branching (src/sampling/is_dmc.rs:278-302): copies per walker from the
+// FP64 log-weight, exclusive scan, order-stable gather into `dst`.
+// stats[0] = new population, stats[1] = sum of copies x E_L, stats[2] = flags.
+int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, int nmax, double e_ref,
+                  double tau, uint64_t seed, uint64_t step, cudaStream_t st);
 
 extern long long g_launch_count;
 

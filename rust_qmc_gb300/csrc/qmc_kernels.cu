@@ -223,6 +223,121 @@ int launch_sum_partials(const double* partial, int nblk, int nrows, double* out,
 }
 
 
+// ---------------------------------------------------------------------------
+// DMC branching (src/sampling/is_dmc.rs:278-302) with on-device compaction.
+// ---------------------------------------------------------------------------
+// Copies per walker: m = min(floor(exp(tau (E_ref - (E_L + E_old)/2)) + xi), 3),
+// FP64 log-weight, xi from the tag-4 Philox draw of (walker slot, step).
+// Walkers with a non-finite energy get no copy.
+__global__ void k_branch_counts(const double* __restrict__ el, const double* __restrict__ el_old, int W,
+                                double e_ref, double tau, uint64_t seed, uint64_t step, int* __restrict__ counts,
+                                int* flags) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    double e = el[w], eo = el_old[w];
+    int m = 0;
+    if (isfinite(e) && isfinite(eo)) {
+        double logw = tau * (e_ref - 0.5 * (e + eo));
+        U4 x = rng_draw(seed, (uint32_t)w, step, 0, TAG_BRANCH);
+        double f = floor(exp(logw) + to_u01(x.x, 0.0));
+        m = f >= 3.0 ? 3 : (f <= 0.0 ? 0 : (int)f);
+    } else {
+        atomicOr(flags, FLAG_NONFINITE);
+    }
+    counts[w] = m;
+}
+
+// One block: exclusive scan of the counts (offsets), the new population size
+// and the compensated sum of copies x E_L, in a fixed order.
+__global__ void __launch_bounds__(1024) k_branch_scan(const int* __restrict__ counts, const double* __restrict__ el,
+                                                      int W, int* __restrict__ offsets, double* __restrict__ stats) {
+    __shared__ int ssum[1024];
+    __shared__ double se[1024], sc[1024];
+    const int t = threadIdx.x;
+    const int per = (W + 1023) / 1024;
+    const int b = min(W, t * per), e = min(W, b + per);
+    int local = 0;
+    Comp ce{0.0, 0.0};
+    for (int i = b; i < e; ++i) {
+        int c = counts[i];
+        local += c;
+        if (c) ce = comp_add(ce, Comp{(double)c * el[i], 0.0});
+    }
+    ssum[t] = local;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int v = t >= off ? ssum[t - off] : 0;
+        __syncthreads();
+        ssum[t] += v;
+        __syncthreads();
+    }
+    int run = ssum[t] - local;
+    for (int i = b; i < e; ++i) { offsets[i] = run; run += counts[i]; }
+    se[t] = ce.s;
+    sc[t] = ce.c;
+    __syncthreads();
+    for (int o = 512; o > 0; o >>= 1) {
+        if (t < o) {
+            Comp x = comp_add(Comp{se[t], sc[t]}, Comp{se[t + o], sc[t + o]});
+            se[t] = x.s;
+            sc[t] = x.c;
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        stats[0] = (double)ssum[1023];
+        stats[1] = se[0] + sc[0];
+    }
+}
+
+// Order-stable gather: destination slot d takes the walker w with
+// offsets[w] <= d < offsets[w] + counts[w] (the last w with offsets[w] <= d).
+template <class TS>
+__global__ void k_branch_gather(const int* __restrict__ offsets, int W, const double* __restrict__ stats, int cap,
+                                const TS* __restrict__ spos, const TS* __restrict__ sdinv,
+                                const double* __restrict__ slog, const int* __restrict__ ssign,
+                                const double* __restrict__ sel, int sWcap, TS* __restrict__ dpos,
+                                TS* __restrict__ ddinv, double* __restrict__ dlog, int* __restrict__ dsign,
+                                double* __restrict__ del, int dWcap, int npos, int ndinv) {
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    int total = (int)stats[0];
+    if (d >= total || d >= cap) return;
+    int lo = 0, hi = W - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (offsets[mid] <= d) lo = mid; else hi = mid - 1;
+    }
+    const int w = lo;
+    for (int i = 0; i < npos; ++i) dpos[(size_t)i * dWcap + d] = spos[(size_t)i * sWcap + w];
+    for (int i = 0; i < ndinv; ++i) ddinv[(size_t)i * dWcap + d] = sdinv[(size_t)i * sWcap + w];
+    dlog[d] = slog[w];
+    dsign[d] = ssign[w];
+    del[d] = sel[w];
+}
+
+int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, int nmax, double e_ref, double tau,
+                  uint64_t seed, uint64_t step, cudaStream_t st) {
+    int W = src.W;
+    if (W <= 0 || W > br.cap) return 1;
+    k_branch_counts<<<(W + 255) / 256, 256, 0, st>>>(src.el, br.el_old, W, e_ref, tau, seed, step, br.counts,
+                                                       src.flags);
+    k_branch_scan<<<1, 1024, 0, st>>>(br.counts, src.el, W, br.offsets, br.stats);
+    int most = std::min(3 * W, dst.Wcap);
+    int npos = 3 * n_elec, ndinv = 2 * nmax * nmax;
+    if (src.prec == 0)
+        k_branch_gather<double><<<(most + 127) / 128, 128, 0, st>>>(
+            br.offsets, W, br.stats, dst.Wcap, (const double*)src.pos, (const double*)src.dinv, src.logabs,
+            src.sign, src.el, src.Wcap, (double*)dst.pos, (double*)dst.dinv, dst.logabs, dst.sign, dst.el, dst.Wcap,
+            npos, ndinv);
+    else
+        k_branch_gather<float><<<(most + 127) / 128, 128, 0, st>>>(
+            br.offsets, W, br.stats, dst.Wcap, (const float*)src.pos, (const float*)src.dinv, src.logabs,
+            src.sign, src.el, src.Wcap, (float*)dst.pos, (float*)dst.dinv, dst.logabs, dst.sign, dst.el, dst.Wcap,
+            npos, ndinv);
+    g_launch_count += 3;
+    return cuda_status(cudaGetLastError());
+}
+
 // FMA-chain kernels used to measure the SIMT peaks (roofline denominators for
 // the compute-bound sweep kernels).  8 independent chains per thread.
 template <class T>

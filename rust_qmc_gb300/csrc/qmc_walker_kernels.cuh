@@ -526,8 +526,8 @@ __global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH
 // barrier is needed.
 template <class SH, class T, int SIG, int MOVE, int TPB>
 __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, int t, uint32_t w, uint64_t st,
-                                             uint64_t seed, T step, T tau, T maxd, int& sgn, unsigned& acc,
-                                             int& flg) {
+                                             uint64_t seed, T step, T tau, T maxd, int fixed_node, int& sgn,
+                                             unsigned& acc, int& flg) {
     constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
     constexpr int NM = SH::NMAX;
     auto P = [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; };
@@ -585,7 +585,8 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
         T prob = ratio * ratio;
         if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
         if (prob != prob) flg |= FLAG_NONFINITE;
-        if (md.uacc < prob && R != T(0)) {
+        // fixed-node rejection: a proposal that changes the sign of psi is refused
+        if (md.uacc < prob && R != T(0) && !(fixed_node && R < T(0))) {
             sp[(3 * e + 0) * TPB + t] = nx;
             sp[(3 * e + 1) * TPB + t] = ny;
             sp[(3 * e + 2) * TPB + t] = nz;
@@ -616,7 +617,8 @@ template <class SH, class T, int MOVE, int TPB>
 __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
                                                    T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
                                                    int n_sweeps, uint64_t step0, T step, T tau, T maxd,
-                                                   uint64_t seed, unsigned long long* acc_out, int* flags) {
+                                                   uint64_t seed, unsigned long long* acc_out, int* flags,
+                                                   int fixed_node) {
     extern __shared__ __align__(16) unsigned char smraw[];
     constexpr int NM = SH::NMAX;
     T* sp = reinterpret_cast<T*>(smraw);
@@ -633,8 +635,8 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
     int flg = 0;
     for (int it = 0; it < n_sweeps; ++it) {
         uint64_t st = step0 + (uint64_t)it;
-        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, sgn, acc, flg);
-        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, sgn, acc, flg);
+        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn, acc, flg);
+        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn, acc, flg);
     }
 #pragma unroll
     for (int i = 0; i < 3 * SH::NE; ++i) gpos[(size_t)i * Wcap + w] = sp[i * TPB + t];
@@ -788,7 +790,7 @@ struct ShapeOps {
         }
         int nb = (dw.W + TPB - 1) / TPB;
         kern<<<nb, TPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W, dw.Wcap, n, s0, (T)step, (T)tau,
-                                    (T)maxd, seed, dw.acc, dw.flags);
+                                    (T)maxd, seed, dw.acc, dw.flags, dw.fixed_node);
         ++g_launch_count;
         return cuda_status(cudaGetLastError());
     }

@@ -234,3 +234,59 @@ def test_vmc_run_precisions_agree_ch4(ctx):
     a, b = res[L.QMC_FP64], res[L.QMC_FP32_REFINE]
     sig = np.hypot(max(a["error"], 1e-6), max(b["error"], 1e-6))
     assert abs(a["energy"] - b["energy"]) < 4 * sig + 1e-3 * abs(a["energy"]), (a, b)
+
+
+@pytest.mark.parametrize("name,fixed_node", [("h2", True), ("ch4_min", True), ("li_ref", False)])
+def test_fp64_dmc_population_matches_oracle(ctx, oracle, name, fixed_node):
+    """IS-DMC branching + compaction: the FP64 device population follows the
+    oracle's reference-algorithm DMC step for step (same Philox stream,
+    order-stable copies), so populations and mean energies agree."""
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    target, n_steps, tau = 48, 6, 0.02
+    wk = Q.Walkers(sysh, target, L.QMC_FP64, capacity=4 * target)
+    wk.init(seed=21)
+    e_sum = wk.refresh()
+    e_ref = e_sum / target
+    pos0 = wk.get_positions()
+    pops, ens = [], []
+    er = e_ref
+    for t in range(n_steps):
+        n, em = wk.dmc_step(tau, er, seed=77, step=t, fixed_node=fixed_node)
+        assert n > 0
+        pops.append(n)
+        ens.append(em)
+        er = em - 0.5 * np.log(n / target) / tau
+    _, pops_o, ens_o, er_o = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node)
+    assert list(pops) == list(pops_o)
+    np.testing.assert_allclose(ens, ens_o, rtol=1e-9, atol=1e-9)
+    got = wk.get_positions()
+    want, _, _, _ = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node)
+    np.testing.assert_allclose(got, want, atol=1e-8)
+
+
+def test_dmc_run_h2_energy(ctx):
+    """Fixed-node DMC of H2 (nodeless ground state): the energy lies below the
+    VMC energy of the same trial function and near the exact -1.1745 Ha
+    (time-step and population bias allowed)."""
+    sysh = Q.System(ctx, Q.h2_mo())
+    d = Q.dmc_run(sysh, n_walkers=2048, n_steps=400, n_burnin=200, tau=0.01, seed=3)
+    v = Q.vmc_run(sysh, n_walkers=2048, n_steps=400, n_burnin=100, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0, seed=4)
+    assert -1.19 < d["energy"] < -1.16, d
+    assert d["energy"] < v["energy"] + 3 * (d["error"] + v["error"])
+    assert 1500 < d["avg_population"] < 2700
+    assert 0.9 < d["acceptance_rate"] <= 1.0
+
+
+def test_dmc_precisions_agree_ch4(ctx):
+    """FP32+refine and FP64 DMC populations give statistically compatible
+    energies; the FP32 form measures E_L in FP64 every 8 steps."""
+    sysh = Q.System(ctx, Q.methane_minimal())
+    r = {}
+    for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
+        r[prec] = Q.dmc_run(sysh, n_walkers=4096, n_steps=120, n_burnin=40, tau=0.005, precision=prec,
+                            refresh_every=8, seed=5 + prec)
+    a, b = r[L.QMC_FP64], r[L.QMC_FP32_REFINE]
+    assert np.isfinite(a["energy"]) and np.isfinite(b["energy"])
+    sig = np.hypot(max(a["error"], 1e-4), max(b["error"], 1e-4))
+    assert abs(a["energy"] - b["energy"]) < 5 * sig + 2e-3 * abs(a["energy"]), (a, b)

@@ -191,6 +191,9 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
     if (hs.N == 3 && hs.n_up == 2 && hs.n_nuc == 1 && hs.basis == QMC_BASIS_STO && hs.jk == QMC_JAS_PADE_F) hs.shape = SHAPE_LI;
     if (hs.N == 10 && hs.n_up == 5 && hs.n_nuc == 5 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN)
         hs.shape = layout_matches_ch4min(hs) ? SHAPE_CH4MIN : SHAPE_CH4;
+    if (hs.N == 42 && hs.n_up == 21 && hs.n_nuc == 12 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN &&
+        hs.n_ao <= 64)
+        hs.shape = SHAPE_C6H6;
     if (hs.shape < 0) return QMC_ERR_UNSUPPORTED;
     return QMC_OK;
 }
@@ -509,6 +512,8 @@ int qmc_system_destroy(qmc_sys_t s) {
     free_walkers(s->scratch[0]);
     free_walkers(s->scratch[1]);
     cudaFree(s->d_perm);
+    cudaFree(s->hs.dev_table[0]);
+    cudaFree(s->hs.dev_table[1]);
     delete s;
     return QMC_OK;
 }
@@ -531,6 +536,7 @@ int qmc_system_set_params(qmc_sys_t s, const double* p, int P) {
     for (int i = 0; i < P; ++i) if (!std::isfinite(p[i])) return QMC_ERR_ARG;
     for (int i = 0; i < 8; ++i) s->hs.jas[i] = p[i];
     for (size_t q = 0; q < s->hs.rot_angle.size(); ++q) s->hs.rot_angle[q] = p[8 + q];
+    s->hs.version++;
     return QMC_OK;
 }
 
@@ -539,6 +545,7 @@ int qmc_system_set_nuclei(qmc_sys_t s, const double* R, int n_nuc) {
     for (int i = 0; i < 3 * n_nuc; ++i) if (!std::isfinite(R[i])) return QMC_ERR_ARG;
     s->hs.R.assign(R, R + 3 * n_nuc);
     HostSys& hs = s->hs;
+    hs.version++;
     hs.v_nn = 0.0;
     for (int I = 0; I < hs.n_nuc; ++I)
         for (int J = I + 1; J < hs.n_nuc; ++J) {

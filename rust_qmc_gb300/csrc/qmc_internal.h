@@ -11,7 +11,7 @@ namespace qmc {
 // Kernel shapes compiled into the library.  A shape fixes the electron
 // counts and nucleus count at compile time so per-walker arrays live in
 // registers / shared memory with static indices.
-enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_CH4MIN = 3, SHAPE_COUNT = 4 };
+enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_CH4MIN = 3, SHAPE_C6H6 = 4, SHAPE_COUNT = 5 };
 
 // A basis shell: primitives shared by up to two s-type AOs and one p triplet
 // (the SP shells of 6-31G share exponents between 2s and 2p; Li's STO-7G 1s
@@ -48,6 +48,9 @@ struct HostSys {
     std::vector<int> init_nuc;           // caller order
     double init_sigma = 0.5;
     double v_nn = 0.0;
+    int version = 0;                     // bumped when parameters or nuclei change
+    mutable void* dev_table[2] = {nullptr, nullptr};     // cached device tables (warp kernels)
+    mutable int dev_table_version[2] = {-1, -1};
 
     int n_params() const { return 8 + (int)rot_occ.size(); }
     // Effective (rotated) MO coefficients in caller AO order.

@@ -31,6 +31,7 @@ QMC_DECLARE_SHAPE(h2)
 QMC_DECLARE_SHAPE(li)
 QMC_DECLARE_SHAPE(ch4)
 QMC_DECLARE_SHAPE(ch4min)
+QMC_DECLARE_SHAPE(c6h6)
 
 // The compile-time CH4 layout has no all-electron kernels of its own.
 int shape_step_all_ch4min(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, uint64_t seed,
@@ -56,6 +57,7 @@ bool layout_matches_ch4min(const HostSys& hs) {
         case SHAPE_LI: return CALL(li);                \
         case SHAPE_CH4: return CALL(ch4);              \
         case SHAPE_CH4MIN: return CALL(ch4min);        \
+        case SHAPE_C6H6: return CALL(c6h6);            \
     }                                                  \
     return 7;
 

@@ -1,0 +1,702 @@
+// qmc_warp_kernels.cuh -- warp-per-walker kernels for systems with large spin
+// sectors (benzene: 21x21 determinants, 42 electrons, 36 Gaussian AOs).
+//
+// One warp owns one walker.  Lane j holds column j of each inverse Slater
+// matrix in registers (Dinv[k][j], k = 0..n-1) and the positions of
+// electrons j and j+32.  AOs are evaluated lane-parallel from tables in
+// shared memory; the AO->MO contraction, the determinant ratio and the
+// Sherman-Morrison update broadcast one lane's values with shuffles, so every
+// register index stays static.  The FP64 refresh is a warp-cooperative
+// Gauss-Jordan elimination in which lane j carries column j of [D | I] and
+// ends holding column j of D^-1 -- exactly the sweep kernel's layout.
+#pragma once
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include "qmc_internal.h"
+#include "qmc_device.cuh"
+
+namespace qmc {
+
+constexpr int WMAX_AO = 64;       // two rounds of 32 AOs
+constexpr int WMAX_PRIM = 256;
+constexpr int WMAX_NUC = 16;
+
+// Shared-memory system table of the warp kernels (one copy per block).
+template <class T>
+struct SysW {
+    int n_ao;
+    int quirk_lap;
+    T F, invF, qa, v_nn;
+    T b_ee[2], a_ee[2];
+    T nuc[WMAX_NUC][3];
+    T Z[WMAX_NUC], enA[WMAX_NUC], enB[WMAX_NUC];
+    int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];   // type 0 s, 1..3 p_x..p_z
+    T pexp[WMAX_PRIM], pcoef[WMAX_PRIM];
+    T C[2][WMAX_AO][32];        // [sector][AO][column]
+    T init_sigma;
+    int init_nuc[64];           // internal electron order
+    int perm[64];
+};
+
+template <class T>
+static bool fill_sysw(const HostSys& hs, int NE, int NUP, int NNUC, SysW<T>& S) {
+    std::memset(&S, 0, sizeof(S));
+    if (hs.N != NE || hs.n_up != NUP || hs.n_nuc != NNUC || hs.n_ao > WMAX_AO || NNUC > WMAX_NUC) return false;
+    if (hs.basis != BASIS_GTO) return false;
+    S.n_ao = hs.n_ao;
+    S.quirk_lap = (hs.quirks & 2) ? 1 : 0;
+    S.F = (T)hs.F;
+    S.invF = (T)(1.0 / hs.F);
+    S.qa = (hs.quirks & 1) ? (T)hs.F : (T)1;
+    S.v_nn = (T)hs.v_nn;
+    S.b_ee[0] = (T)hs.jas[0]; S.b_ee[1] = (T)hs.jas[1];
+    S.a_ee[0] = (T)hs.jas[2]; S.a_ee[1] = (T)hs.jas[3];
+    for (int I = 0; I < NNUC; ++I) {
+        for (int c = 0; c < 3; ++c) S.nuc[I][c] = (T)hs.R[3 * I + c];
+        S.Z[I] = (T)hs.Z[I];
+        int sp = hs.species[I];
+        S.enA[I] = (T)(hs.jas[6 + sp] * hs.Z[I]);
+        S.enB[I] = (T)hs.jas[4 + sp];
+    }
+    // AOs in internal (shell) order; each AO keeps its own primitive list
+    int np = 0;
+    for (const HostShell& sh : hs.shells) {
+        auto put = [&](int caller_ao, int type, const std::vector<double>& coef) -> bool {
+            int a = hs.ao_int[caller_ao];
+            if ((int)(np + sh.exps.size()) > WMAX_PRIM) return false;
+            S.ao_nuc[a] = sh.nuc;
+            S.ao_type[a] = type;
+            S.ao_p0[a] = np;
+            S.ao_np[a] = (int)sh.exps.size();
+            for (size_t p = 0; p < sh.exps.size(); ++p) { S.pexp[np] = (T)sh.exps[p]; S.pcoef[np] = (T)coef[p]; ++np; }
+            return true;
+        };
+        for (int k = 0; k < 2; ++k)
+            if (sh.s_ao[k] >= 0 && !put(sh.s_ao[k], 0, sh.s_coef[k])) return false;
+        if (sh.p_ao[0] >= 0)
+            for (int m = 0; m < 3; ++m)
+                if (!put(sh.p_ao[m], 1 + m, sh.p_coef)) return false;
+    }
+    std::vector<double> Ce = hs.effective_mo();
+    for (int sig = 0; sig < 2; ++sig) {
+        int col = 0;
+        for (int ei = 0; ei < hs.N; ++ei) {
+            int e = hs.perm[ei];
+            if ((hs.spins[e] > 0) != (sig == 0)) continue;
+            int k = hs.occ[e];
+            for (int a = 0; a < hs.n_ao; ++a) S.C[sig][hs.ao_int[a]][col] = (T)Ce[(size_t)k * hs.n_ao + a];
+            ++col;
+        }
+    }
+    S.init_sigma = (T)hs.init_sigma;
+    for (int ei = 0; ei < hs.N; ++ei) {
+        S.perm[ei] = hs.perm[ei];
+        S.init_nuc[ei] = hs.init_nuc[hs.perm[ei]];
+    }
+    return true;
+}
+
+// Copy the table from global to shared memory (whole block).
+template <class T>
+__device__ __forceinline__ void load_sysw(SysW<T>* dst, const SysW<T>* __restrict__ src) {
+    const int4* s = reinterpret_cast<const int4*>(src);
+    int4* d = reinterpret_cast<int4*>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(SysW<T>) / sizeof(int4)); i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Lane-parallel AO evaluation: lane l evaluates AO l (round 0) and AO l+32
+// (round 1) at point (x,y,z): value, gradient, Laplacian (MODE >= 1 / 2).
+// ---------------------------------------------------------------------------
+template <class T, int MODE>
+struct AOLane {
+    T v[2], gx[2], gy[2], gz[2], l[2];
+};
+
+template <class T, int MODE>
+__device__ __forceinline__ void ao_lane(const SysW<T>& S, T x, T y, T z, int lane, AOLane<T, MODE>& o) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int a = lane + 32 * r;
+        T v = 0, gxx = 0, gyy = 0, gzz = 0, lp = 0;
+        if (a < S.n_ao) {
+            const int I = S.ao_nuc[a], type = S.ao_type[a], p0 = S.ao_p0[a], np = S.ao_np[a];
+            T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+            T r2 = dx * dx + dy * dy + dz * dz;
+            T s0 = 0, s1 = 0, s2 = 0;
+            for (int p = p0; p < p0 + np; ++p) {
+                T al = S.pexp[p];
+                T e = S.pcoef[p] * fexp(-al * r2);
+                s0 += e;
+                if (MODE >= 1) s1 += al * e;
+                if (MODE >= 2) s2 += al * al * e;
+            }
+            // s: chi = R; grad = -2 R1 dr; lap = -6 R1 + 4 r^2 R2
+            // p_m: chi = x_m R; grad = x_m(-2 R1 dr) + e_m R; lap = x_m(-10 R1 + 4 r^2 R2)
+            T ang = type == 0 ? T(1) : (type == 1 ? dx : (type == 2 ? dy : dz));
+            v = ang * s0;
+            if (MODE >= 1) {
+                T g = -2 * s1 * ang;
+                gxx = g * dx + (type == 1 ? s0 : T(0));
+                gyy = g * dy + (type == 2 ? s0 : T(0));
+                gzz = g * dz + (type == 3 ? s0 : T(0));
+            }
+            if (MODE >= 2) lp = ang * ((type == 0 ? T(-6) : T(-10)) * s1 + 4 * r2 * s2);
+        }
+        o.v[r] = v;
+        if (MODE >= 1) { o.gx[r] = gxx; o.gy[r] = gyy; o.gz[r] = gzz; }
+        if (MODE >= 2) o.l[r] = lp;
+    }
+}
+
+__device__ __forceinline__ float wshfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double wshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ int wshfl(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+template <class T>
+__device__ __forceinline__ T wsum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// MO contraction: lane k receives phi_k = sum_a C[sig][a][k] chi_a (and
+// gradient / Laplacian), chi_a broadcast from lane a % 32.
+template <class T, int MODE>
+__device__ __forceinline__ void mo_lane(const SysW<T>& S, int sig, int lane, const AOLane<T, MODE>& ao, T& v, T& gx,
+                                        T& gy, T& gz, T& l) {
+    v = 0; gx = 0; gy = 0; gz = 0; l = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int base = 32 * r;
+        if (base >= S.n_ao) break;
+        const int cnt = min(32, S.n_ao - base);
+        for (int t = 0; t < cnt; ++t) {
+            T c = S.C[sig][base + t][lane];
+            v += c * wshfl(ao.v[r], t);
+            if (MODE >= 1) {
+                gx += c * wshfl(ao.gx[r], t);
+                gy += c * wshfl(ao.gy[r], t);
+                gz += c * wshfl(ao.gz[r], t);
+            }
+            if (MODE >= 2) l += c * wshfl(ao.l[r], t);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+template <class TS>
+__global__ void kw_init(const SysW<double>* __restrict__ Sg, TS* __restrict__ pos, int NE, int W, int Wcap,
+                        uint64_t seed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NE * W) return;
+    int e = i / W, w = i - e * W;
+    const SysW<double>& S = *Sg;
+    U4 x = rng_draw(seed, (uint32_t)w, 0, (uint32_t)S.perm[e], TAG_INIT);
+    double n0, n1, n2, n3;
+    bm(x.x, x.y, n0, n1);
+    bm(x.z, x.w, n2, n3);
+    int c = S.init_nuc[e];
+    double cx = c >= 0 ? S.nuc[c][0] : 0.0, cy = c >= 0 ? S.nuc[c][1] : 0.0, cz = c >= 0 ? S.nuc[c][2] : 0.0;
+    pos[(3 * e + 0) * (size_t)Wcap + w] = (TS)(cx + S.init_sigma * n0);
+    pos[(3 * e + 1) * (size_t)Wcap + w] = (TS)(cy + S.init_sigma * n1);
+    pos[(3 * e + 2) * (size_t)Wcap + w] = (TS)(cz + S.init_sigma * n2);
+}
+
+// Positions of electrons `lane` and `lane + 32` live in this lane.
+template <class T, int NE>
+struct LanePos {
+    T x[2], y[2], z[2];
+    __device__ __forceinline__ void get(int e, T& ex, T& ey, T& ez) const {
+        T a = e < 32 ? x[0] : x[1], b = e < 32 ? y[0] : y[1], c = e < 32 ? z[0] : z[1];
+        ex = wshfl(a, e & 31); ey = wshfl(b, e & 31); ez = wshfl(c, e & 31);
+    }
+};
+
+// Jastrow change for electron e moving (o -> n), lane-parallel over partner
+// electrons (the lane's own two) and nuclei (lane I < NNUC); warp-reduced.
+template <int NE, int NUP, int NNUC, class T, bool GRAD>
+__device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, NE>& P, int lane, int e, T ox, T oy,
+                                            T oz, T nx, T ny, T nz, T (&go)[3], T (&gn)[3]) {
+    T du = 0;
+    T g[6] = {0, 0, 0, 0, 0, 0};
+    const bool e_up = e < NUP;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NE && j != e) {
+            const bool para = ((j < NUP) == e_up);
+            T ax = ox - P.x[r], ay = oy - P.y[r], az = oz - P.z[r];
+            T bx = nx - P.x[r], by = ny - P.y[r], bz = nz - P.z[r];
+            T da, ia, db, ib;
+            dist(ax * ax + ay * ay + az * az, da, ia);
+            dist(bx * bx + by * by + bz * bz, db, ib);
+            T ua, upa, lta, ub, upb, ltb;
+            const int c = para ? 1 : 0;
+            pade_ab(S.a_ee[c], S.b_ee[c], da, ia, ua, upa, lta);
+            pade_ab(S.a_ee[c], S.b_ee[c], db, ib, ub, upb, ltb);
+            du += ub - ua;
+            if (GRAD) {
+                g[0] += upa * ax; g[1] += upa * ay; g[2] += upa * az;
+                g[3] += upb * bx; g[4] += upb * by; g[5] += upb * bz;
+            }
+        }
+    }
+    if (lane < NNUC) {
+        const int I = lane;
+        T ax = ox - S.nuc[I][0], ay = oy - S.nuc[I][1], az = oz - S.nuc[I][2];
+        T bx = nx - S.nuc[I][0], by = ny - S.nuc[I][1], bz = nz - S.nuc[I][2];
+        T da, ia, db, ib;
+        dist(ax * ax + ay * ay + az * az, da, ia);
+        dist(bx * bx + by * by + bz * bz, db, ib);
+        T ua, upa, lta, ub, upb, ltb;
+        pade_ab(S.enA[I], S.enB[I], da, ia, ua, upa, lta);
+        pade_ab(S.enA[I], S.enB[I], db, ib, ub, upb, ltb);
+        du -= ub - ua;
+        if (GRAD) {
+            g[0] -= upa * ax; g[1] -= upa * ay; g[2] -= upa * az;
+            g[3] -= upb * bx; g[4] -= upb * by; g[5] -= upb * bz;
+        }
+    }
+    du = wsum(du);
+    if (GRAD) {
+        go[0] = wsum(g[0]) * S.qa; go[1] = wsum(g[1]) * S.qa; go[2] = wsum(g[2]) * S.qa;
+        gn[0] = wsum(g[3]) * S.qa; gn[1] = wsum(g[4]) * S.qa; gn[2] = wsum(g[5]) * S.qa;
+    }
+    return du;
+}
+
+// Single-electron sweeps, one warp per walker, WPB walkers per block.
+template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__ Sg, T* __restrict__ gpos,
+                                                     T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
+                                                     int n_sweeps, uint64_t step0, T step, T tau, T maxd,
+                                                     uint64_t seed, unsigned long long* acc_out, int* flags,
+                                                     int fixed_node) {
+    constexpr int NDN = NE - NUP;
+    constexpr int NM = NUP > NDN ? NUP : NDN;
+    __shared__ SysW<T> S;
+    load_sysw(&S, Sg);
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
+    if (w >= W) return;                        // whole warps only; no block barrier below
+    LanePos<T, NE> P;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        const bool ok = j < NE;
+        P.x[r] = ok ? gpos[(3 * j + 0) * (size_t)Wcap + w] : T(0);
+        P.y[r] = ok ? gpos[(3 * j + 1) * (size_t)Wcap + w] : T(0);
+        P.z[r] = ok ? gpos[(3 * j + 2) * (size_t)Wcap + w] : T(0);
+    }
+    T D0[NM], D1[NM];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        D0[k] = lane < NUP ? gdinv[((size_t)(0 * NM * NM + k * NM + lane)) * Wcap + w] : T(0);
+        D1[k] = lane < NDN ? gdinv[((size_t)(1 * NM * NM + k * NM + lane)) * Wcap + w] : T(0);
+    }
+    int sgn = gsign[w];
+    unsigned acc = 0;
+    int flg = 0;
+    for (int it = 0; it < n_sweeps; ++it) {
+        const uint64_t st = step0 + (uint64_t)it;
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            T (&D)[NM] = sig == 0 ? D0 : D1;
+            const int NS = sig == 0 ? NUP : NDN;
+            for (int q = 0; q < NS; ++q) {
+                const int e = sig * NUP + q;
+                T rx, ry, rz;
+                P.get(e, rx, ry, rz);
+                MoveDraw<T> md = move_draw<T>(seed, (uint32_t)w, st, (uint32_t)e);
+                T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
+                T gq[3];
+                if (MOVE == MOVE_ONE_DRIFT) {
+                    AOLane<T, 1> ao;
+                    ao_lane<T, 1>(S, rx, ry, rz, lane, ao);
+                    T v, gx, gy, gz, l;
+                    mo_lane<T, 1>(S, sig, lane, ao, v, gx, gy, gz, l);
+                    // lane j: sum_k grad phi_k Dinv[k][j]; lane q holds the drift term
+                    T ax = 0, ay = 0, az = 0;
+#pragma unroll
+                    for (int k = 0; k < NM; ++k) {
+                        ax += wshfl(gx, k) * D[k]; ay += wshfl(gy, k) * D[k]; az += wshfl(gz, k) * D[k];
+                    }
+                    ax = wshfl(ax, q); ay = wshfl(ay, q); az = wshfl(az, q);
+                    T g0[3], g1[3];
+                    wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
+                    dlx = tau * 2 * (ax + g0[0]); dly = tau * 2 * (ay + g0[1]); dlz = tau * 2 * (az + g0[2]);
+                    T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
+                    if (m > maxd) { T s = maxd / m; dlx *= s; dly *= s; dlz *= s; }
+                    T sd2 = fsqrt(2 * tau);
+                    nx = rx + dlx + sd2 * md.n0; ny = ry + dly + sd2 * md.n1; nz = rz + dlz + sd2 * md.n2;
+                } else {
+                    nx = rx + step * md.n0; ny = ry + step * md.n1; nz = rz + step * md.n2;
+                }
+                AOLane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0> ao;
+                ao_lane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0>(S, nx, ny, nz, lane, ao);
+                T phi, pgx, pgy, pgz, pl;
+                mo_lane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0>(S, sig, lane, ao, phi, pgx, pgy, pgz, pl);
+                // t_j = sum_k phi_k Dinv[k][j]; R = t_q
+                T tj = 0, bx = 0, by = 0, bz = 0;
+#pragma unroll
+                for (int k = 0; k < NM; ++k) {
+                    T d = D[k];
+                    tj += wshfl(phi, k) * d;
+                    if (MOVE == MOVE_ONE_DRIFT) { bx += wshfl(pgx, k) * d; by += wshfl(pgy, k) * d; bz += wshfl(pgz, k) * d; }
+                }
+                const T R = wshfl(tj, q);
+                T g0[3], gn[3];
+                T du = wjastrow_delta<NE, NUP, NNUC, T, MOVE == MOVE_ONE_DRIFT>(S, P, lane, e, rx, ry, rz, nx, ny, nz,
+                                                                               g0, gn);
+                if (MOVE == MOVE_ONE_DRIFT) {
+                    bx = wshfl(bx, q); by = wshfl(by, q); bz = wshfl(bz, q);
+                    T iR = R != T(0) ? T(1) / R : T(0);
+                    T cx = tau * 2 * (bx * iR + gn[0]), cy = tau * 2 * (by * iR + gn[1]), cz = tau * 2 * (bz * iR + gn[2]);
+                    T m = fsqrt(cx * cx + cy * cy + cz * cz);
+                    if (m > maxd) { T s = maxd / m; cx *= s; cy *= s; cz *= s; }
+                    T fx = nx - rx - dlx, fy = ny - ry - dly, fz = nz - rz - dlz;
+                    T qx = rx - nx - cx, qy = ry - ny - cy, qz = rz - nz - cz;
+                    logG = ((fx * fx + fy * fy + fz * fz) - (qx * qx + qy * qy + qz * qz)) / (4 * tau);
+                }
+                (void)gq;
+                T ratio = R * fexp(du);
+                T prob = ratio * ratio;
+                if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
+                if (prob != prob) flg |= FLAG_NONFINITE;
+                if (md.uacc < prob && R != T(0) && !(fixed_node && R < T(0))) {
+                    // positions: the owner lane of e stores the new coordinates
+                    if ((e & 31) == lane) {
+                        if (e < 32) { P.x[0] = nx; P.y[0] = ny; P.z[0] = nz; }
+                        else { P.x[1] = nx; P.y[1] = ny; P.z[1] = nz; }
+                    }
+                    const T iR = T(1) / R;
+                    const T f = tj * iR;
+#pragma unroll
+                    for (int k = 0; k < NM; ++k) {
+                        T dq = wshfl(D[k], q);
+                        D[k] = (lane == q) ? dq * iR : D[k] - dq * f;
+                    }
+                    if (R < 0) sgn = -sgn;
+                    ++acc;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NE) {
+            gpos[(3 * j + 0) * (size_t)Wcap + w] = P.x[r];
+            gpos[(3 * j + 1) * (size_t)Wcap + w] = P.y[r];
+            gpos[(3 * j + 2) * (size_t)Wcap + w] = P.z[r];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        if (lane < NUP) gdinv[((size_t)(0 * NM * NM + k * NM + lane)) * Wcap + w] = D0[k];
+        if (lane < NDN) gdinv[((size_t)(1 * NM * NM + k * NM + lane)) * Wcap + w] = D1[k];
+    }
+    if (lane == 0) {
+        gsign[w] = sgn;
+        if (acc) atomicAdd(acc_out, (unsigned long long)acc);
+        if (flg) atomicOr(flags, flg);
+    }
+}
+
+// Full evaluation from positions (refresh + E_L), one warp per walker.
+// Per-warp shared scratch holds the sector's D, grad D and lap D rows.
+template <int NE, int NUP, int NNUC, class TC, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restrict__ Sg, const TS* __restrict__ gpos,
+                                                       TS* __restrict__ gdinv, double* __restrict__ glog,
+                                                       int* __restrict__ gsign, double* __restrict__ gel, int W,
+                                                       int Wcap, int write_state, double* __restrict__ out_grad,
+                                                       double* __restrict__ out_lap, double* partial, int* flags) {
+    constexpr int NDN = NE - NUP;
+    constexpr int NM = NUP > NDN ? NUP : NDN;
+    __shared__ SysW<TC> S;
+    extern __shared__ __align__(16) unsigned char wsm[];
+    load_sysw(&S, Sg);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wib;
+    const bool act = w < W;
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;   // [5][NM rows][32 lanes]
+    double e_l = 0.0;
+    if (act) {
+        LanePos<TC, NE> P;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int j = lane + 32 * r;
+            const bool ok = j < NE;
+            P.x[r] = ok ? (TC)gpos[(3 * j + 0) * (size_t)Wcap + w] : TC(0);
+            P.y[r] = ok ? (TC)gpos[(3 * j + 1) * (size_t)Wcap + w] : TC(0);
+            P.z[r] = ok ? (TC)gpos[(3 * j + 2) * (size_t)Wcap + w] : TC(0);
+        }
+        double logdet = 0.0;
+        int sg = 1;
+        bool ok = true;
+        // per-lane electron results: lane owns electron (sig*NUP + lane) of each sector
+        TC gdx[2] = {0, 0}, gdy[2] = {0, 0}, gdz[2] = {0, 0}, ld[2] = {0, 0};
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            const int NS = sig == 0 ? NUP : NDN;
+            for (int q = 0; q < NS; ++q) {
+                const int e = sig * NUP + q;
+                TC rx, ry, rz;
+                P.get(e, rx, ry, rz);
+                AOLane<TC, 2> ao;
+                ao_lane<TC, 2>(S, rx, ry, rz, lane, ao);
+                TC v, gx, gy, gz, l;
+                mo_lane<TC, 2>(S, sig, lane, ao, v, gx, gy, gz, l);
+                Mrow[(0 * NM + q) * 32 + lane] = v;
+                Mrow[(1 * NM + q) * 32 + lane] = gx;
+                Mrow[(2 * NM + q) * 32 + lane] = gy;
+                Mrow[(3 * NM + q) * 32 + lane] = gz;
+                Mrow[(4 * NM + q) * 32 + lane] = l;
+            }
+            __syncwarp();
+            // Gauss-Jordan with partial pivoting: lane j carries column j of [D | I]
+            TC Dc[NM], Ic[NM];
+#pragma unroll
+            for (int i = 0; i < NM; ++i) {
+                Dc[i] = (i < NS && lane < NS) ? Mrow[(0 * NM + i) * 32 + lane] : TC(i == lane ? 1 : 0);
+                Ic[i] = (i == lane) ? TC(1) : TC(0);
+            }
+#pragma unroll
+            for (int k = 0; k < NM; ++k) {
+                if (k >= NS) break;
+                // pivot search in column k (lane k)
+                int p = k;
+                TC best = fabs(Dc[k]);
+#pragma unroll
+                for (int i = k + 1; i < NM; ++i) {
+                    TC a = fabs(Dc[i]);
+                    if (i < NS && a > best) { best = a; p = i; }
+                }
+                p = wshfl(p, k);
+#pragma unroll
+                for (int i = k + 1; i < NM; ++i) {
+                    bool sw = (i == p);
+                    TC a = Dc[k], b = Dc[i];
+                    Dc[k] = sw ? b : a; Dc[i] = sw ? a : b;
+                    TC c = Ic[k], d = Ic[i];
+                    Ic[k] = sw ? d : c; Ic[i] = sw ? c : d;
+                }
+                if (p != k) sg = -sg;
+                TC piv = wshfl(Dc[k], k);
+                if (!(piv != TC(0))) { ok = false; piv = TC(1); }
+                if (piv < 0) sg = -sg;
+                logdet += log(fabs((double)piv));
+                TC ip = TC(1) / piv;
+                Dc[k] *= ip;
+                Ic[k] *= ip;
+#pragma unroll
+                for (int i = 0; i < NM; ++i) {
+                    if (i == k || i >= NS) continue;
+                    TC f = wshfl(Dc[i], k);
+                    Dc[i] -= f * Dc[k];
+                    Ic[i] -= f * Ic[k];
+                }
+            }
+            // lane j now holds column j of D^-1
+            if (write_state && lane < NS) {
+#pragma unroll
+                for (int k = 0; k < NM; ++k)
+                    if (k < NS) gdinv[((size_t)(sig * NM * NM + k * NM + lane)) * Wcap + w] = (TS)Ic[k];
+            }
+            // row-wise products for this lane's electron q = lane
+            if (lane < NS) {
+                TC ax = 0, ay = 0, az = 0, al = 0;
+#pragma unroll
+                for (int k = 0; k < NM; ++k) {
+                    if (k >= NS) break;
+                    TC dk = Ic[k];
+                    ax += Mrow[(1 * NM + lane) * 32 + k] * dk;
+                    ay += Mrow[(2 * NM + lane) * 32 + k] * dk;
+                    az += Mrow[(3 * NM + lane) * 32 + k] * dk;
+                    al += Mrow[(4 * NM + lane) * 32 + k] * dk;
+                }
+                gdx[sig] = ax; gdy[sig] = ay; gdz[sig] = az; ld[sig] = al;
+            }
+            __syncwarp();
+        }
+        // Jastrow + Coulomb for this lane's electrons (pairs counted from both ends)
+        TC u = 0, V = 0, kin = 0;
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            const int NS = sig == 0 ? NUP : NDN;
+            const int i = sig * NUP + lane;
+            const bool own = lane < NS;
+            TC xi, yi, zi;
+            P.get(min(i, NE - 1), xi, yi, zi);
+            TC gx = 0, gy = 0, gz = 0, lu = 0, gsq = 0;
+            for (int j = 0; j < NE; ++j) {
+                TC xj, yj, zj;
+                P.get(j, xj, yj, zj);
+                if (!own || j == i) continue;
+                const bool para = ((j < NUP) == (i < NUP));
+                TC dx = xi - xj, dy = yi - yj, dz = zi - zj;
+                TC d, ri;
+                dist(dx * dx + dy * dy + dz * dz, d, ri);
+                V += TC(0.5) * ri;
+                TC uu, upr, lt;
+                const int c = para ? 1 : 0;
+                pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+                u += TC(0.5) * uu;
+                if (!(d < TC(1e-10))) {
+                    gx += upr * dx; gy += upr * dy; gz += upr * dz;
+                    lu += lt;
+                    TC up = upr * d;
+                    gsq += up * up;
+                }
+            }
+            if (own) {
+                for (int I = 0; I < NNUC; ++I) {
+                    TC dx = xi - S.nuc[I][0], dy = yi - S.nuc[I][1], dz = zi - S.nuc[I][2];
+                    TC d, ri;
+                    dist(dx * dx + dy * dy + dz * dz, d, ri);
+                    V -= S.Z[I] * ri;
+                    TC uu, upr, lt;
+                    pade_ab(S.enA[I], S.enB[I], d, ri, uu, upr, lt);
+                    u -= uu;
+                    if (!(d < TC(1e-10))) {
+                        gx -= upr * dx; gy -= upr * dy; gz -= upr * dz;
+                        lu -= lt;
+                    }
+                }
+                TC ax = S.qa * gx, ay = S.qa * gy, az = S.qa * gz;
+                TC lj = S.quirk_lap ? (lu + gsq) : (lu + gx * gx + gy * gy + gz * gz);
+                TC lp = ld[sig] + 2 * (gdx[sig] * ax + gdy[sig] * ay + gdz[sig] * az) + lj;
+                kin += lp;
+                const int ecall = i;   // internal index; host permutes to caller order
+                if (out_grad) {
+                    out_grad[((size_t)w * NE + ecall) * 3 + 0] = gdx[sig] + ax;
+                    out_grad[((size_t)w * NE + ecall) * 3 + 1] = gdy[sig] + ay;
+                    out_grad[((size_t)w * NE + ecall) * 3 + 2] = gdz[sig] + az;
+                }
+                if (out_lap) out_lap[(size_t)w * NE + ecall] = lp;
+            }
+        }
+        u = wsum(u);
+        V = wsum(V);
+        kin = wsum(kin);
+        e_l = (double)(TC(-0.5) * kin + V + S.v_nn);
+        if (lane == 0) {
+            int fl = 0;
+            if (!ok) fl |= FLAG_SINGULAR;
+            if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
+            if (fl) atomicOr(flags, fl);
+            if (write_state) { glog[w] = logdet + (double)u; gsign[w] = sg; gel[w] = e_l; }
+        }
+    }
+    if (partial) {
+        // block partial of E_L over the block's walkers (lane 0 of each warp)
+        __shared__ double ps[WPB];
+        if (lane == 0) ps[wib] = act ? e_l : 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Comp c{0.0, 0.0};
+            for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
+            partial[2 * blockIdx.x] = c.s;
+            partial[2 * blockIdx.x + 1] = c.c;
+        }
+    }
+}
+
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+
+// Per-shape launchers for the warp kernels.
+template <int NE, int NUP, int NNUC>
+struct WarpShapeOps {
+    static constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    static constexpr int WPB = 4;
+
+    template <class T>
+    static int table(const HostSys& hs, const SysW<T>** out) {
+        // device copies of the table, cached per system and rebuilt when the
+        // parameters or nuclei change (HostSys::version)
+        int slot = sizeof(T) == 8 ? 0 : 1;
+        if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
+            SysW<T>* h = new SysW<T>;
+            if (!fill_sysw<T>(hs, NE, NUP, NNUC, *h)) { delete h; return 7; }
+            if (!hs.dev_table[slot]) {
+                if (cudaMalloc(&hs.dev_table[slot], sizeof(SysW<T>)) != cudaSuccess) { delete h; return 8; }
+            }
+            cudaError_t e = cudaMemcpy(hs.dev_table[slot], h, sizeof(SysW<T>), cudaMemcpyHostToDevice);
+            delete h;
+            if (e != cudaSuccess) return 2;
+            hs.dev_table_version[slot] = hs.version;
+        }
+        *out = static_cast<const SysW<T>*>(hs.dev_table[slot]);
+        return 0;
+    }
+
+    static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
+        const SysW<double>* S;
+        int rc = table<double>(hs, &S);
+        if (rc) return rc;
+        int n = NE * dw.W, tpb = 256;
+        if (dw.prec == 0) kw_init<double><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(S, (double*)dw.pos, NE, dw.W, dw.Wcap, seed);
+        else kw_init<float><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(S, (float*)dw.pos, NE, dw.W, dw.Wcap, seed);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    template <class TC, class TS>
+    static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
+        const SysW<TC>* S;
+        int rc = table<TC>(hs, &S);
+        if (rc) return rc;
+        int nb = (dw.W + WPB - 1) / WPB;
+        size_t smem = sizeof(TC) * WPB * 5 * NM * 32;
+        auto kern = kw_measure<NE, NUP, NNUC, TC, TS, WPB>;
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        double* partial = (ws && dw.partial && dw.partial_cap >= 2 * nb + 1) ? dw.partial : nullptr;
+        kern<<<nb, 32 * WPB, smem, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W, dw.Wcap,
+                                         ws ? 1 : 0, out.grad, out.lap, partial, dw.flags);
+        ++g_launch_count;
+        if (cudaGetLastError() != cudaSuccess) return 2;
+        if (!partial) return 0;
+        return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
+    }
+
+    static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
+        if (out.O || out.fhf || out.omega) return 7;
+        if (cp == 0) return dw.prec == 0 ? measure2<double, double>(hs, dw, ws, out, st)
+                                         : measure2<double, float>(hs, dw, ws, out, st);
+        if (dw.prec == 1) return measure2<float, float>(hs, dw, ws, out, st);
+        return 7;
+    }
+
+    template <class T, int MOVE>
+    static int sweep_t(const HostSys& hs, DevWalkers& dw, int n, uint64_t s0, double step, double tau, double maxd,
+                       uint64_t seed, cudaStream_t st) {
+        const SysW<T>* S;
+        int rc = table<T>(hs, &S);
+        if (rc) return rc;
+        int nb = (dw.W + WPB - 1) / WPB;
+        kw_sweep<NE, NUP, NNUC, T, MOVE, WPB><<<nb, 32 * WPB, 0, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W,
+                                                                     dw.Wcap, n, s0, (T)step, (T)tau, (T)maxd, seed,
+                                                                     dw.acc, dw.flags, dw.fixed_node);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    static int sweep(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,
+                     double maxd, uint64_t seed, cudaStream_t st) {
+        if (mk == MOVE_ONE_GAUSS)
+            return dw.prec == 0 ? sweep_t<double, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                : sweep_t<float, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st);
+        if (mk == MOVE_ONE_DRIFT)
+            return dw.prec == 0 ? sweep_t<double, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                : sweep_t<float, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st);
+        return 7;   // all-electron moves are not compiled for this shape
+    }
+};
+
+}  // namespace qmc

@@ -10,6 +10,8 @@ Builders:
   * ``methane_gto``      CH4 6-31G x Jastrow3, src/systems/methane.rs:600-776
   * ``methane_minimal``  the 9-function CH4 with seeded QR-orthonormal MOs
                          (65 536-walker single-electron workload)
+  * ``benzene_minimal``  planar C6H6, 42 electrons, 36 contracted Gaussians,
+                         seeded QR-orthonormal MOs (16 384-walker VMC/DMC workload)
 """
 import ctypes as C
 import math
@@ -328,3 +330,39 @@ def methane_minimal(seed=SEED_BASE + 2, b_ee=1.5, b_en=2.0, n_rot=4, bond=CH_BON
         ao_prims=prims, mo_coef=mo, occ=[0, 1, 2, 3, 4] * 2, jastrow_kind=L.QMC_JAS_PADE_EEN,
         jas=jastrow3_params(b_ee, b_en), rot_occ=rot_occ, rot_virt=rot_virt, rot_angle=[0.0] * n_rot,
         init_nuc=[0] * 6 + [1, 2, 3, 4], init_sigma=0.5)
+
+
+def hexagonal_c6h6(cc=2.64, ch=2.05):
+    """D6h benzene in the z = 0 plane (src/systems/benzene.rs:119-140):
+    carbons on a hexagon of radius C-C, hydrogens radially outward at C-C + C-H."""
+    C, H = [], []
+    for i in range(6):
+        a = math.pi / 3.0 * i
+        C.append([cc * math.cos(a), cc * math.sin(a), 0.0])
+        H.append([(cc + ch) * math.cos(a), (cc + ch) * math.sin(a), 0.0])
+    return np.array(C + H, dtype=np.float64)
+
+
+def benzene_minimal(seed=SEED_BASE + 4, b_ee=1.5, b_en=2.0, cc=2.64, ch=2.05):
+    """Benzene with a 36-function minimal basis: per carbon C 1s (three most
+    diffuse 6-31G C 1s primitives), C 2s and 2p (6-31G SP inner shell); per
+    hydrogen 1s (6-31G H inner shell).  MOs: QR of a seeded 36x36 normal
+    matrix, MOs 0-20 occupied in both sectors.  Electrons 0-20 spin up, 21-41
+    spin down; initial centres as src/systems/benzene.rs:642-655 (six per
+    carbon, one per hydrogen), width 0.5 bohr."""
+    R = hexagonal_c6h6(cc, ch)
+    ao_nuc, ao_l, ao_m, prims = [], [], [], []
+    for c in range(6):
+        ao_nuc.append(c); ao_l.append(0); ao_m.append(0); prims.append(C_1S[3:])
+        ao_nuc.append(c); ao_l.append(0); ao_m.append(0); prims.append(list(zip(C_SP_INNER_EXP, C_SP_INNER_S)))
+        for m in range(3):
+            ao_nuc.append(c); ao_l.append(1); ao_m.append(m); prims.append(list(zip(C_SP_INNER_EXP, C_SP_INNER_P)))
+    for h in range(6):
+        ao_nuc.append(6 + h); ao_l.append(0); ao_m.append(0); prims.append(H_INNER)
+    Q = seeded_orthonormal(seed, 36)
+    init = [i // 6 for i in range(36)] + [6 + h for h in range(6)]
+    return SystemSpec(
+        name="C6H6-min", spins=[1] * 21 + [-1] * 21, nuc_pos=R, nuc_charge=[6.0] * 6 + [1.0] * 6,
+        nuc_species=[0] * 6 + [1] * 6, basis_kind=L.QMC_BASIS_GTO, ao_nuc=ao_nuc, ao_l=ao_l, ao_m=ao_m,
+        ao_prims=prims, mo_coef=Q.T.copy(), occ=list(range(21)) * 2, jastrow_kind=L.QMC_JAS_PADE_EEN,
+        jas=jastrow3_params(b_ee, b_en), init_nuc=init, init_sigma=0.5)

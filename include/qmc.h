@@ -137,7 +137,9 @@ typedef struct {
     int refresh_every;           /* FP64 inverse recompute + E_L measurement period (sweeps) */
     double e_ref_damping;        /* DMC kappa */
     int fixed_node;              /* DMC: refuse sign-changing proposals (the reference accepts them) */
-    int reserved[5];
+    int reference_diffusion;     /* DMC: move with variance 2 tau as the reference does (is_dmc.rs:218-225);
+                                    0 = Hartree-unit diffusion (variance tau, drift tau grad ln psi) */
+    int reserved[4];
 } qmc_run_params;
 
 typedef struct {
@@ -233,15 +235,18 @@ int qmc_walkers_create_dmc(qmc_sys_t sys, int W, int capacity, int precision, qm
 /* Current population size. */
 int qmc_walkers_count(qmc_walkers_t wk, int* W);
 /* One IS-DMC step (src/sampling/is_dmc.rs:208-302): one drift-diffusion sweep
- * per walker (fixed-node rejection when fixed_node), E_L after the sweep (in
+ * per walker made with the reference-convention move at tau_move (variance
+ * 2 tau_move, drift 2 tau_move grad ln psi; tau_move = tau / 2 is the
+ * Hartree-unit projector, tau_move = tau the reference's), fixed-node
+ * rejection when fixed_node, E_L after the sweep (in
  * the walkers' precision, FP64 when fp64_measure), copies
  * m = min(floor(exp(tau (e_ref - (E_L + E_old)/2)) + xi), 3) with an FP64
  * log-weight and a tag-4 Philox xi per (walker slot, step), and an
  * order-stable on-device compaction.  *n_new receives the new population
  * (0 = collapse), *e_mean its mean E_L.  QMC_ERR_POPULATION if the new
  * population exceeds the capacity (the population is then left unchanged). */
-int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double max_drift, int fixed_node, double e_ref,
-                         uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean);
+int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double max_drift, int fixed_node,
+                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean);
 
 /* ---- drivers --------------------------------------------------------------- */
 /* VMC run: MCMCSimulation::run (src/sampling/vmc.rs:69-92) for all-electron

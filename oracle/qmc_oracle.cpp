@@ -836,7 +836,9 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
 }
 
 // Importance-sampled DMC (src/sampling/is_dmc.rs:208-302, 385-502) with the
-// shared Philox layout: per step one drift-diffusion sweep per walker
+// shared Philox layout: per step one drift-diffusion sweep per walker made
+// with the reference's move at tau_move (variance 2 tau_move; tau_move = tau is
+// the reference, tau / 2 the Hartree-unit projector)
 // (walker id = its slot in the current population, step index = DMC step),
 // E_L after the sweep, copies m = min(floor(exp(tau (E_ref - (E_L + E_old)/2)) + xi), 3)
 // with xi from tag-4 draws, populations rebuilt in slot order, and
@@ -844,7 +846,8 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
 // collapses or exceeds `cap`.  Returns the number of steps done; pos_out
 // receives the final population, pops/energies the per-step values.
 int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps, uint64_t step0, double tau,
-            double max_drift, int fixed_node, double kappa, int target, uint64_t seed, int cap, double* pos_out,
+            double tau_move, double max_drift, int fixed_node, double kappa, int target, uint64_t seed, int cap,
+            double* pos_out,
             int* W_out, int* pops, double* energies, double* e_ref_io, int threads) {
     Sys s = make_sys(d);
     int N = s.N;
@@ -864,7 +867,8 @@ int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps,
         int W = (int)R.size();
         std::vector<double> Eold = E;
         parallel_for(W, threads, [&](int w) {
-            sweep_walker(s, order, R[w], lpv[w], sgv[w], (uint32_t)w, st, 3, 0.0, tau, max_drift, seed, fixed_node);
+            sweep_walker(s, order, R[w], lpv[w], sgv[w], (uint32_t)w, st, 3, 0.0, tau_move, max_drift, seed,
+                         fixed_node);
             Eval e = evaluate_full(s, R[w]);
             E[w] = e.el; lpv[w] = e.logabs; sgv[w] = e.sign;
         });

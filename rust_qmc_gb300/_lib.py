@@ -44,7 +44,7 @@ class RunParams(C.Structure):
         ("n_walkers", C.c_int), ("n_steps", C.c_int), ("n_burnin", C.c_int), ("move_kind", C.c_int),
         ("step", C.c_double), ("tau", C.c_double), ("max_drift", C.c_double),
         ("precision", C.c_int), ("refresh_every", C.c_int), ("e_ref_damping", C.c_double),
-        ("fixed_node", C.c_int), ("reserved", C.c_int * 5),
+        ("fixed_node", C.c_int), ("reference_diffusion", C.c_int), ("reserved", C.c_int * 4),
     ]
 
 
@@ -96,7 +96,8 @@ PROTOTYPES = {
     "qmc_dmc_run": [_vp, C.POINTER(RunParams), _u64, C.POINTER(RunResult), _dp],
     "qmc_walkers_create_dmc": [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)],
     "qmc_walkers_count": [_vp, _ip],
-    "qmc_walkers_dmc_step": [_vp, C.c_double, C.c_double, C.c_int, C.c_double, _u64, _u64, C.c_int, _ip, _dp],
+    "qmc_walkers_dmc_step": [_vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _u64, _u64, C.c_int, _ip,
+                             _dp],
     "qmc_ctx_event_record": [_vp, C.c_int],
     "qmc_ctx_event_elapsed": [_vp, C.c_int, C.c_int, C.POINTER(C.c_float)],
     "qmc_ctx_synchronize": [_vp],

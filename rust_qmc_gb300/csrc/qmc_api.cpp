@@ -372,15 +372,15 @@ double dmc_block_error(const std::vector<double>& x) {
 // One IS-DMC step on a resident population: save E_L, one drift-diffusion
 // sweep, E_L in the walkers' precision (FP64 when fp64_measure), branching
 // and compaction into the alternate buffer, swap.
-int dmc_step(qmc_walkers_s* wk, double tau, double max_drift, int fixed_node, double e_ref, uint64_t seed,
-             uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+int dmc_step(qmc_walkers_s* wk, double tau, double tau_move, double max_drift, int fixed_node, double e_ref,
+             uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
     CK(ensure_dmc(wk));
     const HostSys& hs = wk->sys->hs;
     cudaStream_t st = wk->sys->ctx->stream;
     DevWalkers& dw = wk->dw;
     CU(cudaMemcpyAsync(wk->br.el_old, dw.el, 8 * (size_t)dw.W, cudaMemcpyDeviceToDevice, st));
     dw.fixed_node = fixed_node;
-    int rc = launch_sweep(hs, dw, QMC_MOVE_ONE_DRIFT, 1, step, 0.0, tau, max_drift, seed, st);
+    int rc = launch_sweep(hs, dw, QMC_MOVE_ONE_DRIFT, 1, step, 0.0, tau_move, max_drift, seed, st);
     dw.fixed_node = 0;
     CK(rc);
     MeasureOut none;
@@ -674,11 +674,12 @@ int qmc_walkers_count(qmc_walkers_t wk, int* W) {
     return QMC_OK;
 }
 
-int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double max_drift, int fixed_node, double e_ref,
-                         uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
-    if (!wk || !n_new || !e_mean || !(tau > 0) || !(max_drift > 0) || wk->dw.W <= 0) return QMC_ERR_ARG;
+int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double max_drift, int fixed_node,
+                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+    if (!wk || !n_new || !e_mean || !(tau > 0) || !(tau_move > 0) || !(max_drift > 0) || wk->dw.W <= 0)
+        return QMC_ERR_ARG;
     cudaSetDevice(wk->sys->ctx->device);
-    return dmc_step(wk, tau, max_drift, fixed_node, e_ref, seed, step, fp64_measure, n_new, e_mean);
+    return dmc_step(wk, tau, tau_move, max_drift, fixed_node, e_ref, seed, step, fp64_measure, n_new, e_mean);
 }
 
 int qmc_walkers_destroy(qmc_walkers_t wk) {
@@ -887,7 +888,13 @@ int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
         int Wcur = wk->dw.W, n_new = 0;
         double em = 0.0;
         int fp64 = ((t + 1) % every) == 0;
-        CK(dmc_step(wk, p->tau, p->max_drift, p->fixed_node, e_ref, seed, (uint64_t)t, fp64, &n_new, &em));
+        // The reference diffuses with variance 2 tau and drift 2 tau grad ln psi
+        // (is_dmc.rs:218-225) but branches with tau; the Hartree-unit
+        // projector needs variance tau and drift tau grad ln psi, i.e. the
+        // reference-convention move at tau / 2.
+        const double tau_move = p->reference_diffusion ? p->tau : 0.5 * p->tau;
+        CK(dmc_step(wk, p->tau, tau_move, p->max_drift, p->fixed_node, e_ref, seed, (uint64_t)t, fp64, &n_new,
+                    &em));
         if (t >= p->n_burnin) moves += (long long)Wcur * hs.N;
         if (n_new == 0) {                                // collapse: re-initialise, is_dmc.rs:428-437
             ++collapses;

@@ -236,8 +236,9 @@ def test_vmc_run_precisions_agree_ch4(ctx):
     assert abs(a["energy"] - b["energy"]) < 4 * sig + 1e-3 * abs(a["energy"]), (a, b)
 
 
-@pytest.mark.parametrize("name,fixed_node", [("h2", True), ("ch4_min", True), ("li_ref", False)])
-def test_fp64_dmc_population_matches_oracle(ctx, oracle, name, fixed_node):
+@pytest.mark.parametrize("name,fixed_node,refdiff", [("h2", True, False), ("ch4_min", True, False),
+                                                     ("li_ref", False, True)])
+def test_fp64_dmc_population_matches_oracle(ctx, oracle, name, fixed_node, refdiff):
     """IS-DMC branching + compaction: the FP64 device population follows the
     oracle's reference-algorithm DMC step for step (same Philox stream,
     order-stable copies), so populations and mean energies agree."""
@@ -252,27 +253,32 @@ def test_fp64_dmc_population_matches_oracle(ctx, oracle, name, fixed_node):
     pops, ens = [], []
     er = e_ref
     for t in range(n_steps):
-        n, em = wk.dmc_step(tau, er, seed=77, step=t, fixed_node=fixed_node)
+        n, em = wk.dmc_step(tau, er, seed=77, step=t, fixed_node=fixed_node, reference_diffusion=refdiff)
         assert n > 0
         pops.append(n)
         ens.append(em)
         er = em - 0.5 * np.log(n / target) / tau
-    _, pops_o, ens_o, er_o = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node)
+    _, pops_o, ens_o, er_o = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node,
+                                        reference_diffusion=refdiff)
     assert list(pops) == list(pops_o)
     np.testing.assert_allclose(ens, ens_o, rtol=1e-9, atol=1e-9)
     got = wk.get_positions()
-    want, _, _, _ = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node)
+    want, _, _, _ = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=fixed_node,
+                               reference_diffusion=refdiff)
     np.testing.assert_allclose(got, want, atol=1e-8)
 
 
 def test_dmc_run_h2_energy(ctx):
-    """Fixed-node DMC of H2 (nodeless ground state): the energy lies below the
-    VMC energy of the same trial function and near the exact -1.1745 Ha
-    (time-step and population bias allowed)."""
+    """DMC of H2 (nodeless ground state) with Hartree-unit diffusion reaches
+    the exact -1.1745 Ha within statistical, time-step and population bias;
+    the reference's diffusion (variance 2 tau with branching at tau) settles
+    markedly higher, which is why it is behind a flag."""
     sysh = Q.System(ctx, Q.h2_mo())
-    d = Q.dmc_run(sysh, n_walkers=2048, n_steps=600, n_burnin=800, tau=0.01, seed=3)
+    d = Q.dmc_run(sysh, n_walkers=4096, n_steps=800, n_burnin=800, tau=0.005, seed=3)
+    r = Q.dmc_run(sysh, n_walkers=4096, n_steps=800, n_burnin=800, tau=0.005, seed=3, reference_diffusion=True)
     v = Q.vmc_run(sysh, n_walkers=2048, n_steps=400, n_burnin=100, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0, seed=4)
-    assert -1.19 < d["energy"] < -1.163, d
+    assert abs(d["energy"] - (-1.1745)) < 0.004 + 4 * d["error"], d
+    assert r["energy"] > d["energy"] + 0.005, (r, d)
     assert d["energy"] < v["energy"] + 3 * (d["error"] + v["error"])
     assert 1500 < d["avg_population"] < 2700
     assert 0.9 < d["acceptance_rate"] <= 1.0

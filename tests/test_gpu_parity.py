@@ -280,7 +280,7 @@ def test_dmc_run_h2_energy(ctx):
     assert abs(d["energy"] - (-1.1745)) < 0.004 + 4 * d["error"], d
     assert r["energy"] > d["energy"] + 0.005, (r, d)
     assert d["energy"] < v["energy"] + 3 * (d["error"] + v["error"])
-    assert 1500 < d["avg_population"] < 2700
+    assert 3000 < d["avg_population"] < 5500
     assert 0.9 < d["acceptance_rate"] <= 1.0
 
 

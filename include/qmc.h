@@ -58,8 +58,8 @@ enum {
 
 /* ---- enumerations -------------------------------------------------------- */
 enum { QMC_FP64 = 0, QMC_FP32_REFINE = 1 };          /* walker working precision */
-enum { QMC_BASIS_GTO = 0, QMC_BASIS_STO = 1 };       /* contracted Gaussians / Slater-type */
-enum { QMC_JAS_NONE = 0, QMC_JAS_PADE_F = 1, QMC_JAS_PADE_EEN = 2 };
+enum { QMC_BASIS_GTO = 0, QMC_BASIS_STO = 1, QMC_BASIS_PW = 2 };   /* contracted Gaussians / Slater-type / plane waves */
+enum { QMC_JAS_NONE = 0, QMC_JAS_PADE_F = 1, QMC_JAS_PADE_EEN = 2, QMC_JAS_HEG = 3 };
 enum {
     QMC_MOVE_ALL_GAUSS = 0,   /* all-electron Gaussian, src/sampling/vmc.rs:95-119 */
     QMC_MOVE_ALL_BOX = 1,     /* all-electron uniform box of side `step` */
@@ -68,7 +68,10 @@ enum {
 };
 enum {
     QMC_QUIRK_J2_GRAD = 1,    /* Jastrow2 gradient prefactor F/(2(1+r/F)^2 r), src/correlation/jastrow.rs:102 */
-    QMC_QUIRK_J2_LAP = 2      /* Jastrow2 per-pair Laplacian without cross terms, :110-125 */
+    QMC_QUIRK_J2_LAP = 2,     /* Jastrow2 per-pair Laplacian without cross terms, :110-125 */
+    QMC_QUIRK_HEG_EWALD = 4,  /* electron gas: the reference's Ewald (alpha = 5/L, |n_i| <= 7, minimum
+                                 image, Madelung -0.448 N / r_s), src/systems/heg.rs:526-581 */
+    QMC_QUIRK_HEG_CROSS = 8   /* electron gas: cross term without the orbital factor, heg.rs:711-720 */
 };
 
 /* ---- system description (MultiWfn + EnergyCalculator data) ------------- */
@@ -86,6 +89,13 @@ enum {
  *   s = spin class of the pair, sp = nuc_species[I];
  * the reference Jastrow3 is b_anti=b_para=b_ee, A=1, B_0=B_1=b_en.
  * QMC_JAS_PADE_F is u = sum_{i<j} -F/(2(1+r/F)) (Jastrow1 / Jastrow2).
+ * Periodic electron gas (src/systems/heg.rs): basis_kind QMC_BASIS_PW, box_L
+ * the cubic box side, n_nuc = 0, mo_coef the plane-wave vectors [n_mo][3]
+ * (orbital k = e^{i k.r}), jastrow_kind QMC_JAS_HEG with jas_F = F,
+ * jas[0] = form (0 Pade, 1 RPA, 2 Yukawa), jas[2]/jas[3] = antiparallel /
+ * parallel amplitudes, jas[4] = Ewald alpha * L, jas[5] = reciprocal cutoff
+ * |n| (one-component-plasma Ewald unless QMC_QUIRK_HEG_EWALD).  Walkers start
+ * uniformly in the box; accepted moves are wrapped into it.
  * Optimisable parameters (OptimizableWfn) are jas[0..7] then rot_angle[0..n_rot-1]:
  * angle q mixes MO rot_occ[q] with MO rot_virt[q]:
  *   phi_occ <- cos(t) phi_occ + sin(t) phi_virt.
@@ -119,7 +129,7 @@ typedef struct {
     int quirks;
     const int* init_nuc;         /* [n_elec] initial centre per electron, -1 = origin; NULL = all origin */
     double init_sigma;           /* width of the initial Gaussian (MultiWfn::initialize) */
-    double box_L;                /* must be 0: open boundary conditions */
+    double box_L;                /* 0: open boundaries; > 0: periodic cubic box (plane-wave systems) */
     int reserved[4];
 } qmc_system_desc;
 

@@ -36,6 +36,8 @@ def lib():
                               C.c_double,
                               C.c_int, C.c_uint64, C.c_int, _dp, _ip, _ip, _dp, _dp, C.c_int]
         l.orc_dmc.restype = C.c_int
+        l.orc_heg_ewald.argtypes = [vp, _dp, C.c_double, C.c_int]
+        l.orc_heg_ewald.restype = C.c_double
         _lib = l
     return _lib
 
@@ -155,3 +157,9 @@ def dmc(spec, pos, n_steps, tau, e_ref, target, seed, step0=0, max_drift=1.0, fi
                          kappa, target,
                          seed, cap, _d(out), C.byref(Wout), _i(pops), _d(en), C.byref(er), threads or threads_default())
     return out[:Wout.value], pops[:done], en[:done], er.value
+
+
+def heg_ewald(spec, r, alphaL=0.0, kmax=0):
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    d = spec.desc()
+    return lib().orc_heg_ewald(C.byref(d), _d(r), alphaL, kmax)

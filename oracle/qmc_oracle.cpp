@@ -32,6 +32,7 @@
 #include <vector>
 #include <thread>
 #include <algorithm>
+#include <complex>
 
 extern "C" {
 
@@ -155,6 +156,11 @@ struct Sys {
     double init_sigma = 0.5;
     // sector bookkeeping: electrons of each spin in ascending reference order
     std::vector<int> sec[2];    // sec[0] = spin +1, sec[1] = spin -1
+    // periodic electron gas (basis kind 2): plane waves e^{i k.r}
+    bool pw = false;
+    double L = 0.0, rs = 0.0, alphaL = 5.0;
+    int kmax = 8, form = 1;
+    std::vector<V3> kvec;       // [n_mo] orbital wave vectors
 
     void apply_rotations() {
         C = C0;
@@ -178,6 +184,26 @@ Sys make_sys(const orc_system_desc* d) {
         s.species.push_back(d->nuc_species ? d->nuc_species[I] : 0);
     }
     s.basis = d->basis_kind;
+    if (s.basis == 2) {
+        // periodic electron gas: mo_coef holds the wave vectors [n_mo][3]
+        s.pw = true;
+        s.L = d->box_L;
+        s.n_mo = d->n_mo;
+        for (int k = 0; k < s.n_mo; ++k) s.kvec.push_back({d->mo_coef[3 * k], d->mo_coef[3 * k + 1], d->mo_coef[3 * k + 2]});
+        s.occ.assign(d->occ, d->occ + s.N);
+        s.jk = d->jastrow_kind;
+        s.F = d->jas_F;
+        for (int i = 0; i < 8; ++i) s.jas[i] = d->jas[i];
+        s.form = (int)d->jas[0];
+        s.alphaL = d->jas[4] > 0 ? d->jas[4] : 5.0;
+        s.kmax = d->jas[5] > 0 ? (int)d->jas[5] : 8;
+        s.quirks = d->quirks;
+        s.rs = s.L / std::cbrt(4.0 * M_PI * s.N / 3.0);
+        s.init_sigma = d->init_sigma;
+        s.init_nuc.assign(s.N, -1);
+        for (int e = 0; e < s.N; ++e) s.sec[s.spins[e] > 0 ? 0 : 1].push_back(e);
+        return s;
+    }
     s.n_ao = d->n_ao;
     for (int a = 0; a < s.n_ao; ++a)
         s.ao.push_back({d->ao_nuc[a], d->ao_l[a], d->ao_m[a], d->ao_prim_off[a], d->ao_prim_off[a + 1]});
@@ -452,8 +478,226 @@ double potential(const Sys& s, const std::vector<V3>& r) {
     return v;
 }
 
+
+// ---------------------------------------------------------------------------
+// Homogeneous electron gas (src/systems/heg.rs): complex plane-wave spin
+// determinants, spin-dependent Jastrow with a minimum-image cutoff at L/2,
+// Ewald Coulomb energy.  Quirk bits: 4 = the reference's Ewald (alpha = 5/L,
+// |n_i| <= 7 cube, minimum image only, Madelung -0.448 N / r_s, heg.rs:526-581);
+// 8 = the reference's cross term without the orbital factor (heg.rs:711-720).
+// Without them: the one-component-plasma Ewald sum with its self and
+// background terms, and the exact cross term.
+// ---------------------------------------------------------------------------
+typedef std::complex<double> cplx;
+
+V3 min_image(const Sys& s, V3 v) {
+    return {v.x - s.L * std::round(v.x / s.L), v.y - s.L * std::round(v.y / s.L), v.z - s.L * std::round(v.z / s.L)};
+}
+
+// u, du/dr, lap u of the three forms (heg.rs:352-444); a = cusp amplitude
+void heg_pair(const Sys& s, double r, double a, double& u, double& du, double& lu) {
+    double f = s.F;
+    if (s.form == 0) {                      // Pade
+        u = a * r / (1.0 + r / f);
+        du = a * f * f / ((f + r) * (f + r));
+        lu = 2.0 * a * f * f * f / (r * (f + r) * (f + r) * (f + r));
+    } else if (s.form == 1) {               // RPA
+        double b = 1.0 / f, c = 0.2 / (f * f);
+        double den = 1.0 + b * r + c * r * r;
+        u = a * r / den;
+        du = a * (1.0 - c * r * r) / (den * den);
+        double d2 = -a * 2.0 * (c * r * den + (1.0 - c * r * r) * (b + 2.0 * c * r)) / (den * den * den);
+        lu = d2 + 2.0 / r * du;
+    } else {                                // Yukawa
+        double x = r / f, ex = std::exp(-x);
+        u = a * r * ex / (1.0 + x);
+        du = a * ex * (1.0 - x - x * x) / ((1.0 + x) * (1.0 + x));
+        double d2 = a * ex / (f * f * (1.0 + x) * (1.0 + x) * (1.0 + x)) * (-3.0 - 3.0 * x + x * x + x * x * x);
+        lu = d2 + 2.0 / r * du;
+    }
+}
+
+struct HegSector { int n; std::vector<cplx> inv, M; double logabs; bool ok; };
+
+// M[row][col] = e^{i k_col . r_row}; complex Gauss-Jordan with partial pivoting
+HegSector heg_sector(const Sys& s, const std::vector<V3>& r, int sp) {
+    const std::vector<int>& idx = s.sec[sp];
+    int n = (int)idx.size();
+    HegSector o;
+    o.n = n; o.logabs = 0.0; o.ok = true;
+    o.M.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < n; ++c) {
+            V3 k = s.kvec[s.occ[idx[c]]];
+            double ph = dot(k, r[idx[i]]);
+            o.M[(size_t)i * n + c] = cplx(std::cos(ph), std::sin(ph));
+        }
+    std::vector<cplx> A = o.M, I((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) I[(size_t)i * n + i] = 1.0;
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i) if (std::abs(A[(size_t)i * n + k]) > std::abs(A[(size_t)p * n + k])) p = i;
+        if (p != k) for (int j = 0; j < n; ++j) { std::swap(A[(size_t)k * n + j], A[(size_t)p * n + j]); std::swap(I[(size_t)k * n + j], I[(size_t)p * n + j]); }
+        cplx piv = A[(size_t)k * n + k];
+        if (std::abs(piv) == 0.0) { o.ok = false; o.logabs = -INFINITY; return o; }
+        o.logabs += std::log(std::abs(piv));
+        cplx ip = 1.0 / piv;
+        for (int j = 0; j < n; ++j) { A[(size_t)k * n + j] *= ip; I[(size_t)k * n + j] *= ip; }
+        for (int i = 0; i < n; ++i) {
+            if (i == k) continue;
+            cplx f = A[(size_t)i * n + k];
+            for (int j = 0; j < n; ++j) { A[(size_t)i * n + j] -= f * A[(size_t)k * n + j]; I[(size_t)i * n + j] -= f * I[(size_t)k * n + j]; }
+        }
+    }
+    o.inv = I;                  // inv[k][i]: orbital row k, electron column i
+    return o;
+}
+
+double heg_jastrow(const Sys& s, const std::vector<V3>& r, std::vector<V3>* g, std::vector<double>* lu) {
+    double u = 0.0;
+    if (g) g->assign(s.N, {0, 0, 0});
+    if (lu) lu->assign(s.N, 0.0);
+    for (int i = 0; i < s.N; ++i)
+        for (int j = i + 1; j < s.N; ++j) {
+            V3 rij = min_image(s, r[i] - r[j]);
+            double d = norm(rij);
+            if (!(d < s.L / 2.0 && d > 1e-10)) continue;          // heg.rs:468-470
+            double a = (s.spins[i] == s.spins[j]) ? s.jas[3] : s.jas[2];
+            double uu, du, l;
+            heg_pair(s, d, a, uu, du, l);
+            u += uu;
+            if (g) { V3 gg = (du / d) * rij; (*g)[i] = (*g)[i] + gg; (*g)[j] = (*g)[j] - gg; }
+            if (lu) { (*lu)[i] += l; (*lu)[j] += l; }
+        }
+    return u;
+}
+
+
+// Per-electron constant of the one-component-plasma Ewald energy: half the
+// interaction with its own images, the self term and the background term:
+// (1/2) sum_{n!=0} erfc(alpha nL)/(nL) - alpha/sqrt(pi) - pi N / (2 V alpha^2).
+double heg_madelung_self(const Sys& s) {
+    const double L = s.L, alpha = s.alphaL / L, V = L * L * L;
+    double img = 0.0;
+    for (int a = -3; a <= 3; ++a)
+        for (int b = -3; b <= 3; ++b)
+            for (int c = -3; c <= 3; ++c) {
+                if (!a && !b && !c) continue;
+                double d = L * std::sqrt((double)(a * a + b * b + c * c));
+                img += std::erfc(alpha * d) / d;
+            }
+    // the reciprocal i == j terms are inside |rho_k|^2 of heg_ewald
+    return 0.5 * img - alpha / std::sqrt(M_PI) - M_PI * s.N / (2.0 * V * alpha * alpha);
+}
+
+double heg_ewald(const Sys& s, const std::vector<V3>& r) {
+    const int N = s.N;
+    const double L = s.L, V = L * L * L;
+    if (s.quirks & 4) {                    // heg.rs:526-581
+        double alpha = 5.0 / L, vr = 0.0, vk = 0.0;
+        for (int i = 0; i < N; ++i)
+            for (int j = i + 1; j < N; ++j) {
+                double d = norm(min_image(s, r[i] - r[j]));
+                if (d > 1e-10) vr += std::erfc(alpha * d) / d;
+            }
+        double dk = 2.0 * M_PI / L;
+        for (int nx = -7; nx <= 7; ++nx)
+            for (int ny = -7; ny <= 7; ++ny)
+                for (int nz = -7; nz <= 7; ++nz) {
+                    if (!nx && !ny && !nz) continue;
+                    V3 k{nx * dk, ny * dk, nz * dk};
+                    double k2 = dot(k, k);
+                    double fac = 4.0 * M_PI / (V * k2) * std::exp(-k2 / (4.0 * alpha * alpha));
+                    cplx rho = 0.0;
+                    for (int i = 0; i < N; ++i) { double ph = dot(k, r[i]); rho += cplx(std::cos(ph), std::sin(ph)); }
+                    vk += 0.5 * fac * (std::norm(rho) - N);
+                }
+        return vr + vk - N * 0.448 / s.rs;
+    }
+    // one-component plasma: electrons in a uniform neutralising background
+    const double alpha = s.alphaL / L;
+    const double rcut = 5.6 / alpha;       // erfc(5.6) < 1e-14
+    double vr = 0.0;
+    for (int i = 0; i < N; ++i)
+        for (int j = i + 1; j < N; ++j) {
+            V3 d0 = min_image(s, r[i] - r[j]);
+            for (int a = -1; a <= 1; ++a)
+                for (int b = -1; b <= 1; ++b)
+                    for (int c = -1; c <= 1; ++c) {
+                        V3 d{d0.x + a * L, d0.y + b * L, d0.z + c * L};
+                        double dn = norm(d);
+                        if (dn < rcut) vr += std::erfc(alpha * dn) / dn;
+                    }
+        }
+    double vk = 0.0, dk = 2.0 * M_PI / L;
+    const int K = s.kmax;
+    for (int nx = 0; nx <= K; ++nx)
+        for (int ny = -K; ny <= K; ++ny)
+            for (int nz = -K; nz <= K; ++nz) {
+                // half space: nx > 0, or nx == 0 and (ny > 0 or ny == 0 and nz > 0)
+                if (nx == 0 && (ny < 0 || (ny == 0 && nz <= 0))) continue;
+                if (nx * nx + ny * ny + nz * nz > K * K) continue;
+                V3 k{nx * dk, ny * dk, nz * dk};
+                double k2 = dot(k, k);
+                cplx rho = 0.0;
+                for (int i = 0; i < N; ++i) { double ph = dot(k, r[i]); rho += cplx(std::cos(ph), std::sin(ph)); }
+                vk += 2.0 * (2.0 * M_PI / V) * std::exp(-k2 / (4.0 * alpha * alpha)) / k2 * std::norm(rho);
+            }
+    return vr + vk + N * heg_madelung_self(s);
+}
+
+struct HegEval { double logabs; bool ok; std::vector<V3> grad; std::vector<double> lap; double el; };
+
+// evaluate / local_energy of heg.rs:867-934 in the log domain; grad is
+// Re(grad_i psi / psi) (heg.rs:887-889 takes it numerically from |psi|),
+// lap is Re(lap_i psi / psi), el = -1/2 sum lap + V.
+HegEval heg_evaluate(const Sys& s, const std::vector<V3>& r) {
+    HegEval o;
+    o.grad.assign(s.N, {0, 0, 0});
+    o.lap.assign(s.N, 0.0);
+    std::vector<V3> gu;
+    std::vector<double> lu;
+    double u = heg_jastrow(s, r, &gu, &lu);
+    o.logabs = u;
+    o.ok = true;
+    double kin = 0.0;
+    for (int sp = 0; sp < 2; ++sp) {
+        HegSector sec = heg_sector(s, r, sp);
+        o.ok = o.ok && sec.ok;
+        o.logabs += sec.logabs;
+        const std::vector<int>& idx = s.sec[sp];
+        int n = sec.n;
+        for (int i = 0; i < n; ++i) {
+            int e = idx[i];
+            cplx gx = 0.0, gy = 0.0, gz = 0.0, l = 0.0, qx = 0.0, qy = 0.0, qz = 0.0;
+            for (int c = 0; c < n; ++c) {
+                V3 k = s.kvec[s.occ[idx[c]]];
+                cplx w = sec.inv[(size_t)c * n + i];
+                cplx wf = w * sec.M[(size_t)i * n + c];
+                cplx ik(0.0, 1.0);
+                gx += wf * ik * k.x; gy += wf * ik * k.y; gz += wf * ik * k.z;
+                l += wf * (-dot(k, k));
+                qx += w * ik * k.x; qy += w * ik * k.y; qz += w * ik * k.z;      // reference: no orbital factor
+            }
+            V3 gd{gx.real(), gy.real(), gz.real()};
+            V3 gc = (s.quirks & 8) ? V3{qx.real(), qy.real(), qz.real()} : gd;
+            o.grad[e] = gd + gu[e];
+            o.lap[e] = l.real() + lu[e] + dot(gu[e], gu[e]) + 2.0 * dot(gc, gu[e]);
+            kin += o.lap[e];
+        }
+    }
+    o.el = -0.5 * kin + heg_ewald(s, r);
+    return o;
+}
 // log|psi| only (the reference's evaluate(), src/systems/methane.rs:1122-1124).
 double log_psi(const Sys& s, const std::vector<V3>& r, int& sign, bool& ok) {
+    if (s.pw) {
+        double la = heg_jastrow(s, r, nullptr, nullptr);
+        ok = true;
+        for (int sp = 0; sp < 2; ++sp) { HegSector sec = heg_sector(s, r, sp); la += sec.logabs; ok = ok && sec.ok; }
+        sign = 1;
+        return la;
+    }
     Sector a = slater_sector(s, s.C, r, 0), b = slater_sector(s, s.C, r, 1);
     JOut J = jastrow(s, r);
     sign = a.sign * b.sign;
@@ -465,6 +709,11 @@ double log_psi(const Sys& s, const std::vector<V3>& r, int& sign, bool& ok) {
 // src/systems/lithium.rs:30-81, src/systems/hydrogen.rs:126-200.
 Eval evaluate_full(const Sys& s, const std::vector<V3>& r) {
     Eval e;
+    if (s.pw) {
+        HegEval h = heg_evaluate(s, r);
+        e.logabs = h.logabs; e.sign = 1; e.ok = h.ok; e.grad = h.grad; e.lap = h.lap; e.el = h.el;
+        return e;
+    }
     e.sec[0] = slater_sector(s, s.C, r, 0);
     e.sec[1] = slater_sector(s, s.C, r, 1);
     e.J = jastrow(s, r);
@@ -672,7 +921,11 @@ int sweep_walker(const Sys& s, const std::vector<int>& order, std::vector<V3>& r
         if (!okn) continue;
         if (fixed_node && sgn != sg) continue;
         double prob = std::exp(2.0 * (lpn - lp) + logG);
-        if (uacc < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
+        if (uacc < prob) {
+            if (s.pw) rn[e] = {rn[e].x - s.L * std::floor(rn[e].x / s.L), rn[e].y - s.L * std::floor(rn[e].y / s.L),
+                               rn[e].z - s.L * std::floor(rn[e].z / s.L)};
+            r = rn; lp = lpn; sg = sgn; ++acc;
+        }
     }
     return acc;
 }
@@ -772,8 +1025,12 @@ int orc_init(const orc_system_desc* d, int W, uint32_t walker0, uint64_t seed, d
             double n0, n1, n2, n3;
             box_muller(x.v[0], x.v[1], n0, n1);
             box_muller(x.v[2], x.v[3], n2, n3);
-            V3 c = s.init_nuc[e] >= 0 ? s.R[s.init_nuc[e]] : V3{0, 0, 0};
             double* p = pos + ((size_t)w * s.N + e) * 3;
+            if (s.pw) {   // uniform in the box (heg.rs:841-852)
+                p[0] = s.L * u01(x.v[0]); p[1] = s.L * u01(x.v[1]); p[2] = s.L * u01(x.v[2]);
+                continue;
+            }
+            V3 c = s.init_nuc[e] >= 0 ? s.R[s.init_nuc[e]] : V3{0, 0, 0};
             p[0] = c.x + s.init_sigma * n0;
             p[1] = c.y + s.init_sigma * n1;
             p[2] = c.z + s.init_sigma * n2;
@@ -906,6 +1163,16 @@ int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps,
         }
     *e_ref_io = e_ref;
     return t;
+}
+
+// HEG Ewald energy of one configuration and the per-electron constant
+// (alpha-invariance and Madelung checks).
+double orc_heg_ewald(const orc_system_desc* d, const double* pos, double alphaL, int kmax) {
+    Sys s = make_sys(d);
+    if (alphaL > 0) s.alphaL = alphaL;
+    if (kmax > 0) s.kmax = kmax;
+    std::vector<V3> r = load_cfg(pos, s.N);
+    return heg_ewald(s, r);
 }
 
 }  // extern "C"

@@ -9,9 +9,10 @@ runs in libqmc_gb300.so.
 from . import _lib
 from ._lib import QMCError, load_library
 from .api import Context, PinnedArray, System, Walkers, dmc_run, vmc_run
-from .systems import (SystemSpec, h2_mo, lithium_atom, methane_gto, methane_minimal, benzene_minimal, jastrow3_params,
+from .systems import (SystemSpec, h2_mo, lithium_atom, methane_gto, methane_minimal, benzene_minimal, electron_gas,
+                      heg_k_vectors, jastrow3_params,
                       reference_params_from_general, seeded_orthonormal, philox4x32, SEED_BASE)
 
 __all__ = ["QMCError", "load_library", "Context", "PinnedArray", "System", "Walkers", "vmc_run", "dmc_run", "SystemSpec",
-           "h2_mo", "lithium_atom", "methane_gto", "methane_minimal", "benzene_minimal", "jastrow3_params",
+           "h2_mo", "lithium_atom", "methane_gto", "methane_minimal", "benzene_minimal", "electron_gas", "heg_k_vectors", "jastrow3_params",
            "reference_params_from_general", "seeded_orthonormal", "philox4x32", "SEED_BASE", "_lib"]

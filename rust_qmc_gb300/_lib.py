@@ -13,10 +13,10 @@ LIB_PATH = os.path.join(HERE, "libqmc_gb300.so")
 QMC_OK, QMC_ERR_ARG, QMC_ERR_CUDA, QMC_ERR_TIMEOUT, QMC_ERR_SINGULAR = 0, 1, 2, 3, 4
 QMC_ERR_POPULATION, QMC_ERR_NONFINITE, QMC_ERR_UNSUPPORTED, QMC_ERR_NOMEM = 5, 6, 7, 8
 QMC_FP64, QMC_FP32_REFINE = 0, 1
-QMC_BASIS_GTO, QMC_BASIS_STO = 0, 1
-QMC_JAS_NONE, QMC_JAS_PADE_F, QMC_JAS_PADE_EEN = 0, 1, 2
+QMC_BASIS_GTO, QMC_BASIS_STO, QMC_BASIS_PW = 0, 1, 2
+QMC_JAS_NONE, QMC_JAS_PADE_F, QMC_JAS_PADE_EEN, QMC_JAS_HEG = 0, 1, 2, 3
 QMC_MOVE_ALL_GAUSS, QMC_MOVE_ALL_BOX, QMC_MOVE_ONE_GAUSS, QMC_MOVE_ONE_DRIFT = 0, 1, 2, 3
-QMC_QUIRK_J2_GRAD, QMC_QUIRK_J2_LAP = 1, 2
+QMC_QUIRK_J2_GRAD, QMC_QUIRK_J2_LAP, QMC_QUIRK_HEG_EWALD, QMC_QUIRK_HEG_CROSS = 1, 2, 4, 8
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)

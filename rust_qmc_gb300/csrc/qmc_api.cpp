@@ -67,13 +67,50 @@ int cuda_rc(cudaError_t e) {
 #define CU(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return cuda_rc(_e); } while (0)
 
 // Build the device-ready host description; validates every field.
+// Periodic electron gas: plane-wave orbitals e^{i k.r}; mo_coef holds the
+// wave vectors [n_mo][3] (src/systems/heg.rs:119-170).
+int build_hostsys_pw(const qmc_system_desc* d, HostSys& hs) {
+    if (!(d->box_L > 0) || d->n_mo <= 0 || !d->mo_coef || !d->occ || d->jastrow_kind != QMC_JAS_HEG) return QMC_ERR_ARG;
+    if (d->jas_F <= 0 || d->jas[0] < 0 || d->jas[0] > 2) return QMC_ERR_ARG;
+    if (!(d->quirks & 4) && !(d->jas[4] > 0 && d->jas[5] >= 1 && d->jas[5] <= 13)) return QMC_ERR_ARG;
+    hs.basis = QMC_BASIS_PW;
+    hs.box_L = d->box_L;
+    hs.n_mo = d->n_mo;
+    hs.kvec.assign(d->mo_coef, d->mo_coef + 3 * (size_t)d->n_mo);
+    hs.occ.assign(d->occ, d->occ + hs.N);
+    for (int e = 0; e < hs.N; ++e) if (hs.occ[e] < 0 || hs.occ[e] >= hs.n_mo) return QMC_ERR_ARG;
+    hs.jk = d->jastrow_kind;
+    hs.F = d->jas_F;
+    for (int i = 0; i < 8; ++i) hs.jas[i] = d->jas[i];
+    hs.quirks = d->quirks;
+    hs.init_nuc.assign(hs.N, -1);
+    hs.init_sigma = d->init_sigma;
+    hs.shape = -1;
+    if (hs.N == 54 && hs.n_up == 27) hs.shape = SHAPE_HEG54;
+    return hs.shape < 0 ? QMC_ERR_UNSUPPORTED : QMC_OK;
+}
+
 int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
-    if (!d || d->n_elec <= 0 || d->n_elec > 64 || !d->spins || d->n_nuc <= 0 || d->n_nuc > 32) return QMC_ERR_ARG;
+    if (!d || d->n_elec <= 0 || d->n_elec > 64 || !d->spins) return QMC_ERR_ARG;
+    if (d->basis_kind == QMC_BASIS_PW) {
+        hs = HostSys();
+        hs.N = d->n_elec;
+        hs.spins.assign(d->spins, d->spins + hs.N);
+        for (int e = 0; e < hs.N; ++e) {
+            if (hs.spins[e] != 1 && hs.spins[e] != -1) return QMC_ERR_ARG;
+            if (hs.spins[e] > 0) hs.n_up++; else hs.n_dn++;
+        }
+        for (int sig = 0; sig < 2; ++sig)
+            for (int e = 0; e < hs.N; ++e)
+                if ((hs.spins[e] > 0) == (sig == 0)) hs.perm.push_back(e);
+        return build_hostsys_pw(d, hs);
+    }
+    if (d->n_nuc <= 0 || d->n_nuc > 32) return QMC_ERR_ARG;
     if (!d->nuc_pos || !d->nuc_charge || d->n_ao <= 0 || !d->ao_nuc || !d->ao_l || !d->ao_m || !d->ao_prim_off) return QMC_ERR_ARG;
     if (!d->prim_exp || !d->prim_coef || d->n_mo <= 0 || !d->mo_coef || !d->occ) return QMC_ERR_ARG;
     if (d->box_L != 0.0) return QMC_ERR_UNSUPPORTED;
     if (d->basis_kind != QMC_BASIS_GTO && d->basis_kind != QMC_BASIS_STO) return QMC_ERR_ARG;
-    if (d->jastrow_kind < 0 || d->jastrow_kind > 2) return QMC_ERR_ARG;
+    if (d->jastrow_kind < 0 || d->jastrow_kind > 2) return QMC_ERR_ARG;   // QMC_JAS_HEG needs plane waves
     if (d->n_rot < 0 || d->n_rot > 16 || (d->n_rot && (!d->rot_occ || !d->rot_virt || !d->rot_angle))) return QMC_ERR_ARG;
     hs = HostSys();
     hs.N = d->n_elec;
@@ -209,13 +246,13 @@ int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cuda
     dw.Wcap = ((Wcap + 127) / 128) * 128;
     dw.prec = prec;
     size_t ts = prec == QMC_FP64 ? 8 : 4;
-    int nm = nmax_of_shape(hs.shape);
+    size_t nd = (size_t)dinv_elems_of_shape(hs.shape);
     size_t Wc = dw.Wcap;
     int nblk = (int)((Wc + 63) / 64);
     dw.partial_cap = 2 * nblk + 64;
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = cudaMalloc(&dw.pos, ts * 3 * hs.N * Wc);
-    if (e == cudaSuccess) e = cudaMalloc(&dw.dinv, ts * 2 * nm * nm * Wc);
+    if (e == cudaSuccess) e = cudaMalloc(&dw.dinv, ts * nd * Wc);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.logabs, 8 * Wc);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.sign, 4 * Wc);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.el, 8 * Wc);
@@ -226,7 +263,7 @@ int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cuda
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.el, 0, 8 * Wc, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dw.dinv, 0, ts * 2 * nm * nm * Wc, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dw.dinv, 0, ts * nd * Wc, st);
     if (e != cudaSuccess) { free_dev(dw); return cuda_rc(e); }
     return QMC_OK;
 }
@@ -385,7 +422,7 @@ int dmc_step(qmc_walkers_s* wk, double tau, double tau_move, double max_drift, i
     CK(rc);
     MeasureOut none;
     CK(launch_measure(hs, dw, (fp64_measure || dw.prec == QMC_FP64) ? 0 : 1, true, none, st));
-    CK(launch_branch(dw, wk->alt, wk->br, hs.N, nmax_of_shape(hs.shape), e_ref, tau, seed, step, st));
+    CK(launch_branch(dw, wk->alt, wk->br, hs.N, dinv_elems_of_shape(hs.shape), e_ref, tau, seed, step, st));
     double stats[2] = {0, 0};
     CU(cudaMemcpyAsync(stats, wk->br.stats, 16, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));

@@ -1,0 +1,711 @@
+// qmc_heg_kernels.cuh -- warp-per-walker kernels of the periodic homogeneous
+// electron gas (src/systems/heg.rs): complex plane-wave determinants
+// phi_k(r) = e^{i k.r}, a spin-dependent Jastrow with minimum image and a
+// cutoff at L/2, and the Ewald Coulomb energy.
+//
+// Lane j holds column j of each complex inverse Slater matrix; lane k
+// evaluates its own orbital e^{i k.r} (no AO contraction is needed).  The
+// FP64 measurement rebuilds the inverses by complex Gauss-Jordan elimination
+// and evaluates the Ewald sum: real-space pairs with images inside the erfc
+// cutoff, reciprocal sum over a half-space k list (rho_k built from per-lane
+// phase recursions and a warp reduction), and FP64 constants from the host.
+#pragma once
+#include <cstdio>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "qmc_internal.h"
+#include "qmc_device.cuh"
+
+namespace qmc {
+
+constexpr int HMAX_K = 1800;      // reciprocal half-space vectors (|n_i| <= 7 cube: 1687)
+
+template <class T>
+struct SysH {
+    T L, invL, halfL;
+    T F, pb, pc;                   // Jastrow: F, RPA b = 1/F, c = 0.2/F^2
+    int form;                      // 0 Pade, 1 RPA, 2 Yukawa
+    T a_ee[2];                     // [0] antiparallel, [1] parallel
+    int quirk_cross;               // reference cross term without the orbital factor
+    int real_images;               // 1: images inside the erfc cutoff; 0: minimum image only
+    T alpha, rcut;
+    double e_const;                // FP64 constant part of the Ewald energy
+    double ksum_const;             // added per walker with the reciprocal sum
+    T k2sum;                       // (1/2) sum over occupied |k|^2 of both sectors
+    T kvec[2][32][3];              // [sector][column][xyz]
+    int nk;
+    int perm[64];                  // internal -> caller electron index
+};
+
+// Reciprocal-space table of the Ewald sum (global memory, read uniformly).
+struct KTable {
+    int kint[HMAX_K][3];
+    double kw[HMAX_K];
+};
+
+template <class T>
+static bool fill_sysh(const HostSys& hs, int NE, int NUP, SysH<T>& S, KTable& KT) {
+    std::memset(&S, 0, sizeof(S));
+    std::memset(&KT, 0, sizeof(KT));
+    for (int ei = 0; ei < hs.N && ei < 64; ++ei) S.perm[ei] = hs.perm[ei];
+    if (hs.N != NE || hs.n_up != NUP || !(hs.box_L > 0)) return false;
+    const double L = hs.box_L, V = L * L * L;
+    S.L = (T)L; S.invL = (T)(1.0 / L); S.halfL = (T)(0.5 * L);
+    S.F = (T)hs.F; S.pb = (T)(1.0 / hs.F); S.pc = (T)(0.2 / (hs.F * hs.F));
+    S.form = (int)hs.jas[0];
+    S.a_ee[0] = (T)hs.jas[2]; S.a_ee[1] = (T)hs.jas[3];
+    S.quirk_cross = (hs.quirks & 8) ? 1 : 0;
+    const bool qe = (hs.quirks & 4) != 0;
+    const double alpha = qe ? 5.0 / L : hs.jas[4] / L;
+    const int K = qe ? 7 : (int)hs.jas[5];
+    S.alpha = (T)alpha;
+    S.real_images = qe ? 0 : 1;
+    S.rcut = (T)(5.6 / alpha);
+    // reciprocal half space; weight (4 pi / V) e^{-k^2 / 4 alpha^2} / k^2
+    int nk = 0;
+    double wsum = 0.0;
+    const double dk = 2.0 * M_PI / L;
+    for (int nx = 0; nx <= K; ++nx)
+        for (int ny = -K; ny <= K; ++ny)
+            for (int nz = -K; nz <= K; ++nz) {
+                if (nx == 0 && (ny < 0 || (ny == 0 && nz <= 0))) continue;
+                if (!qe && nx * nx + ny * ny + nz * nz > K * K) continue;
+                if (nk >= HMAX_K) return false;
+                double k2 = dk * dk * (nx * nx + ny * ny + nz * nz);
+                KT.kint[nk][0] = nx; KT.kint[nk][1] = ny; KT.kint[nk][2] = nz;
+                KT.kw[nk] = 4.0 * M_PI / V * std::exp(-k2 / (4.0 * alpha * alpha)) / k2;
+                wsum += KT.kw[nk];
+                ++nk;
+            }
+    S.nk = nk;
+    const int N = hs.N;
+    if (qe) {
+        // heg.rs:526-581: (1/2) sum_k f_k (|rho_k|^2 - N) and -0.448 N / r_s
+        const double rs = L / std::cbrt(4.0 * M_PI * N / 3.0);
+        S.ksum_const = -N * wsum;
+        S.e_const = -N * 0.448 / rs;
+    } else {
+        // one-component plasma: N [ (1/2) sum_{n!=0} erfc(alpha nL)/(nL) - alpha/sqrt(pi) - pi N/(2 V alpha^2) ]
+        double img = 0.0;
+        for (int a = -3; a <= 3; ++a)
+            for (int b = -3; b <= 3; ++b)
+                for (int c = -3; c <= 3; ++c) {
+                    if (!a && !b && !c) continue;
+                    double d = L * std::sqrt((double)(a * a + b * b + c * c));
+                    img += std::erfc(alpha * d) / d;
+                }
+        S.ksum_const = 0.0;
+        S.e_const = N * (0.5 * img - alpha / std::sqrt(M_PI) - M_PI * N / (2.0 * V * alpha * alpha));
+    }
+    double k2s = 0.0;
+    for (int sig = 0; sig < 2; ++sig) {
+        int col = 0;
+        for (int ei = 0; ei < hs.N; ++ei) {
+            int e = hs.perm[ei];
+            if ((hs.spins[e] > 0) != (sig == 0)) continue;
+            int k = hs.occ[e];
+            if (col >= 32) return false;
+            for (int c = 0; c < 3; ++c) S.kvec[sig][col][c] = (T)hs.kvec[3 * k + c];
+            k2s += hs.kvec[3 * k] * hs.kvec[3 * k] + hs.kvec[3 * k + 1] * hs.kvec[3 * k + 1] +
+                   hs.kvec[3 * k + 2] * hs.kvec[3 * k + 2];
+            ++col;
+        }
+    }
+    S.k2sum = (T)(0.5 * k2s);
+    return true;
+}
+
+template <class T>
+__device__ __forceinline__ void load_sysh(SysH<T>* dst, const SysH<T>* __restrict__ src, int bytes) {
+    const int4* s = reinterpret_cast<const int4*>(src);
+    int4* d = reinterpret_cast<int4*>(dst);
+    for (int i = threadIdx.x; i < bytes / (int)sizeof(int4); i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
+__device__ __forceinline__ void fsincos(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void fsincos(float x, float* s, float* c) { __sincosf(x, s, c); }
+
+template <class T>
+__device__ __forceinline__ T min_img(T d, const SysH<T>& S) { return d - S.L * rint(d * S.invL); }
+
+// Jastrow pair (src/systems/heg.rs:352-444): u, u'(r) and u'' + 2u'/r;
+// zero outside (1e-10, L/2).
+template <class T>
+__device__ __forceinline__ void heg_u(const SysH<T>& S, T r, T a, T& u, T& du, T& lu) {
+    u = 0; du = 0; lu = 0;
+    if (!(r < S.halfL && r > T(1e-10))) return;
+    if (S.form == 0) {
+        T fr = S.F + r;
+        u = a * r / (1 + r / S.F);
+        du = a * S.F * S.F / (fr * fr);
+        lu = 2 * a * S.F * S.F * S.F / (r * fr * fr * fr);
+    } else if (S.form == 1) {
+        T den = 1 + S.pb * r + S.pc * r * r;
+        u = a * r / den;
+        du = a * (1 - S.pc * r * r) / (den * den);
+        T d2 = -a * 2 * (S.pc * r * den + (1 - S.pc * r * r) * (S.pb + 2 * S.pc * r)) / (den * den * den);
+        lu = d2 + 2 / r * du;
+    } else {
+        T x = r / S.F, ex = fexp(-x), op = 1 + x;
+        u = a * r * ex / op;
+        du = a * ex * (1 - x - x * x) / (op * op);
+        T d2 = a * ex / (S.F * S.F * op * op * op) * (-3 - 3 * x + x * x + x * x * x);
+        lu = d2 + 2 / r * du;
+    }
+}
+
+template <class T, int NE>
+struct HLanePos {
+    T x[2], y[2], z[2];
+    __device__ __forceinline__ void get(int e, T& ex, T& ey, T& ez) const {
+        T a = e < 32 ? x[0] : x[1], b = e < 32 ? y[0] : y[1], c = e < 32 ? z[0] : z[1];
+        ex = __shfl_sync(0xffffffffu, a, e & 31);
+        ey = __shfl_sync(0xffffffffu, b, e & 31);
+        ez = __shfl_sync(0xffffffffu, c, e & 31);
+    }
+};
+
+template <class T>
+__device__ __forceinline__ T hsum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Jastrow change (and gradients) for electron e moving o -> n.
+template <int NE, int NUP, class T, bool GRAD>
+__device__ __forceinline__ T hjastrow_delta(const SysH<T>& S, const HLanePos<T, NE>& P, int lane, int e, T ox, T oy,
+                                            T oz, T nx, T ny, T nz, T (&go)[3], T (&gn)[3]) {
+    T du = 0, g[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NE && j != e) {
+            const T a = S.a_ee[((j < NUP) == (e < NUP)) ? 1 : 0];
+            T ax = min_img(ox - P.x[r], S), ay = min_img(oy - P.y[r], S), az = min_img(oz - P.z[r], S);
+            T bx = min_img(nx - P.x[r], S), by = min_img(ny - P.y[r], S), bz = min_img(nz - P.z[r], S);
+            T ra = fsqrt(ax * ax + ay * ay + az * az), rb = fsqrt(bx * bx + by * by + bz * bz);
+            T ua, dua, lua, ub, dub, lub;
+            heg_u(S, ra, a, ua, dua, lua);
+            heg_u(S, rb, a, ub, dub, lub);
+            du += ub - ua;
+            if (GRAD) {
+                T fa = ra > 0 ? dua / ra : T(0), fb = rb > 0 ? dub / rb : T(0);
+                g[0] += fa * ax; g[1] += fa * ay; g[2] += fa * az;
+                g[3] += fb * bx; g[4] += fb * by; g[5] += fb * bz;
+            }
+        }
+    }
+    du = hsum(du);
+    if (GRAD) {
+        go[0] = hsum(g[0]); go[1] = hsum(g[1]); go[2] = hsum(g[2]);
+        gn[0] = hsum(g[3]); gn[1] = hsum(g[4]); gn[2] = hsum(g[5]);
+    }
+    return du;
+}
+
+template <class TS>
+__global__ void khw_init(const SysH<double>* __restrict__ S, TS* __restrict__ pos, int NE, int W, int Wcap,
+                         uint64_t seed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NE * W) return;
+    int e = i / W, w = i - e * W;
+    U4 x = rng_draw(seed, (uint32_t)w, 0, (uint32_t)S->perm[e], TAG_INIT);
+    double L = S->L;
+    pos[(3 * e + 0) * (size_t)Wcap + w] = (TS)(L * to_u01(x.x, 0.0));
+    pos[(3 * e + 1) * (size_t)Wcap + w] = (TS)(L * to_u01(x.y, 0.0));
+    pos[(3 * e + 2) * (size_t)Wcap + w] = (TS)(L * to_u01(x.z, 0.0));
+}
+
+// Single-electron sweeps, one warp per walker.
+template <int NE, int NUP, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
+                                                      T* __restrict__ gdinv, int W, int Wcap, int n_sweeps,
+                                                      uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+                                                      unsigned long long* acc_out, int* flags) {
+    constexpr int NDN = NE - NUP;
+    constexpr int NM = NUP > NDN ? NUP : NDN;
+    __shared__ SysH<T> S;
+    load_sysh(&S, Sg, (int)sizeof(SysH<T>));
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
+    if (w >= W) return;
+    HLanePos<T, NE> P;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        const bool ok = j < NE;
+        P.x[r] = ok ? gpos[(3 * j + 0) * (size_t)Wcap + w] : T(0);
+        P.y[r] = ok ? gpos[(3 * j + 1) * (size_t)Wcap + w] : T(0);
+        P.z[r] = ok ? gpos[(3 * j + 2) * (size_t)Wcap + w] : T(0);
+    }
+    // complex inverse columns: [sector][k] (re, im); storage [2][NM*NM][2][Wcap]
+    T Dr0[NM], Di0[NM], Dr1[NM], Di1[NM];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
+        Dr0[k] = lane < NUP ? gdinv[b0 + w] : T(0);
+        Di0[k] = lane < NUP ? gdinv[b0 + Wcap + w] : T(0);
+        Dr1[k] = lane < NDN ? gdinv[b1 + w] : T(0);
+        Di1[k] = lane < NDN ? gdinv[b1 + Wcap + w] : T(0);
+    }
+    unsigned acc = 0;
+    int flg = 0;
+    for (int it = 0; it < n_sweeps; ++it) {
+        const uint64_t st = step0 + (uint64_t)it;
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            T (&Dr)[NM] = sig == 0 ? Dr0 : Dr1;
+            T (&Di)[NM] = sig == 0 ? Di0 : Di1;
+            const int NS = sig == 0 ? NUP : NDN;
+            const T kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
+            for (int q = 0; q < NS; ++q) {
+                const int e = sig * NUP + q;
+                T rx, ry, rz;
+                P.get(e, rx, ry, rz);
+                MoveDraw<T> md = move_draw<T>(seed, (uint32_t)w, st, (uint32_t)e);
+                T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
+                if (MOVE == MOVE_ONE_DRIFT) {
+                    // Re(grad ln D) at the current position: lane l sums (i k_j phi_j) Dinv[j][l]
+                    T s, c;
+                    fsincos(kx * rx + ky * ry + kz * rz, &s, &c);
+                    T ax = 0, ay = 0, az = 0;
+#pragma unroll
+                    for (int j = 0; j < NM; ++j) {
+                        T pr = __shfl_sync(0xffffffffu, c, j), pi = __shfl_sync(0xffffffffu, s, j);
+                        T kjx = S.kvec[sig][j][0], kjy = S.kvec[sig][j][1], kjz = S.kvec[sig][j][2];
+                        // Re(i k phi D) = -k Im(phi D)
+                        T im = pr * Di[j] + pi * Dr[j];
+                        ax -= kjx * im; ay -= kjy * im; az -= kjz * im;
+                    }
+                    ax = __shfl_sync(0xffffffffu, ax, q); ay = __shfl_sync(0xffffffffu, ay, q); az = __shfl_sync(0xffffffffu, az, q);
+                    T g0[3], g1[3];
+                    hjastrow_delta<NE, NUP, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
+                    dlx = tau * 2 * (ax + g0[0]); dly = tau * 2 * (ay + g0[1]); dlz = tau * 2 * (az + g0[2]);
+                    T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
+                    if (m > maxd) { T sc = maxd / m; dlx *= sc; dly *= sc; dlz *= sc; }
+                    T sd2 = fsqrt(2 * tau);
+                    nx = rx + dlx + sd2 * md.n0; ny = ry + dly + sd2 * md.n1; nz = rz + dlz + sd2 * md.n2;
+                } else {
+                    nx = rx + step * md.n0; ny = ry + step * md.n1; nz = rz + step * md.n2;
+                }
+                T ps, pc;
+                fsincos(kx * nx + ky * ny + kz * nz, &ps, &pc);
+                // t_l = sum_j phi_j Dinv[j][l]; R = t_q
+                T tr = 0, ti = 0;
+#pragma unroll
+                for (int j = 0; j < NM; ++j) {
+                    T pr = __shfl_sync(0xffffffffu, pc, j), pi = __shfl_sync(0xffffffffu, ps, j);
+                    tr += pr * Dr[j] - pi * Di[j];
+                    ti += pr * Di[j] + pi * Dr[j];
+                }
+                const T Rr = __shfl_sync(0xffffffffu, tr, q), Ri = __shfl_sync(0xffffffffu, ti, q);
+                const T R2 = Rr * Rr + Ri * Ri;
+                T g0[3], gn[3];
+                T du = hjastrow_delta<NE, NUP, T, MOVE == MOVE_ONE_DRIFT>(S, P, lane, e, rx, ry, rz, nx, ny, nz, g0, gn);
+                if (MOVE == MOVE_ONE_DRIFT) {
+                    // Re(grad ln D') = Re(G / R) with G = sum_j i k_j phi_j(r') Dinv[j][q]
+                    T Gx_r = 0, Gy_r = 0, Gz_r = 0, Gx_i = 0, Gy_i = 0, Gz_i = 0;
+#pragma unroll
+                    for (int j = 0; j < NM; ++j) {
+                        T pr = __shfl_sync(0xffffffffu, pc, j), pi = __shfl_sync(0xffffffffu, ps, j);
+                        T re = pr * Dr[j] - pi * Di[j], im = pr * Di[j] + pi * Dr[j];
+                        T kjx = S.kvec[sig][j][0], kjy = S.kvec[sig][j][1], kjz = S.kvec[sig][j][2];
+                        Gx_r -= kjx * im; Gy_r -= kjy * im; Gz_r -= kjz * im;
+                        Gx_i += kjx * re; Gy_i += kjy * re; Gz_i += kjz * re;
+                    }
+                    Gx_r = __shfl_sync(0xffffffffu, Gx_r, q); Gy_r = __shfl_sync(0xffffffffu, Gy_r, q); Gz_r = __shfl_sync(0xffffffffu, Gz_r, q);
+                    Gx_i = __shfl_sync(0xffffffffu, Gx_i, q); Gy_i = __shfl_sync(0xffffffffu, Gy_i, q); Gz_i = __shfl_sync(0xffffffffu, Gz_i, q);
+                    T iR2 = R2 > 0 ? T(1) / R2 : T(0);
+                    // Re(G / R) = (G_r R_r + G_i R_i) / |R|^2
+                    T cx = (Gx_r * Rr + Gx_i * Ri) * iR2 + gn[0];
+                    T cy = (Gy_r * Rr + Gy_i * Ri) * iR2 + gn[1];
+                    T cz = (Gz_r * Rr + Gz_i * Ri) * iR2 + gn[2];
+                    cx *= 2 * tau; cy *= 2 * tau; cz *= 2 * tau;
+                    T m = fsqrt(cx * cx + cy * cy + cz * cz);
+                    if (m > maxd) { T sc = maxd / m; cx *= sc; cy *= sc; cz *= sc; }
+                    T fx = nx - rx - dlx, fy = ny - ry - dly, fz = nz - rz - dlz;
+                    T qx = rx - nx - cx, qy = ry - ny - cy, qz = rz - nz - cz;
+                    logG = ((fx * fx + fy * fy + fz * fz) - (qx * qx + qy * qy + qz * qz)) / (4 * tau);
+                }
+                T prob = R2 * fexp(2 * du);
+                if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
+                if (prob != prob) flg |= FLAG_NONFINITE;
+                if (md.uacc < prob && R2 > T(0)) {
+                    // wrap the new position into the box
+                    T wx = nx - S.L * floor(nx * S.invL), wy = ny - S.L * floor(ny * S.invL), wz = nz - S.L * floor(nz * S.invL);
+                    if ((e & 31) == lane) {
+                        if (e < 32) { P.x[0] = wx; P.y[0] = wy; P.z[0] = wz; }
+                        else { P.x[1] = wx; P.y[1] = wy; P.z[1] = wz; }
+                    }
+                    // complex Sherman-Morrison: D'[k][l] = D[k][l] - D[k][q] t_l / R, D'[k][q] = D[k][q] / R
+                    const T iR2 = T(1) / R2;
+                    const T iRr = Rr * iR2, iRi = -Ri * iR2;              // 1/R
+                    const T fr = tr * iRr - ti * iRi, fi = tr * iRi + ti * iRr;   // t_l / R
+#pragma unroll
+                    for (int k = 0; k < NM; ++k) {
+                        T qr = __shfl_sync(0xffffffffu, Dr[k], q), qi = __shfl_sync(0xffffffffu, Di[k], q);
+                        T nr, ni;
+                        if (lane == q) { nr = qr * iRr - qi * iRi; ni = qr * iRi + qi * iRr; }
+                        else { nr = Dr[k] - (qr * fr - qi * fi); ni = Di[k] - (qr * fi + qi * fr); }
+                        Dr[k] = nr; Di[k] = ni;
+                    }
+                    ++acc;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int j = lane + 32 * r;
+        if (j < NE) {
+            gpos[(3 * j + 0) * (size_t)Wcap + w] = P.x[r];
+            gpos[(3 * j + 1) * (size_t)Wcap + w] = P.y[r];
+            gpos[(3 * j + 2) * (size_t)Wcap + w] = P.z[r];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
+        if (lane < NUP) { gdinv[b0 + w] = Dr0[k]; gdinv[b0 + Wcap + w] = Di0[k]; }
+        if (lane < NDN) { gdinv[b1 + w] = Dr1[k]; gdinv[b1 + Wcap + w] = Di1[k]; }
+    }
+    if (lane == 0) {
+        if (acc) atomicAdd(acc_out, (unsigned long long)acc);
+        if (flg) atomicOr(flags, flg);
+    }
+}
+
+// FP64 (or FP32) full evaluation: complex Gauss-Jordan, kinetic terms, Ewald.
+template <int NE, int NUP, class TC, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
+                                                        const TS* __restrict__ gpos,
+                                                        TS* __restrict__ gdinv, double* __restrict__ glog,
+                                                        int* __restrict__ gsign, double* __restrict__ gel, int W,
+                                                        int Wcap, int write_state, double* __restrict__ out_grad,
+                                                        double* __restrict__ out_lap, double* partial, int* flags) {
+    constexpr int NDN = NE - NUP;
+    constexpr int NM = NUP > NDN ? NUP : NDN;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
+    TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
+    load_sysh(&S, Sg, (int)sizeof(SysH<TC>));
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wib;
+    const bool act = w < W;
+    TC* Mr = rows + (size_t)wib * 2 * NM * 32;        // [re|im][row][lane]
+    TC* Mi = Mr + NM * 32;
+    double e_l = 0.0;
+    if (act) {
+        HLanePos<TC, NE> P;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int j = lane + 32 * r;
+            const bool ok = j < NE;
+            P.x[r] = ok ? (TC)gpos[(3 * j + 0) * (size_t)Wcap + w] : TC(0);
+            P.y[r] = ok ? (TC)gpos[(3 * j + 1) * (size_t)Wcap + w] : TC(0);
+            P.z[r] = ok ? (TC)gpos[(3 * j + 2) * (size_t)Wcap + w] : TC(0);
+        }
+        double logdet = 0.0;
+        bool ok = true;
+        TC gdx[2] = {0, 0}, gdy[2] = {0, 0}, gdz[2] = {0, 0}, gqx[2] = {0, 0}, gqy[2] = {0, 0}, gqz[2] = {0, 0};
+        TC ldet[2] = {0, 0};
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            const int NS = sig == 0 ? NUP : NDN;
+            const TC kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
+            for (int q = 0; q < NS; ++q) {
+                TC rx, ry, rz;
+                P.get(sig * NUP + q, rx, ry, rz);
+                TC s, c;
+                fsincos(kx * rx + ky * ry + kz * rz, &s, &c);
+                Mr[q * 32 + lane] = c;
+                Mi[q * 32 + lane] = s;
+            }
+            __syncwarp();
+            // complex Gauss-Jordan: lane j carries column j of [D | I]
+            TC Ar[NM], Ai[NM], Ir[NM], Ii[NM];
+#pragma unroll
+            for (int i = 0; i < NM; ++i) {
+                bool in = i < NS && lane < NS;
+                Ar[i] = in ? Mr[i * 32 + lane] : TC(i == lane ? 1 : 0);
+                Ai[i] = in ? Mi[i * 32 + lane] : TC(0);
+                Ir[i] = (i == lane) ? TC(1) : TC(0);
+                Ii[i] = 0;
+            }
+#pragma unroll
+            for (int k = 0; k < NM; ++k) {
+                if (k >= NS) break;
+                int p = k;
+                TC best = Ar[k] * Ar[k] + Ai[k] * Ai[k];
+#pragma unroll
+                for (int i = k + 1; i < NM; ++i) {
+                    TC a = Ar[i] * Ar[i] + Ai[i] * Ai[i];
+                    if (i < NS && a > best) { best = a; p = i; }
+                }
+                p = __shfl_sync(0xffffffffu, p, k);
+#pragma unroll
+                for (int i = k + 1; i < NM; ++i) {
+                    bool sw = (i == p);
+                    TC a = Ar[k], b = Ar[i]; Ar[k] = sw ? b : a; Ar[i] = sw ? a : b;
+                    a = Ai[k]; b = Ai[i]; Ai[k] = sw ? b : a; Ai[i] = sw ? a : b;
+                    a = Ir[k]; b = Ir[i]; Ir[k] = sw ? b : a; Ir[i] = sw ? a : b;
+                    a = Ii[k]; b = Ii[i]; Ii[k] = sw ? b : a; Ii[i] = sw ? a : b;
+                }
+                TC pr = __shfl_sync(0xffffffffu, Ar[k], k), pi = __shfl_sync(0xffffffffu, Ai[k], k);
+                TC pa = pr * pr + pi * pi;
+                if (!(pa > TC(0))) { ok = false; pr = 1; pi = 0; pa = 1; }
+                logdet += 0.5 * log((double)pa);
+                TC ipr = pr / pa, ipi = -pi / pa;
+                TC t;
+                t = Ar[k] * ipr - Ai[k] * ipi; Ai[k] = Ar[k] * ipi + Ai[k] * ipr; Ar[k] = t;
+                t = Ir[k] * ipr - Ii[k] * ipi; Ii[k] = Ir[k] * ipi + Ii[k] * ipr; Ir[k] = t;
+#pragma unroll
+                for (int i = 0; i < NM; ++i) {
+                    if (i == k || i >= NS) continue;
+                    TC fr = __shfl_sync(0xffffffffu, Ar[i], k), fi = __shfl_sync(0xffffffffu, Ai[i], k);
+                    Ar[i] -= fr * Ar[k] - fi * Ai[k]; Ai[i] -= fr * Ai[k] + fi * Ar[k];
+                    Ir[i] -= fr * Ir[k] - fi * Ii[k]; Ii[i] -= fr * Ii[k] + fi * Ir[k];
+                }
+            }
+            if (write_state && lane < NS) {
+#pragma unroll
+                for (int k = 0; k < NM; ++k) {
+                    if (k >= NS) break;
+                    size_t b = ((size_t)(sig * NM * NM + k * NM + lane)) * 2 * Wcap;
+                    gdinv[b + w] = (TS)Ir[k];
+                    gdinv[b + Wcap + w] = (TS)Ii[k];
+                }
+            }
+            // lane = electron row q: grad ln D = sum_j Dinv[j][q] i k_j phi_j(r_q); lap D / D = -sum_j Dinv phi k^2
+            if (lane < NS) {
+                TC ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0, lr = 0;
+#pragma unroll
+                for (int j = 0; j < NM; ++j) {
+                    if (j >= NS) break;
+                    TC pr = Mr[lane * 32 + j], pi = Mi[lane * 32 + j];
+                    TC re = pr * Ir[j] - pi * Ii[j], im = pr * Ii[j] + pi * Ir[j];
+                    TC kjx = S.kvec[sig][j][0], kjy = S.kvec[sig][j][1], kjz = S.kvec[sig][j][2];
+                    ax -= kjx * im; ay -= kjy * im; az -= kjz * im;                 // Re(i k w phi)
+                    bx -= kjx * Ii[j]; by -= kjy * Ii[j]; bz -= kjz * Ii[j];         // Re(i k w), reference form
+                    lr -= (kjx * kjx + kjy * kjy + kjz * kjz) * re;
+                }
+                gdx[sig] = ax; gdy[sig] = ay; gdz[sig] = az;
+                gqx[sig] = bx; gqy[sig] = by; gqz[sig] = bz;
+                ldet[sig] = lr;
+            }
+            __syncwarp();
+        }
+        // Jastrow and real-space Ewald for this lane's electrons (pairs from both ends)
+        TC u = 0, kin = 0;
+        double vreal = 0.0;
+#pragma unroll
+        for (int sig = 0; sig < 2; ++sig) {
+            const int NS = sig == 0 ? NUP : NDN;
+            const int i = sig * NUP + lane;
+            const bool own = lane < NS;
+            TC xi, yi, zi;
+            P.get(min(i, NE - 1), xi, yi, zi);
+            TC gx = 0, gy = 0, gz = 0, lu = 0;
+            for (int j = 0; j < NE; ++j) {
+                TC xj, yj, zj;
+                P.get(j, xj, yj, zj);
+                if (!own || j == i) continue;
+                const TC a = S.a_ee[((j < NUP) == (i < NUP)) ? 1 : 0];
+                TC dx = min_img(xi - xj, S), dy = min_img(yi - yj, S), dz = min_img(zi - zj, S);
+                TC r = fsqrt(dx * dx + dy * dy + dz * dz);
+                TC uu, du, l;
+                heg_u(S, r, a, uu, du, l);
+                u += TC(0.5) * uu;
+                if (r < S.halfL && r > TC(1e-10)) {
+                    TC f = du / r;
+                    gx += f * dx; gy += f * dy; gz += f * dz;
+                    lu += l;
+                }
+                if (S.real_images) {
+                    for (int ia = -1; ia <= 1; ++ia)
+                        for (int ib = -1; ib <= 1; ++ib)
+                            for (int ic = -1; ic <= 1; ++ic) {
+                                double ex = (double)dx + ia * (double)S.L, ey = (double)dy + ib * (double)S.L,
+                                       ez = (double)dz + ic * (double)S.L;
+                                double d = sqrt(ex * ex + ey * ey + ez * ez);
+                                if (d < (double)S.rcut) vreal += 0.5 * erfc((double)S.alpha * d) / d;
+                            }
+                } else if (r > TC(1e-10)) {
+                    vreal += 0.5 * erfc((double)S.alpha * (double)r) / (double)r;
+                }
+            }
+            if (own) {
+                TC cx = S.quirk_cross ? gqx[sig] : gdx[sig], cy = S.quirk_cross ? gqy[sig] : gdy[sig],
+                   cz = S.quirk_cross ? gqz[sig] : gdz[sig];
+                TC lp = ldet[sig] + lu + gx * gx + gy * gy + gz * gz + 2 * (cx * gx + cy * gy + cz * gz);
+                kin += lp;
+                if (out_grad) {
+                    out_grad[((size_t)w * NE + i) * 3 + 0] = gdx[sig] + gx;
+                    out_grad[((size_t)w * NE + i) * 3 + 1] = gdy[sig] + gy;
+                    out_grad[((size_t)w * NE + i) * 3 + 2] = gdz[sig] + gz;
+                }
+                if (out_lap) out_lap[(size_t)w * NE + i] = lp;
+            }
+        }
+        // reciprocal Ewald: rho_k = sum_i e^{i k.r_i}.  Each lane owns electrons
+        // lane and lane+32 and builds e^{i m dk x} (m = 0..KM) by repeated
+        // multiplication; negative m are conjugates.  One warp reduction per k.
+        double vk = 0.0;
+        {
+            constexpr int KM = 14;
+            const double dk = 2.0 * M_PI / (double)S.L;
+            double Exr[2][KM + 1], Exi[2][KM + 1], Eyr[2][KM + 1], Eyi[2][KM + 1], Ezr[2][KM + 1], Ezi[2][KM + 1];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                double bxs, bxc, bys, byc, bzs, bzc;
+                sincos(dk * (double)P.x[r], &bxs, &bxc);
+                sincos(dk * (double)P.y[r], &bys, &byc);
+                sincos(dk * (double)P.z[r], &bzs, &bzc);
+                Exr[r][0] = 1; Exi[r][0] = 0; Eyr[r][0] = 1; Eyi[r][0] = 0; Ezr[r][0] = 1; Ezi[r][0] = 0;
+                for (int m = 1; m <= KM; ++m) {
+                    Exr[r][m] = Exr[r][m - 1] * bxc - Exi[r][m - 1] * bxs; Exi[r][m] = Exr[r][m - 1] * bxs + Exi[r][m - 1] * bxc;
+                    Eyr[r][m] = Eyr[r][m - 1] * byc - Eyi[r][m - 1] * bys; Eyi[r][m] = Eyr[r][m - 1] * bys + Eyi[r][m - 1] * byc;
+                    Ezr[r][m] = Ezr[r][m - 1] * bzc - Ezi[r][m - 1] * bzs; Ezi[r][m] = Ezr[r][m - 1] * bzs + Ezi[r][m - 1] * bzc;
+                }
+            }
+            for (int t = 0; t < S.nk; ++t) {
+                const int nx = KT->kint[t][0], ny = KT->kint[t][1], nz = KT->kint[t][2];
+                const int ay = ny < 0 ? -ny : ny, az = nz < 0 ? -nz : nz;
+                double rr = 0.0, ri = 0.0;
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    if (lane + 32 * r >= NE) continue;
+                    double xr = Exr[r][nx], xi = Exi[r][nx];
+                    double yr = Eyr[r][ay], yi = ny < 0 ? -Eyi[r][ay] : Eyi[r][ay];
+                    double zr = Ezr[r][az], zi = nz < 0 ? -Ezi[r][az] : Ezi[r][az];
+                    double pr = xr * yr - xi * yi, pi = xr * yi + xi * yr;
+                    rr += pr * zr - pi * zi;
+                    ri += pr * zi + pi * zr;
+                }
+                rr = hsum(rr); ri = hsum(ri);
+                vk += KT->kw[t] * (rr * rr + ri * ri);
+            }
+        }
+        u = hsum(u);
+        kin = hsum(kin);
+        vreal = hsum(vreal);
+        double V = vreal + vk + S.ksum_const + S.e_const;
+        e_l = -0.5 * (double)kin + V;
+        if (lane == 0) {
+            int fl = 0;
+            if (!ok) fl |= FLAG_SINGULAR;
+            if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
+            if (fl) atomicOr(flags, fl);
+            if (write_state) { glog[w] = logdet + (double)u; gsign[w] = 1; gel[w] = e_l; }
+        }
+    }
+    if (partial) {
+        __shared__ double ps[WPB];
+        if (lane == 0) ps[wib] = act ? e_l : 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Comp c{0.0, 0.0};
+            for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
+            partial[2 * blockIdx.x] = c.s;
+            partial[2 * blockIdx.x + 1] = c.c;
+        }
+    }
+}
+
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+
+template <int NE, int NUP>
+struct HegShapeOps {
+    static constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    static constexpr int WPB = 4;
+
+    // Device copies: [SysH<T> | pad | KTable], cached per system and rebuilt
+    // when the parameters change (HostSys::version).
+    template <class T>
+    static int table(const HostSys& hs, const SysH<T>** out, const KTable** kt = nullptr) {
+        int slot = sizeof(T) == 8 ? 0 : 1;
+        const size_t off = ((sizeof(SysH<T>) + 255) / 256) * 256;
+        if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
+            std::vector<unsigned char> buf(off + sizeof(KTable));
+            SysH<T>* h = reinterpret_cast<SysH<T>*>(buf.data());
+            KTable* k = reinterpret_cast<KTable*>(buf.data() + off);
+            if (!fill_sysh<T>(hs, NE, NUP, *h, *k)) return 7;
+            if (!hs.dev_table[slot] && cudaMalloc(&hs.dev_table[slot], buf.size()) != cudaSuccess) return 8;
+            if (cudaMemcpy(hs.dev_table[slot], buf.data(), buf.size(), cudaMemcpyHostToDevice) != cudaSuccess) return 2;
+            hs.dev_table_version[slot] = hs.version;
+        }
+        *out = static_cast<const SysH<T>*>(hs.dev_table[slot]);
+        if (kt) *kt = reinterpret_cast<const KTable*>(static_cast<const unsigned char*>(hs.dev_table[slot]) + off);
+        return 0;
+    }
+
+    static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
+        const SysH<double>* S;
+        int rc = table<double>(hs, &S);
+        if (rc) return rc;
+        int n = NE * dw.W, tpb = 256;
+        if (dw.prec == 0) khw_init<double><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(S, (double*)dw.pos, NE, dw.W, dw.Wcap, seed);
+        else khw_init<float><<<(n + tpb - 1) / tpb, tpb, 0, st>>>(S, (float*)dw.pos, NE, dw.W, dw.Wcap, seed);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    template <class TC, class TS>
+    static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
+        const SysH<TC>* S;
+        const KTable* KT;
+        int rc = table<TC>(hs, &S, &KT);
+        if (rc) return rc;
+        int nb = (dw.W + WPB - 1) / WPB;
+        size_t smem = ((sizeof(SysH<TC>) + 15) / 16) * 16 + sizeof(TC) * WPB * 2 * NM * 32;
+        auto kern = khw_measure<NE, NUP, TC, TS, WPB>;
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        double* partial = (ws && dw.partial && dw.partial_cap >= 2 * nb + 1) ? dw.partial : nullptr;
+        kern<<<nb, 32 * WPB, smem, st>>>(S, KT, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W,
+                                         dw.Wcap, ws ? 1 : 0, out.grad, out.lap, partial, dw.flags);
+        ++g_launch_count;
+        if (cudaGetLastError() != cudaSuccess) return 2;
+        if (!partial) return 0;
+        return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
+    }
+
+    static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
+        if (out.O || out.fhf || out.omega) return 7;
+        if (cp == 0) return dw.prec == 0 ? measure2<double, double>(hs, dw, ws, out, st)
+                                         : measure2<double, float>(hs, dw, ws, out, st);
+        if (dw.prec == 1) return measure2<float, float>(hs, dw, ws, out, st);
+        return 7;
+    }
+
+    template <class T, int MOVE>
+    static int sweep_t(const HostSys& hs, DevWalkers& dw, int n, uint64_t s0, double step, double tau, double maxd,
+                       uint64_t seed, cudaStream_t st) {
+        const SysH<T>* S;
+        int rc = table<T>(hs, &S);
+        if (rc) return rc;
+        int nb = (dw.W + WPB - 1) / WPB;
+        khw_sweep<NE, NUP, T, MOVE, WPB><<<nb, 32 * WPB, 0, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.W, dw.Wcap, n, s0,
+                                                                (T)step, (T)tau, (T)maxd, seed, dw.acc, dw.flags);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    static int sweep(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,
+                     double maxd, uint64_t seed, cudaStream_t st) {
+        if (dw.fixed_node) return 7;     // complex determinants have no nodal surface to fix
+        if (mk == MOVE_ONE_GAUSS)
+            return dw.prec == 0 ? sweep_t<double, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                : sweep_t<float, MOVE_ONE_GAUSS>(hs, dw, n, s0, step, tau, maxd, seed, st);
+        if (mk == MOVE_ONE_DRIFT)
+            return dw.prec == 0 ? sweep_t<double, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st)
+                                : sweep_t<float, MOVE_ONE_DRIFT>(hs, dw, n, s0, step, tau, maxd, seed, st);
+        return 7;
+    }
+};
+
+}  // namespace qmc

@@ -11,7 +11,7 @@ namespace qmc {
 // Kernel shapes compiled into the library.  A shape fixes the electron
 // counts and nucleus count at compile time so per-walker arrays live in
 // registers / shared memory with static indices.
-enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_CH4MIN = 3, SHAPE_C6H6 = 4, SHAPE_COUNT = 5 };
+enum Shape { SHAPE_H2 = 0, SHAPE_LI = 1, SHAPE_CH4 = 2, SHAPE_CH4MIN = 3, SHAPE_C6H6 = 4, SHAPE_HEG54 = 5, SHAPE_COUNT = 6 };
 
 // A basis shell: primitives shared by up to two s-type AOs and one p triplet
 // (the SP shells of 6-31G share exponents between 2s and 2p; Li's STO-7G 1s
@@ -48,6 +48,8 @@ struct HostSys {
     std::vector<int> init_nuc;           // caller order
     double init_sigma = 0.5;
     double v_nn = 0.0;
+    double box_L = 0.0;                  // periodic electron gas: box side
+    std::vector<double> kvec;            // periodic electron gas: [n_mo*3] orbital wave vectors
     int version = 0;                     // bumped when parameters or nuclei change
     mutable void* dev_table[2] = {nullptr, nullptr};     // cached device tables (warp kernels)
     mutable int dev_table_version[2] = {-1, -1};
@@ -93,6 +95,9 @@ struct MeasureOut {
 };
 
 int nmax_of_shape(int shape);
+// Scalars per walker in the inverse-matrix block (2 x nmax^2, doubled for
+// complex determinants).
+int dinv_elems_of_shape(int shape);
 // True when the system's shells match the compile-time 9-function CH4 layout.
 bool layout_matches_ch4min(const HostSys& hs);
 

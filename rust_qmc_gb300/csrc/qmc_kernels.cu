@@ -32,6 +32,12 @@ QMC_DECLARE_SHAPE(li)
 QMC_DECLARE_SHAPE(ch4)
 QMC_DECLARE_SHAPE(ch4min)
 QMC_DECLARE_SHAPE(c6h6)
+QMC_DECLARE_SHAPE(heg)
+
+int dinv_elems_of_shape(int shape) {
+    int nm = nmax_of_shape(shape);
+    return 2 * nm * nm * (shape == SHAPE_HEG54 ? 2 : 1);
+}
 
 // The compile-time CH4 layout has no all-electron kernels of its own.
 int shape_step_all_ch4min(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, uint64_t seed,
@@ -58,6 +64,7 @@ bool layout_matches_ch4min(const HostSys& hs) {
         case SHAPE_CH4: return CALL(ch4);              \
         case SHAPE_CH4MIN: return CALL(ch4min);        \
         case SHAPE_C6H6: return CALL(c6h6);            \
+        case SHAPE_HEG54: return CALL(heg);            \
     }                                                  \
     return 7;
 
@@ -325,7 +332,7 @@ int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, i
                                                        src.flags);
     k_branch_scan<<<1, 1024, 0, st>>>(br.counts, src.el, W, br.offsets, br.stats);
     int most = std::min(3 * W, dst.Wcap);
-    int npos = 3 * n_elec, ndinv = 2 * nmax * nmax;
+    int npos = 3 * n_elec, ndinv = nmax;   // caller passes the per-walker inverse-block size
     if (src.prec == 0)
         k_branch_gather<double><<<(most + 127) / 128, 128, 0, st>>>(
             br.offsets, W, br.stats, dst.Wcap, (const double*)src.pos, (const double*)src.dinv, src.logabs,

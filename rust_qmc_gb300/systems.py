@@ -12,6 +12,7 @@ Builders:
                          (65 536-walker single-electron workload)
   * ``benzene_minimal``  planar C6H6, 42 electrons, 36 contracted Gaussians,
                          seeded QR-orthonormal MOs (16 384-walker VMC/DMC workload)
+  * ``electron_gas``     periodic homogeneous electron gas, src/systems/heg.rs
 """
 import ctypes as C
 import math
@@ -116,10 +117,11 @@ class SystemSpec:
     def __init__(self, *, spins, nuc_pos, nuc_charge, basis_kind, ao_nuc, ao_l, ao_m, ao_prims,
                  mo_coef, occ, jastrow_kind, jas_F=1.0, jas=None, nuc_species=None,
                  rot_occ=(), rot_virt=(), rot_angle=(), quirks=0, init_nuc=None, init_sigma=0.5,
-                 name="system"):
+                 box_L=0.0, name="system"):
         self.name = name
         self.spins = np.ascontiguousarray(spins, dtype=np.int32)
         self.nuc_pos = np.ascontiguousarray(nuc_pos, dtype=np.float64).reshape(-1, 3)
+        self.box_L = float(box_L)
         self.nuc_charge = np.ascontiguousarray(nuc_charge, dtype=np.float64)
         n_nuc = len(self.nuc_charge)
         self.nuc_species = np.ascontiguousarray(nuc_species if nuc_species is not None else [0] * n_nuc,
@@ -183,6 +185,8 @@ class SystemSpec:
         return copy.deepcopy(self)
 
     def v_nn(self):
+        if self.box_L > 0:
+            return 0.0
         v = 0.0
         for I in range(self.n_nuc):
             for J in range(I + 1, self.n_nuc):
@@ -210,6 +214,8 @@ class SystemSpec:
         d.ao_nuc, d.ao_l, d.ao_m, d.ao_prim_off = ip(self.ao_nuc), ip(self.ao_l), ip(self.ao_m), ip(self.ao_prim_off)
         d.prim_exp, d.prim_coef = dp(self.prim_exp), dp(self.prim_coef)
         d.prim_pow = ip(self.prim_pow) if self.basis_kind == L.QMC_BASIS_STO else None
+        if not self.prim_exp.size:
+            d.ao_prim_off = None
         d.n_mo = self.mo_coef.shape[0]
         self._mo_flat = np.ascontiguousarray(self.mo_coef.reshape(-1))
         d.mo_coef = dp(self._mo_flat)
@@ -223,7 +229,7 @@ class SystemSpec:
         d.quirks = self.quirks
         d.init_nuc = ip(self.init_nuc)
         d.init_sigma = self.init_sigma
-        d.box_L = 0.0
+        d.box_L = self.box_L
         return d
 
 
@@ -366,3 +372,44 @@ def benzene_minimal(seed=SEED_BASE + 4, b_ee=1.5, b_en=2.0, cc=2.64, ch=2.05):
         nuc_species=[0] * 6 + [1] * 6, basis_kind=L.QMC_BASIS_GTO, ao_nuc=ao_nuc, ao_l=ao_l, ao_m=ao_m,
         ao_prims=prims, mo_coef=Q.T.copy(), occ=list(range(21)) * 2, jastrow_kind=L.QMC_JAS_PADE_EEN,
         jas=jastrow3_params(b_ee, b_en), init_nuc=init, init_sigma=0.5)
+
+
+def heg_k_vectors(n, L):
+    """The n lowest plane waves of a cubic box (src/systems/heg.rs:198-235):
+    integer vectors in [-m, m]^3 generated in nx, ny, nz order and stably
+    sorted by |k|^2, m = ceil(2 n^(1/3)) + 2."""
+    m = int(math.ceil(n ** (1.0 / 3.0) * 2.0)) + 2
+    dk = 2.0 * math.pi / L
+    cand = []
+    for nx in range(-m, m + 1):
+        for ny in range(-m, m + 1):
+            for nz in range(-m, m + 1):
+                cand.append(((nx * dk) ** 2 + (ny * dk) ** 2 + (nz * dk) ** 2, nx, ny, nz))
+    cand.sort(key=lambda t: t[0])        # Python's sort is stable, like Rust's sort_by
+    return np.array([[c[1] * dk, c[2] * dk, c[3] * dk] for c in cand[:n]])
+
+
+HEG_FORMS = {"pade": 0, "rpa": 1, "yukawa": 2}
+
+
+def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, alpha_L=5.0, kmax=8):
+    """Homogeneous electron gas (src/systems/heg.rs:119-170): box
+    L = (4 pi N / 3)^(1/3) r_s, closed-shell plane-wave determinants (N/2 per
+    spin, same k set), Jastrow u = A r/(1 + r/F + 0.2 r^2/F^2) (RPA form) with
+    the reference's amplitudes A_same = 0.5, A_anti = 0.25, minimum image and
+    cutoff at L/2.  With ``reference_quirks`` the Ewald sum and cross term are
+    the reference's; otherwise the one-component-plasma Ewald sum with
+    alpha = alpha_L / L and |n| <= kmax reciprocal vectors."""
+    box = (4.0 * math.pi / 3.0 * n_elec) ** (1.0 / 3.0) * rs
+    nup = n_elec // 2
+    k = heg_k_vectors(nup, box)
+    jas = np.zeros(8)
+    jas[0] = HEG_FORMS[form]
+    jas[2], jas[3] = 0.25, 0.5          # antiparallel, parallel (heg.rs:146-147)
+    jas[4], jas[5] = alpha_L, kmax
+    quirks = (4 | 8) if reference_quirks else 0
+    return SystemSpec(
+        name="HEG-%d" % n_elec, spins=[1] * nup + [-1] * (n_elec - nup), nuc_pos=np.zeros((0, 3)), nuc_charge=[],
+        basis_kind=L.QMC_BASIS_PW, ao_nuc=[], ao_l=[], ao_m=[], ao_prims=[], mo_coef=k,
+        occ=list(range(nup)) + list(range(n_elec - nup)), jastrow_kind=3, jas_F=F, jas=jas, quirks=quirks,
+        init_sigma=-1.0, box_L=box)

@@ -44,7 +44,9 @@ def test_status_strings(qmc_lib):
 
 
 @pytest.mark.parametrize("builder,shape", [(lambda: Q.h2_mo(), 0), (lambda: Q.lithium_atom(), 1),
-                                           (lambda: Q.methane_gto(), 2), (lambda: Q.methane_minimal(), 3)])
+                                           (lambda: Q.methane_gto(), 2), (lambda: Q.methane_minimal(), 3),
+                                           (lambda: Q.benzene_minimal(), 4), (lambda: Q.electron_gas(), 5),
+                                           (lambda: Q.electron_gas(reference_quirks=True), 5)])
 def test_system_check_maps_shapes(qmc_lib, builder, shape):
     spec = builder()
     d = spec.desc()

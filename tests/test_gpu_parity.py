@@ -363,3 +363,54 @@ def test_benzene_fp64_dmc_matches_oracle(ctx, oracle):
     _, pops_o, ens_o, _ = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 13, fixed_node=True)
     assert list(pops) == list(pops_o)
     np.testing.assert_allclose(ens, ens_o, rtol=1e-9, atol=1e-8)
+
+
+# ---------------------------------------------------------------------------
+# Periodic electron gas (complex plane-wave determinants, Ewald)
+# ---------------------------------------------------------------------------
+HEG_BUILDERS = {"heg": lambda: Q.electron_gas(), "heg_ref": lambda: Q.electron_gas(reference_quirks=True)}
+
+
+@pytest.mark.parametrize("name", list(HEG_BUILDERS))
+def test_heg_eval_fp64_matches_oracle(ctx, oracle, name):
+    spec = HEG_BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    cfg = np.random.default_rng(8).uniform(0, spec.box_L, (9, 54, 3))
+    g = sysh.eval_batch(cfg, L.QMC_FP64)
+    o = oracle.evaluate(spec, cfg)
+    assert rel(g["logabs"], o["logabs"]) < 1e-10
+    assert rel(g["grad"], o["grad"]) < 1e-9
+    assert rel(g["lap"], o["lap"]) < 1e-9
+    assert rel(g["e_local"], o["e_local"]) < 1e-10
+
+
+@pytest.mark.parametrize("move", [L.QMC_MOVE_ONE_GAUSS, L.QMC_MOVE_ONE_DRIFT])
+def test_heg_fp64_trajectory_matches_oracle(ctx, oracle, move):
+    spec = Q.electron_gas()
+    sysh = Q.System(ctx, spec)
+    W = 6
+    wk = Q.Walkers(sysh, W, L.QMC_FP64)
+    wk.init(seed=15)
+    wk.refresh()
+    pos0 = wk.get_positions()
+    init = oracle.init_positions(spec, W, seed=15)
+    np.testing.assert_allclose(pos0, init, atol=1e-12)
+    acc = wk.sweep(move, 1, 2, seed=616, step=1.0, tau=0.05, max_drift=1.0)
+    got = wk.get_positions()
+    want, acc_o, _ = oracle.sweeps(spec, pos0, 1, 2, move, 616, step=1.0, tau=0.05, max_drift=1.0, want_energy=False)
+    same = np.all(np.abs(got - want) < 1e-8, axis=(1, 2))
+    assert same.mean() >= 0.8, same.mean()
+    assert abs(acc - acc_o.sum()) <= max(2, int(0.03 * acc_o.sum()))
+
+
+def test_heg_fp32_refresh_energy_within_1e6(ctx, oracle):
+    spec = Q.electron_gas()
+    sysh = Q.System(ctx, spec)
+    wk = Q.Walkers(sysh, 32, L.QMC_FP32_REFINE)
+    wk.init(seed=17)
+    wk.refresh()
+    acc = wk.sweep(L.QMC_MOVE_ONE_GAUSS, 4, 0, seed=18, step=1.0)
+    assert acc > 0
+    _, el = wk.refresh(want_energies=True)
+    o = oracle.evaluate(spec, wk.get_positions())
+    assert np.max(np.abs(el - o["e_local"])) <= 1e-6

@@ -197,3 +197,67 @@ def test_oracle_sweeps_deterministic(oracle):
     b = oracle.sweeps(spec, pos, 3, 0, 2, seed=99, step=0.3, threads=4)
     np.testing.assert_array_equal(a[0], b[0])
     assert a[1].sum() > 0
+
+
+# ---------------------------------------------------------------------------
+# Homogeneous electron gas (src/systems/heg.rs)
+# ---------------------------------------------------------------------------
+def test_heg_box_and_shells():
+    """heg.rs:943-972: L = (4 pi N / 3)^(1/3) r_s; first k = 0, next six at 2 pi / L;
+    27 orbitals per spin close the third shell."""
+    spec = Q.electron_gas(54, 4.0)
+    assert abs(spec.box_L - (4 * math.pi / 3 * 54) ** (1 / 3) * 4.0) < 1e-12
+    kn = np.linalg.norm(spec.mo_coef, axis=1)
+    assert kn[0] == 0.0
+    np.testing.assert_allclose(kn[1:7], 2 * math.pi / spec.box_L, rtol=1e-14)
+    shells = sorted(set(np.round(kn / (2 * math.pi / spec.box_L), 8)))
+    assert shells == [0.0, 1.0, round(math.sqrt(2), 8), round(math.sqrt(3), 8)]
+
+
+def test_heg_madelung_constant(oracle):
+    """One electron in a cubic box with a neutralising background: the Ewald
+    energy is -xi / (2 L) with the simple-cubic Madelung constant
+    xi = 2.837297 (Nijboer & de Wette)."""
+    spec = Q.electron_gas(n_elec=1, rs=3.0)
+    e = oracle.heg_ewald(spec, np.array([[0.3, 1.7, 2.2]]))
+    assert abs(e - (-2.837297479 / (2 * spec.box_L))) < 1e-8
+
+
+@pytest.mark.parametrize("alphaL,kmax", [(4.0, 7), (6.0, 11), (7.0, 13)])
+def test_heg_ewald_alpha_invariance(oracle, alphaL, kmax):
+    """The one-component-plasma Ewald energy does not depend on the splitting
+    parameter to 1e-8 Ha (the 54-electron workload's convergence target)."""
+    spec = Q.electron_gas(54, 4.0)
+    r = np.random.default_rng(3).uniform(0, spec.box_L, (54, 3))
+    assert abs(oracle.heg_ewald(spec, r, 5.0, 8) - oracle.heg_ewald(spec, r, alphaL, kmax)) < 1e-8
+
+
+def test_heg_local_energy_vs_fd(oracle):
+    """Closed-shell Gamma-point determinants have a constant phase, so
+    Re(lap psi / psi) = lap ln|psi| + |grad ln|psi||^2: the analytic gradient
+    and Laplacian match central differences of ln|psi|."""
+    spec = Q.electron_gas(54, 4.0)
+    r = np.random.default_rng(5).uniform(0, spec.box_L, (54, 3))
+    o = oracle.evaluate(spec, r)
+    g, l = fd_grad_lap(oracle, spec, r, h=1e-4)
+    np.testing.assert_allclose(o["grad"][0], g, rtol=1e-6, atol=1e-6 * np.abs(g).max())
+    np.testing.assert_allclose(o["lap"][0], l, rtol=1e-4, atol=1e-4 * np.abs(l).max())
+
+
+def test_heg_reference_quirks_differ(oracle):
+    """The reference's Ewald (alpha = 5/L, |n_i| <= 7, no self or background
+    term, -0.448 N / r_s) and cross term give a different local energy; both
+    stay finite (heg.rs:1009-1030)."""
+    r = np.random.default_rng(6).uniform(0, 24.0, (2, 54, 3))
+    a = oracle.evaluate(Q.electron_gas(54, 4.0), r)["e_local"]
+    b = oracle.evaluate(Q.electron_gas(54, 4.0, reference_quirks=True), r)["e_local"]
+    assert np.all(np.isfinite(a)) and np.all(np.isfinite(b))
+    assert np.all(np.abs(a - b) > 1e-3)
+
+
+def test_heg_jastrow_gradient_antisymmetric(oracle):
+    """heg.rs:1051-1063: two electrons, grad_1 u = -grad_2 u."""
+    spec = Q.electron_gas(54, 4.0)
+    r = np.random.default_rng(7).uniform(0, spec.box_L, (54, 3))
+    o = oracle.evaluate(spec, r)
+    assert np.linalg.norm(o["grad"][0].sum(axis=0)) < 1e-6 * np.abs(o["grad"]).max() * 54

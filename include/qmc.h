@@ -18,8 +18,10 @@
  *  - psi is reported as (log|psi|, sign) instead of the reference's raw psi;
  *    gradients are grad_i psi / psi, Laplacians lap_i psi / psi.
  *  - One context = one CUDA stream; calls on one context are serialised.
- *  - Handles are destroyed children first: walker sets, then systems, then
- *    the context (a parent's destroy invalidates the children's handles).
+ *  - Handles may be destroyed in any order.  Destroying a context that still
+ *    has systems, or a system that still has walker sets, releases the handle
+ *    at once (it accepts no further calls) and frees its memory when its last
+ *    child is destroyed; the children stay fully usable until then.
  *
  * Random numbers: Philox4x32-10 keyed by the 64-bit seed, counter
  *   c0 = walker id, c1 = step (low 32 bits), c2 = electron / sub-index,

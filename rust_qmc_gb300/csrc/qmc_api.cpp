@@ -33,6 +33,8 @@ struct qmc_ctx_s {
     void* flush_buf = nullptr;
     size_t flush_bytes = 0;
     long long launches0 = 0;
+    int n_children = 0;                    // live systems
+    bool released = false;                 // qmc_destroy called while systems were alive
 };
 
 struct qmc_walkers_s;
@@ -42,6 +44,8 @@ struct qmc_sys_s {
     HostSys hs;
     int* d_perm = nullptr;                 // internal -> caller electron index (device)
     qmc_walkers_s* scratch[2] = {nullptr, nullptr};   // batch-evaluation walker sets per precision
+    int n_children = 0;                    // live caller-owned walker sets
+    bool released = false;                 // qmc_system_destroy called while walker sets were alive
 };
 
 struct qmc_walkers_s {
@@ -506,19 +510,47 @@ int qmc_init(int device, qmc_ctx_t* out) {
     return QMC_OK;
 }
 
-int qmc_destroy(qmc_ctx_t c) {
-    if (!c) return QMC_ERR_ARG;
+namespace {
+
+// A handle whose owner releases it while children are alive is only marked; the
+// memory goes when its last child does. Destruction order between handles is then
+// free, as it is for garbage-collected or reference-counted callers.
+void free_ctx(qmc_ctx_s* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (int i = 0; i < 16; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->flush_buf) cudaFree(c->flush_buf);
     cudaStreamDestroy(c->stream);
     delete c;
+}
+
+void free_sys(qmc_sys_s* s) {
+    qmc_ctx_s* c = s->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_walkers(s->scratch[0]);
+    free_walkers(s->scratch[1]);
+    cudaFree(s->d_perm);
+    cudaFree(s->hs.dev_table[0]);
+    cudaFree(s->hs.dev_table[1]);
+    delete s;
+    if (--c->n_children == 0 && c->released) free_ctx(c);
+}
+
+}  // namespace
+
+int qmc_destroy(qmc_ctx_t c) {
+    if (!c || c->released) return QMC_ERR_ARG;
+    if (c->n_children > 0) {
+        c->released = true;
+        return QMC_OK;
+    }
+    free_ctx(c);
     return QMC_OK;
 }
 
 int qmc_system_create(qmc_ctx_t ctx, const qmc_system_desc* desc, qmc_sys_t* out) {
-    if (!ctx || !desc || !out) return QMC_ERR_ARG;
+    if (!ctx || !desc || !out || ctx->released) return QMC_ERR_ARG;
     *out = nullptr;
     qmc_sys_s* s = new (std::nothrow) qmc_sys_s();
     if (!s) return QMC_ERR_NOMEM;
@@ -531,6 +563,7 @@ int qmc_system_create(qmc_ctx_t ctx, const qmc_system_desc* desc, qmc_sys_t* out
         e = cudaMemcpyAsync(s->d_perm, s->hs.perm.data(), sizeof(int) * s->hs.N, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { cudaFree(s->d_perm); delete s; return cuda_rc(e); }
+    ++ctx->n_children;
     *out = s;
     return QMC_OK;
 }
@@ -543,15 +576,12 @@ int qmc_system_check(const qmc_system_desc* desc, int* shape) {
 }
 
 int qmc_system_destroy(qmc_sys_t s) {
-    if (!s) return QMC_ERR_ARG;
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
-    free_walkers(s->scratch[0]);
-    free_walkers(s->scratch[1]);
-    cudaFree(s->d_perm);
-    cudaFree(s->hs.dev_table[0]);
-    cudaFree(s->hs.dev_table[1]);
-    delete s;
+    if (!s || s->released) return QMC_ERR_ARG;
+    if (s->n_children > 0) {
+        s->released = true;
+        return QMC_OK;
+    }
+    free_sys(s);
     return QMC_OK;
 }
 
@@ -694,15 +724,19 @@ int qmc_forces_batch(qmc_sys_t s, int W, const double* pos, double* F_hf, double
 }
 
 int qmc_walkers_create(qmc_sys_t s, int W, int precision, qmc_walkers_t* out) {
-    if (!s || !out) return QMC_ERR_ARG;
+    if (!s || !out || s->released) return QMC_ERR_ARG;
     *out = nullptr;
-    return alloc_walkers(s, W, precision, out);
+    CK(alloc_walkers(s, W, precision, out));
+    ++s->n_children;
+    return QMC_OK;
 }
 
 int qmc_walkers_create_dmc(qmc_sys_t s, int W, int capacity, int precision, qmc_walkers_t* out) {
-    if (!s || !out || capacity < W) return QMC_ERR_ARG;
+    if (!s || !out || s->released || capacity < W) return QMC_ERR_ARG;
     *out = nullptr;
-    return alloc_walkers(s, W, precision, out, capacity);
+    CK(alloc_walkers(s, W, precision, out, capacity));
+    ++s->n_children;
+    return QMC_OK;
 }
 
 int qmc_walkers_count(qmc_walkers_t wk, int* W) {
@@ -721,9 +755,11 @@ int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double m
 
 int qmc_walkers_destroy(qmc_walkers_t wk) {
     if (!wk) return QMC_ERR_ARG;
-    cudaSetDevice(wk->sys->ctx->device);
-    cudaStreamSynchronize(wk->sys->ctx->stream);
+    qmc_sys_s* s = wk->sys;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
     free_walkers(wk);
+    if (--s->n_children == 0 && s->released) free_sys(s);
     return QMC_OK;
 }
 

@@ -165,6 +165,15 @@ struct HLanePos {
         ey = __shfl_sync(0xffffffffu, b, e & 31);
         ez = __shfl_sync(0xffffffffu, c, e & 31);
     }
+    // Same, for an index that differs between lanes: the source lane cannot know which
+    // half the reading lane wants, so both halves travel and the reader selects.
+    __device__ __forceinline__ void get_own(int e, T& ex, T& ey, T& ez) const {
+        const int s = e & 31;
+        T x0 = __shfl_sync(0xffffffffu, x[0], s), x1 = __shfl_sync(0xffffffffu, x[1], s);
+        T y0 = __shfl_sync(0xffffffffu, y[0], s), y1 = __shfl_sync(0xffffffffu, y[1], s);
+        T z0 = __shfl_sync(0xffffffffu, z[0], s), z1 = __shfl_sync(0xffffffffu, z[1], s);
+        ex = e < 32 ? x0 : x1; ey = e < 32 ? y0 : y1; ez = e < 32 ? z0 : z1;
+    }
 };
 
 template <class T>
@@ -508,7 +517,7 @@ __global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restri
             const int i = sig * NUP + lane;
             const bool own = lane < NS;
             TC xi, yi, zi;
-            P.get(min(i, NE - 1), xi, yi, zi);
+            P.get_own(min(i, NE - 1), xi, yi, zi);
             TC gx = 0, gy = 0, gz = 0, lu = 0;
             for (int j = 0; j < NE; ++j) {
                 TC xj, yj, zj;

@@ -214,6 +214,14 @@ struct LanePos {
         T a = e < 32 ? x[0] : x[1], b = e < 32 ? y[0] : y[1], c = e < 32 ? z[0] : z[1];
         ex = wshfl(a, e & 31); ey = wshfl(b, e & 31); ez = wshfl(c, e & 31);
     }
+    // Same, for an index that differs between lanes: the source lane cannot know which
+    // half the reading lane wants, so both halves travel and the reader selects.
+    __device__ __forceinline__ void get_own(int e, T& ex, T& ey, T& ez) const {
+        const int s = e & 31;
+        T x0 = wshfl(x[0], s), x1 = wshfl(x[1], s), y0 = wshfl(y[0], s), y1 = wshfl(y[1], s);
+        T z0 = wshfl(z[0], s), z1 = wshfl(z[1], s);
+        ex = e < 32 ? x0 : x1; ey = e < 32 ? y0 : y1; ez = e < 32 ? z0 : z1;
+    }
 };
 
 // Jastrow change for electron e moving (o -> n), lane-parallel over partner
@@ -532,7 +540,7 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
             const int i = sig * NUP + lane;
             const bool own = lane < NS;
             TC xi, yi, zi;
-            P.get(min(i, NE - 1), xi, yi, zi);
+            P.get_own(min(i, NE - 1), xi, yi, zi);
             TC gx = 0, gy = 0, gz = 0, lu = 0, gsq = 0;
             for (int j = 0; j < NE; ++j) {
                 TC xj, yj, zj;

@@ -414,3 +414,22 @@ def test_heg_fp32_refresh_energy_within_1e6(ctx, oracle):
     _, el = wk.refresh(want_energies=True)
     o = oracle.evaluate(spec, wk.get_positions())
     assert np.max(np.abs(el - o["e_local"])) <= 1e-6
+
+
+def test_handles_release_in_any_order(qmc_lib):
+    """Parent handles destroyed before their children: the walker set keeps
+    working and the deferred release frees everything when it goes."""
+    c2 = Q.Context(0)
+    sysh = Q.System(c2, Q.h2_mo())
+    wk = Q.Walkers(sysh, 64, L.QMC_FP64)
+    wk.init(seed=5)
+    e0 = wk.refresh()
+    assert qmc_lib.qmc_destroy(c2.h) == L.QMC_OK
+    c2.h = None
+    assert qmc_lib.qmc_system_destroy(sysh.h) == L.QMC_OK
+    sysh.h = None
+    wk.sweep(L.QMC_MOVE_ONE_GAUSS, 4, 0, seed=5, step=0.5)
+    e1 = wk.refresh()
+    assert np.isfinite(e0) and np.isfinite(e1) and e1 != e0
+    assert qmc_lib.qmc_walkers_destroy(wk.h) == L.QMC_OK
+    wk.h = None

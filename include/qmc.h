@@ -169,6 +169,7 @@ typedef struct {
 typedef struct qmc_ctx_s* qmc_ctx_t;
 typedef struct qmc_sys_s* qmc_sys_t;
 typedef struct qmc_walkers_s* qmc_walkers_t;
+typedef struct qmc_batch_s* qmc_batch_t;
 
 /* ---- context --------------------------------------------------------------- */
 int qmc_init(int device, qmc_ctx_t* out);
@@ -277,6 +278,42 @@ int qmc_vmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed,
  * E_L in FP64 every refresh_every steps. */
 int qmc_dmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed, qmc_run_result* result,
                 double* energies);
+
+/* ---- uneven batches (no reference counterpart: rust_qmc runs one system
+ * per process, src/main.rs) ---------------------------------------------------
+ * A batch binds walker sets of one context -- any mix of systems, shapes,
+ * precisions and sizes -- and advances them together: one persistent launch
+ * per (shape, precision) class over (system, walker tile) pairs, the class
+ * launches running concurrently inside one CUDA graph per step.
+ * Walker set i of a batch driven with `seed` draws from the Philox key
+ * qmc_batch_system_seed(seed, i) (SplitMix64 of seed + (i+1) * 0x9E3779B97F4A7C15),
+ * so a batched sweep of set i equals qmc_walkers_sweep of that set with that
+ * key.  A walker set may belong to several batches (not at the same time on
+ * different streams); destroying it while bound defers its release until the
+ * last batch binding it is destroyed. */
+uint64_t qmc_batch_system_seed(uint64_t seed, int i);
+/* Binds n distinct walker sets of ctx (n >= 1). */
+int qmc_batch_create(qmc_ctx_t ctx, int n, const qmc_walkers_t* walkers, qmc_batch_t* out);
+int qmc_batch_destroy(qmc_batch_t batch);
+/* n_sweeps single-electron sweeps (QMC_MOVE_ONE_GAUSS / QMC_MOVE_ONE_DRIFT) of
+ * every walker set, sweep counters step0 .. step0 + n_sweeps - 1. */
+int qmc_batch_sweep(qmc_batch_t batch, int move_kind, int n_sweeps, uint64_t step0, double step, double tau,
+                    double max_drift, uint64_t seed);
+/* FP64 refresh of every walker set (inverse, log|psi|, E_L) and the mean E_L
+ * of each set, e_mean[n] (may be NULL). */
+int qmc_batch_refresh(qmc_batch_t batch, double* e_mean);
+/* n_steps graph-captured steps: sweeps_per_step sweeps, then the FP64
+ * refresh; e_series[n_steps][n] (may be NULL) receives the per-step mean E_L
+ * of every set.  Step k sweeps with counters step0 + k * sweeps_per_step + j. */
+int qmc_batch_run_steps(qmc_batch_t batch, int move_kind, int n_steps, int sweeps_per_step, uint64_t step0,
+                        double step, double tau, double max_drift, uint64_t seed, double* e_series);
+/* VMC of n_sys systems in one batch (W[i] walkers each, params->n_walkers
+ * ignored; single-electron moves): system i follows exactly the schedule of
+ * qmc_vmc_run(systems[i], params, qmc_batch_system_seed(seed, i)) and
+ * per_sys[i] holds its result.  energies (may be NULL) receives
+ * [ceil(n_steps / refresh_every)][n_sys] per-measurement means. */
+int qmc_batch_run(qmc_ctx_t ctx, int n_sys, const qmc_sys_t* systems, const int* W, const qmc_run_params* params,
+                  uint64_t seed, qmc_run_result* per_sys, double* energies);
 
 /* ---- timing helpers (no reference counterpart; used by the benchmark) ---- */
 /* Records CUDA event `slot` (0..15) on the context's stream. */

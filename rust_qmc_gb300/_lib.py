@@ -107,8 +107,15 @@ PROTOTYPES = {
     "qmc_host_alloc": [C.c_size_t, C.POINTER(_vp)],
     "qmc_host_free": [_vp],
     "qmc_sr_sums_noalloc": [_dp, _dp, C.c_int, C.c_int, _dp, _vp],
+    "qmc_batch_system_seed": [_u64, C.c_int],
+    "qmc_batch_create": [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)],
+    "qmc_batch_destroy": [_vp],
+    "qmc_batch_sweep": [_vp, C.c_int, C.c_int, _u64, C.c_double, C.c_double, C.c_double, _u64],
+    "qmc_batch_refresh": [_vp, _dp],
+    "qmc_batch_run_steps": [_vp, C.c_int, C.c_int, C.c_int, _u64, C.c_double, C.c_double, C.c_double, _u64, _dp],
+    "qmc_batch_run": [_vp, C.c_int, C.POINTER(_vp), _ip, C.POINTER(RunParams), _u64, C.POINTER(RunResult), _dp],
 }
-_RESTYPES = {"qmc_status_string": C.c_char_p}
+_RESTYPES = {"qmc_status_string": C.c_char_p, "qmc_batch_system_seed": _u64}
 
 _lib = None
 _load_error = None

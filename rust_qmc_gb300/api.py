@@ -310,6 +310,74 @@ class Walkers:
         return f.value
 
 
+class Batch:
+    """Walker sets of one context advanced together (qmc_batch_*): one
+    persistent launch per shape class, one CUDA graph per step."""
+
+    def __init__(self, ctx, walkers):
+        self.ctx, self.lib, self.walkers = ctx, ctx.lib, list(walkers)
+        arr = (C.c_void_p * len(self.walkers))(*[w.h.value for w in self.walkers])
+        h = C.c_void_p()
+        L.check(self.lib.qmc_batch_create(ctx.h, len(self.walkers), arr, C.byref(h)), "qmc_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qmc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def system_seed(self, seed, i):
+        return int(self.lib.qmc_batch_system_seed(seed, i))
+
+    def sweep(self, move_kind, n_sweeps, step0, seed, step=0.3, tau=0.01, max_drift=1.0):
+        L.check(self.lib.qmc_batch_sweep(self.h, move_kind, n_sweeps, step0, step, tau, max_drift, seed),
+                "qmc_batch_sweep")
+
+    def refresh(self):
+        e = np.zeros(len(self.walkers))
+        L.check(self.lib.qmc_batch_refresh(self.h, _d(e)), "qmc_batch_refresh")
+        return e
+
+    def run_steps(self, move_kind, n_steps, sweeps_per_step, step0, seed, step=0.3, tau=0.01, max_drift=1.0):
+        e = np.zeros((n_steps, len(self.walkers)))
+        L.check(self.lib.qmc_batch_run_steps(self.h, move_kind, n_steps, sweeps_per_step, step0, step, tau,
+                                             max_drift, seed, _d(e)), "qmc_batch_run_steps")
+        return e
+
+
+def batch_system_seed(seed, i):
+    return int(L.load_library().qmc_batch_system_seed(seed, i))
+
+
+def batch_run(ctx, systems, walkers_per_system, *, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ONE_GAUSS, step=0.3,
+              tau=0.01, max_drift=1.0, precision=L.QMC_FP32_REFINE, refresh_every=64, seed=1):
+    """VMC of many systems in one batch (qmc_batch_run); one result dict per system."""
+    n = len(systems)
+    p = L.RunParams()
+    p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = 0, n_steps, n_burnin, move_kind
+    p.step, p.tau, p.max_drift, p.precision, p.refresh_every = step, tau, max_drift, precision, refresh_every
+    res = (L.RunResult * n)()
+    W = np.ascontiguousarray(walkers_per_system, dtype=np.int32)
+    every = refresh_every if refresh_every > 0 else 1
+    rows = (n_steps + every - 1) // every
+    energies = np.zeros((rows, n))
+    hs = (C.c_void_p * n)(*[s.h.value for s in systems])
+    L.check(ctx.lib.qmc_batch_run(ctx.h, n, hs, _i(W), C.byref(p), seed, res, _d(energies)), "qmc_batch_run")
+    out = []
+    for i in range(n):
+        r = res[i]
+        out.append(dict(energy=r.energy, error=r.error, autocorrelation_time=r.autocorrelation_time,
+                        acceptance_rate=r.acceptance_rate, variance=r.variance, n_samples=r.n_samples,
+                        status_flags=r.status_flags, energies=energies[:, i].copy()))
+    return out
+
+
 def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0, tau=0.01,
             max_drift=1.0, precision=L.QMC_FP64, refresh_every=64, seed=1):
     """MCMCSimulation::run / DriftDiffusionVMC::run on the device."""

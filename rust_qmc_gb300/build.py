@@ -20,7 +20,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--use_fast_math", "-Xcompiler",
 CU_SOURCES = ["qmc_kernels.cu", "qmc_shape_h2.cu", "qmc_shape_li.cu", "qmc_shape_ch4_measure.cu",
               "qmc_shape_ch4_sweep.cu", "qmc_shape_ch4_allstep.cu", "qmc_shape_ch4min_measure.cu",
               "qmc_shape_ch4min_sweep.cu", "qmc_shape_c6h6.cu", "qmc_shape_heg.cu",
-              "qmc_noalloc.cu"]
+              "qmc_shape_ch4_batch.cu", "qmc_shape_ch4min_batch.cu", "qmc_shape_c6h6_batch.cu",
+              "qmc_shape_heg_batch.cu", "qmc_noalloc.cu"]
 CPP_SOURCES = ["qmc_api.cpp"]
 
 

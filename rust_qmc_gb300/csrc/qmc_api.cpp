@@ -57,6 +57,8 @@ struct qmc_walkers_s {
     double* d_out = nullptr;               // generic device output scratch
     size_t d_out_cap = 0;
     unsigned long long acc_host = 0;
+    int n_batches = 0;                     // live batches that bind this walker set
+    bool released = false;                 // qmc_walkers_destroy called while bound
 };
 
 namespace {
@@ -753,13 +755,23 @@ int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double m
     return dmc_step(wk, tau, tau_move, max_drift, fixed_node, e_ref, seed, step, fp64_measure, n_new, e_mean);
 }
 
-int qmc_walkers_destroy(qmc_walkers_t wk) {
-    if (!wk) return QMC_ERR_ARG;
+namespace {
+void release_walkers(qmc_walkers_s* wk) {
     qmc_sys_s* s = wk->sys;
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     free_walkers(wk);
     if (--s->n_children == 0 && s->released) free_sys(s);
+}
+}  // namespace
+
+int qmc_walkers_destroy(qmc_walkers_t wk) {
+    if (!wk || wk->released) return QMC_ERR_ARG;
+    if (wk->n_batches > 0) {
+        wk->released = true;               // freed when the last batch binding it is destroyed
+        return QMC_OK;
+    }
+    release_walkers(wk);
     return QMC_OK;
 }
 
@@ -1061,3 +1073,400 @@ int qmc_host_free(void* p) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Uneven batches: many systems advanced together.  Walker sets are grouped
+// into classes by (shape, precision); each class is one persistent launch over
+// its (system, walker tile) list.  A step (sweeps + FP64 refresh + per-system
+// mean E_L + step-counter advance) is captured once into a CUDA graph whose
+// class branches run concurrently; the per-call scalars live in a device
+// control block, so the same graph replays for every step and every call.
+// ---------------------------------------------------------------------------
+struct qmc_batch_s {
+    struct Cls {
+        BatchClass bc;
+        std::vector<int> members;          // batch indices, in batch order
+        std::vector<BatchRec> recs;
+        BatchTile* d_tiles = nullptr;
+        BatchRec* d_recs = nullptr;
+        int* d_tile_begin = nullptr;
+        double* d_partial = nullptr;
+        int grid_sweep[2] = {0, 0};        // per single-electron move kind
+        int grid_measure = 0;
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    qmc_ctx_s* ctx = nullptr;
+    std::vector<qmc_walkers_s*> wk;
+    std::vector<int> versions;             // HostSys::version at the last table upload
+    std::vector<Cls> cls;
+    BatchCtl* d_ctl = nullptr;
+    double* d_series = nullptr;            // [series_rows][n]
+    int series_rows = 0;
+    cudaEvent_t fork = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool owns_walkers = false;             // created by qmc_batch_run
+};
+
+namespace {
+
+constexpr int kBatchSeriesRows = 1024;
+
+void batch_free(qmc_batch_s* b) {
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    for (auto& g : b->graph) if (g) cudaGraphExecDestroy(g);
+    for (auto& c : b->cls) {
+        if (c.stream) { cudaStreamSynchronize(c.stream); cudaStreamDestroy(c.stream); }
+        if (c.done) cudaEventDestroy(c.done);
+        cudaFree(c.d_tiles); cudaFree(c.d_recs); cudaFree(c.d_tile_begin); cudaFree(c.d_partial);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    cudaFree(b->d_ctl);
+    cudaFree(b->d_series);
+    for (qmc_walkers_s* w : b->wk) {
+        if (b->owns_walkers) { free_walkers(w); continue; }
+        if (--w->n_batches == 0 && w->released) release_walkers(w);
+    }
+    delete b;
+}
+
+// Upload (again) the system tables of every member whose parameters changed.
+int batch_sync_tables(qmc_batch_s* b) {
+    for (auto& c : b->cls) {
+        bool dirty = false;
+        for (size_t r = 0; r < c.members.size(); ++r) {
+            const int i = c.members[r];
+            const HostSys& hs = b->wk[i]->sys->hs;
+            if (b->versions[i] == hs.version && c.recs[r].tab_d) continue;
+            CK(batch_tables(hs, c.bc.prec, c.recs[r]));
+            b->versions[i] = hs.version;
+            dirty = true;
+        }
+        if (dirty) CU(cudaMemcpy(c.d_recs, c.recs.data(), sizeof(BatchRec) * c.recs.size(), cudaMemcpyHostToDevice));
+    }
+    return QMC_OK;
+}
+
+int batch_build(qmc_ctx_s* ctx, const std::vector<qmc_walkers_s*>& wk, bool owns, qmc_batch_s** out) {
+    qmc_batch_s* b = new (std::nothrow) qmc_batch_s();
+    if (!b) return QMC_ERR_NOMEM;
+    b->ctx = ctx;
+    b->wk = wk;
+    b->owns_walkers = owns;
+    b->versions.assign(wk.size(), -1);
+    if (!owns) for (qmc_walkers_s* w : wk) ++w->n_batches;
+    // on failure the caller keeps the walker sets it passed in
+    struct Guard {
+        qmc_batch_s* b;
+        ~Guard() {
+            if (!b) return;
+            if (b->owns_walkers) b->wk.clear();
+            batch_free(b);
+        }
+    } guard{b};
+    int nsm = 0;
+    CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    std::map<std::pair<int, int>, int> index;
+    for (size_t i = 0; i < wk.size(); ++i) {
+        auto key = std::make_pair(wk[i]->sys->hs.shape, wk[i]->dw.prec);
+        auto it = index.find(key);
+        if (it == index.end()) {
+            it = index.emplace(key, (int)b->cls.size()).first;
+            b->cls.emplace_back();
+            b->cls.back().bc.shape = key.first;
+            b->cls.back().bc.prec = key.second;
+        }
+        b->cls[it->second].members.push_back((int)i);
+    }
+    for (auto& c : b->cls) {
+        const int width = batch_tile_width(c.bc.shape);
+        if (width <= 0) return QMC_ERR_UNSUPPORTED;
+        std::vector<BatchTile> tiles;
+        std::vector<int> begin;
+        for (size_t r = 0; r < c.members.size(); ++r) {
+            qmc_walkers_s* w = wk[c.members[r]];
+            BatchRec rec;
+            rec.pos = w->dw.pos;
+            rec.dinv = w->dw.dinv;
+            rec.sign = w->dw.sign;
+            rec.logabs = w->dw.logabs;
+            rec.el = w->dw.el;
+            rec.acc = w->dw.acc;
+            rec.flags = w->dw.flags;
+            rec.W = w->dw.W;
+            rec.Wcap = w->dw.Wcap;
+            rec.index = c.members[r];
+            rec.fixed_node = w->dw.fixed_node;
+            c.recs.push_back(rec);
+            begin.push_back((int)tiles.size());
+            for (int w0 = 0; w0 < rec.W; w0 += width) tiles.push_back(BatchTile{(int)r, w0});
+        }
+        begin.push_back((int)tiles.size());
+        c.bc.ntiles = (int)tiles.size();
+        c.bc.nrec = (int)c.recs.size();
+        CU(cudaMalloc((void**)&c.d_tiles, sizeof(BatchTile) * std::max<size_t>(1, tiles.size())));
+        CU(cudaMalloc((void**)&c.d_recs, sizeof(BatchRec) * c.recs.size()));
+        CU(cudaMalloc((void**)&c.d_tile_begin, sizeof(int) * begin.size()));
+        CU(cudaMalloc((void**)&c.d_partial, 16 * std::max<size_t>(1, tiles.size())));
+        if (!tiles.empty())
+            CU(cudaMemcpy(c.d_tiles, tiles.data(), sizeof(BatchTile) * tiles.size(), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(c.d_tile_begin, begin.data(), sizeof(int) * begin.size(), cudaMemcpyHostToDevice));
+        c.bc.tiles = c.d_tiles;
+        c.bc.recs = c.d_recs;
+        c.bc.tile_begin = c.d_tile_begin;
+        c.bc.tile_partial = c.d_partial;
+        // persistent grids: every resident block slot of the GPU (occupancy x SMs)
+        for (int m = 0; m < 2; ++m) {
+            int occ = batch_occupancy(c.bc.shape, c.bc.prec, QMC_MOVE_ONE_GAUSS + m, false);
+            if (occ < 0) return -occ;
+            c.grid_sweep[m] = std::max(1, occ) * nsm;
+        }
+        int occ = batch_occupancy(c.bc.shape, c.bc.prec, 0, true);
+        if (occ < 0) return -occ;
+        c.grid_measure = std::max(1, occ) * nsm;
+        c.bc.grid_measure = c.grid_measure;
+        CU(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    }
+    CU(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    CU(cudaMalloc((void**)&b->d_ctl, sizeof(BatchCtl)));
+    b->series_rows = kBatchSeriesRows;
+    CU(cudaMalloc((void**)&b->d_series, 8 * (size_t)b->series_rows * wk.size()));
+    CK(batch_sync_tables(b));
+    guard.b = nullptr;
+    *out = b;
+    return QMC_OK;
+}
+
+int batch_check_move(const qmc_batch_s* b, int mk) {
+    if (mk != QMC_MOVE_ONE_GAUSS && mk != QMC_MOVE_ONE_DRIFT) return QMC_ERR_ARG;
+    for (const auto& c : b->cls)
+        if (c.bc.shape == SHAPE_HEG54)
+            for (const auto& r : c.recs) if (r.fixed_node) return QMC_ERR_UNSUPPORTED;
+    return QMC_OK;
+}
+
+int batch_upload_ctl(qmc_batch_s* b, const BatchCtl& h) {
+    CU(cudaMemcpyAsync(b->d_ctl, &h, sizeof(BatchCtl), cudaMemcpyHostToDevice, b->ctx->stream));
+    // pageable source: wait so that `h` may go out of scope
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    return QMC_OK;
+}
+
+// One step on the context stream, class after class (eager form).
+int batch_sweep_eager(qmc_batch_s* b, int mk) {
+    for (auto& c : b->cls) {
+        c.bc.grid_sweep = c.grid_sweep[mk - QMC_MOVE_ONE_GAUSS];
+        CK(launch_batch_sweep(c.bc, mk, b->d_ctl, b->ctx->stream));
+    }
+    return QMC_OK;
+}
+
+int batch_measure_eager(qmc_batch_s* b) {
+    for (auto& c : b->cls) {
+        CK(launch_batch_measure(c.bc, b->ctx->stream));
+        CK(launch_batch_energy(c.bc, b->d_ctl, b->d_series, (int)b->wk.size(), b->ctx->stream));
+    }
+    return QMC_OK;
+}
+
+// Capture one step: fork to the class streams, sweep + measure + energy per
+// class, join, advance the control block.
+int batch_capture(qmc_batch_s* b, int mk, cudaGraphExec_t* out) {
+    cudaStream_t st = b->ctx->stream;
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = cuda_rc(cudaEventRecord(b->fork, st));
+    for (auto& c : b->cls) {
+        if (rc) break;
+        rc = cuda_rc(cudaStreamWaitEvent(c.stream, b->fork, 0));
+        c.bc.grid_sweep = c.grid_sweep[mk - QMC_MOVE_ONE_GAUSS];
+        if (!rc) rc = launch_batch_sweep(c.bc, mk, b->d_ctl, c.stream);
+        if (!rc) rc = launch_batch_measure(c.bc, c.stream);
+        if (!rc) rc = launch_batch_energy(c.bc, b->d_ctl, b->d_series, (int)b->wk.size(), c.stream);
+        if (!rc) rc = cuda_rc(cudaEventRecord(c.done, c.stream));
+        if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, c.done, 0));
+    }
+    if (!rc) rc = launch_batch_advance(b->d_ctl, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (!rc && e != cudaSuccess) rc = cuda_rc(e);
+    if (!rc) rc = cuda_rc(cudaGraphInstantiate(out, g, 0));
+    if (g) cudaGraphDestroy(g);
+    return rc;
+}
+
+// n_steps graph steps of `sweeps` sweeps each, starting at sweep counter
+// step0; series rows (n_steps x n) copied to `series` when given.
+int batch_steps(qmc_batch_s* b, int mk, int n_steps, int sweeps, uint64_t step0, double step, double tau,
+                double max_drift, uint64_t seed, double* series) {
+    CK(batch_check_move(b, mk));
+    CK(batch_sync_tables(b));
+    cudaGraphExec_t& g = b->graph[mk - QMC_MOVE_ONE_GAUSS];
+    if (!g) CK(batch_capture(b, mk, &g));
+    cudaStream_t st = b->ctx->stream;
+    const size_t n = b->wk.size();
+    for (int done = 0; done < n_steps; done += b->series_rows) {
+        const int rows = std::min(b->series_rows, n_steps - done);
+        BatchCtl h;
+        h.step = step0 + (uint64_t)done * (uint64_t)sweeps;
+        h.seed = seed;
+        h.step_size = step;
+        h.tau = tau;
+        h.max_drift = max_drift;
+        h.n_sweeps = sweeps;
+        h.row = 0;
+        CK(batch_upload_ctl(b, h));
+        for (int r = 0; r < rows; ++r) CU(cudaGraphLaunch(g, st));
+        if (series)
+            CU(cudaMemcpyAsync(series + (size_t)done * n, b->d_series, 8 * (size_t)rows * n, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+    }
+    return QMC_OK;
+}
+
+}  // namespace
+
+uint64_t qmc_batch_system_seed(uint64_t seed, int s) { return batch_system_seed(seed, s); }
+
+int qmc_batch_create(qmc_ctx_t ctx, int n, const qmc_walkers_t* walkers, qmc_batch_t* out) {
+    if (!ctx || ctx->released || n <= 0 || !walkers || !out) return QMC_ERR_ARG;
+    *out = nullptr;
+    std::vector<qmc_walkers_s*> wk(walkers, walkers + n);
+    for (int i = 0; i < n; ++i) {
+        if (!wk[i] || wk[i]->released || wk[i]->sys->ctx != ctx || wk[i]->dw.W <= 0) return QMC_ERR_ARG;
+        for (int j = 0; j < i; ++j) if (wk[j] == wk[i]) return QMC_ERR_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    return batch_build(ctx, wk, false, out);
+}
+
+int qmc_batch_destroy(qmc_batch_t b) {
+    if (!b) return QMC_ERR_ARG;
+    batch_free(b);
+    return QMC_OK;
+}
+
+int qmc_batch_sweep(qmc_batch_t b, int move_kind, int n_sweeps, uint64_t step0, double step, double tau,
+                    double max_drift, uint64_t seed) {
+    if (!b || n_sweeps < 0) return QMC_ERR_ARG;
+    if (move_kind == QMC_MOVE_ONE_DRIFT && !(tau > 0 && max_drift > 0)) return QMC_ERR_ARG;
+    if (move_kind == QMC_MOVE_ONE_GAUSS && !(step > 0)) return QMC_ERR_ARG;
+    CK(batch_check_move(b, move_kind));
+    if (n_sweeps == 0) return QMC_OK;
+    cudaSetDevice(b->ctx->device);
+    CK(batch_sync_tables(b));
+    BatchCtl h;
+    h.step = step0;
+    h.seed = seed;
+    h.step_size = step;
+    h.tau = tau;
+    h.max_drift = max_drift;
+    h.n_sweeps = n_sweeps;
+    CK(batch_upload_ctl(b, h));
+    CK(batch_sweep_eager(b, move_kind));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    return QMC_OK;
+}
+
+int qmc_batch_refresh(qmc_batch_t b, double* e_mean) {
+    if (!b) return QMC_ERR_ARG;
+    cudaSetDevice(b->ctx->device);
+    CK(batch_sync_tables(b));
+    BatchCtl h;                            // row 0
+    CK(batch_upload_ctl(b, h));
+    CK(batch_measure_eager(b));
+    if (e_mean)
+        CU(cudaMemcpyAsync(e_mean, b->d_series, 8 * b->wk.size(), cudaMemcpyDeviceToHost, b->ctx->stream));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    return QMC_OK;
+}
+
+int qmc_batch_run_steps(qmc_batch_t b, int move_kind, int n_steps, int sweeps_per_step, uint64_t step0, double step,
+                        double tau, double max_drift, uint64_t seed, double* e_series) {
+    if (!b || n_steps < 0 || sweeps_per_step <= 0) return QMC_ERR_ARG;
+    if (move_kind == QMC_MOVE_ONE_DRIFT && !(tau > 0 && max_drift > 0)) return QMC_ERR_ARG;
+    if (move_kind == QMC_MOVE_ONE_GAUSS && !(step > 0)) return QMC_ERR_ARG;
+    if (n_steps == 0) return QMC_OK;
+    cudaSetDevice(b->ctx->device);
+    return batch_steps(b, move_kind, n_steps, sweeps_per_step, step0, step, tau, max_drift, seed, e_series);
+}
+
+int qmc_batch_run(qmc_ctx_t ctx, int n_sys, const qmc_sys_t* systems, const int* W, const qmc_run_params* p,
+                  uint64_t seed, qmc_run_result* per_sys, double* energies) {
+    if (!ctx || ctx->released || n_sys <= 0 || !systems || !W || !p || !per_sys) return QMC_ERR_ARG;
+    if (p->n_steps <= 0 || p->n_burnin < 0) return QMC_ERR_ARG;
+    if (p->move_kind != QMC_MOVE_ONE_GAUSS && p->move_kind != QMC_MOVE_ONE_DRIFT) return QMC_ERR_ARG;
+    if (p->move_kind == QMC_MOVE_ONE_DRIFT && !(p->tau > 0 && p->max_drift > 0)) return QMC_ERR_ARG;
+    if (p->move_kind == QMC_MOVE_ONE_GAUSS && !(p->step > 0)) return QMC_ERR_ARG;
+    if (p->precision != QMC_FP64 && p->precision != QMC_FP32_REFINE) return QMC_ERR_ARG;
+    for (int i = 0; i < n_sys; ++i)
+        if (!systems[i] || systems[i]->released || systems[i]->ctx != ctx || W[i] <= 0) return QMC_ERR_ARG;
+    std::memset(per_sys, 0, sizeof(qmc_run_result) * n_sys);
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    std::vector<qmc_walkers_s*> wk;
+    struct WGuard {
+        std::vector<qmc_walkers_s*>* v;
+        ~WGuard() { if (v) for (auto* w : *v) { cudaStreamSynchronize(w->sys->ctx->stream); free_walkers(w); } }
+    } wguard{&wk};
+    for (int i = 0; i < n_sys; ++i) {
+        qmc_walkers_s* w = nullptr;
+        CK(alloc_walkers(systems[i], W[i], p->precision, &w));
+        wk.push_back(w);
+    }
+    // the same start as qmc_vmc_run of each system with its batch seed
+    MeasureOut none;
+    for (int i = 0; i < n_sys; ++i) {
+        CK(launch_init(systems[i]->hs, wk[i]->dw, batch_system_seed(seed, i), st));
+        CK(launch_measure(systems[i]->hs, wk[i]->dw, 0, true, none, st));
+    }
+    qmc_batch_s* b = nullptr;
+    CK(batch_build(ctx, wk, true, &b));
+    wguard.v = nullptr;                    // the batch frees the walker sets
+    struct BGuard { qmc_batch_s* b; ~BGuard() { batch_free(b); } } bguard{b};
+    const int every = p->refresh_every > 0 ? p->refresh_every : 1;
+    const int mk = p->move_kind;
+    // burn-in: full steps, then the remainder
+    const int nb_full = p->n_burnin / every, nb_rem = p->n_burnin % every;
+    uint64_t sweep = 0;
+    if (nb_full) CK(batch_steps(b, mk, nb_full, every, sweep, p->step, p->tau, p->max_drift, seed, nullptr));
+    sweep += (uint64_t)nb_full * every;
+    if (nb_rem) CK(batch_steps(b, mk, 1, nb_rem, sweep, p->step, p->tau, p->max_drift, seed, nullptr));
+    sweep += (uint64_t)nb_rem;
+    for (qmc_walkers_s* w : wk) CU(cudaMemsetAsync(w->dw.acc, 0, 8, st));
+    const int ns_full = p->n_steps / every, ns_rem = p->n_steps % every;
+    const int rows = ns_full + (ns_rem ? 1 : 0);
+    std::vector<double> series((size_t)rows * n_sys);
+    if (ns_full) CK(batch_steps(b, mk, ns_full, every, sweep, p->step, p->tau, p->max_drift, seed, series.data()));
+    sweep += (uint64_t)ns_full * every;
+    if (ns_rem)
+        CK(batch_steps(b, mk, 1, ns_rem, sweep, p->step, p->tau, p->max_drift, seed,
+                       series.data() + (size_t)ns_full * n_sys));
+    for (int i = 0; i < n_sys; ++i) {
+        unsigned long long acc = 0;
+        int flags = 0;
+        CU(cudaMemcpyAsync(&acc, wk[i]->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(&flags, wk[i]->dw.flags, 4, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        std::vector<double> e(rows);
+        for (int r = 0; r < rows; ++r) e[r] = series[(size_t)r * n_sys + i];
+        double mean = 0.0;
+        for (double v : e) mean += v;
+        mean /= (double)rows;
+        double var = 0.0;
+        for (double v : e) var += (v - mean) * (v - mean);
+        qmc_run_result& res = per_sys[i];
+        res.energy = mean;
+        res.variance = var / (double)rows;
+        res.autocorrelation_time = autocorrelation_time(e);
+        res.error = blocking_error(e, res.autocorrelation_time);
+        const double proposals = (double)p->n_steps * systems[i]->hs.N * W[i];
+        res.acceptance_rate = (double)acc / proposals;
+        res.n_samples = rows;
+        res.status_flags = flags;
+    }
+    if (energies) std::memcpy(energies, series.data(), sizeof(double) * series.size());
+    return QMC_OK;
+}

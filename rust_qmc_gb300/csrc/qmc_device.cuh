@@ -412,4 +412,21 @@ __device__ __forceinline__ Comp comp_add(Comp a, Comp b) {
     return {s, a.c + b.c + e};
 }
 
+// Persistent batched launches: block b owns the contiguous run of tiles
+// [t0, t1) of the class's tile list, so consecutive tiles mostly share a
+// system and its table is staged once per run.
+__device__ __forceinline__ void batch_tile_range(int ntiles, int& t0, int& t1) {
+    t0 = (int)(((long long)ntiles * blockIdx.x) / gridDim.x);
+    t1 = (int)(((long long)ntiles * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// Whole-block copy of a system table into shared memory (no barrier).
+template <class TAB>
+__device__ __forceinline__ void stage_table(TAB* dst, const void* src) {
+    static_assert(sizeof(TAB) % 4 == 0, "table size must be a multiple of 4 bytes");
+    const int* s = static_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(TAB) / 4); i += blockDim.x) d[i] = __ldg(s + i);
+}
+
 }  // namespace qmc

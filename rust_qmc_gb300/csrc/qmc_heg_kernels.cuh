@@ -229,18 +229,13 @@ __global__ void khw_init(const SysH<double>* __restrict__ S, TS* __restrict__ po
 }
 
 // Single-electron sweeps, one warp per walker.
-template <int NE, int NUP, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
-                                                      T* __restrict__ gdinv, int W, int Wcap, int n_sweeps,
-                                                      uint64_t step0, T step, T tau, T maxd, uint64_t seed,
-                                                      unsigned long long* acc_out, int* flags) {
+template <int NE, int NUP, class T, int MOVE>
+__device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict__ gpos, T* __restrict__ gdinv,
+                                                 int w, int Wcap, int n_sweeps, uint64_t step0, T step, T tau,
+                                                 T maxd, uint64_t seed, unsigned long long* acc_out, int* flags) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
-    __shared__ SysH<T> S;
-    load_sysh(&S, Sg, (int)sizeof(SysH<T>));
     const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
-    if (w >= W) return;
     HLanePos<T, NE> P;
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
@@ -387,26 +382,57 @@ __global__ void __launch_bounds__(32 * WPB) khw_sweep(const SysH<T>* __restrict_
     }
 }
 
+template <int NE, int NUP, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
+                                                      T* __restrict__ gdinv, int W, int Wcap, int n_sweeps,
+                                                      uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+                                                      unsigned long long* acc_out, int* flags) {
+    __shared__ SysH<T> S;
+    load_sysh(&S, Sg, (int)sizeof(SysH<T>));
+    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
+    if (w >= W) return;
+    khw_sweep_walker<NE, NUP, T, MOVE>(S, gpos, gdinv, w, Wcap, n_sweeps, step0, step, tau, maxd, seed, acc_out,
+                                       flags);
+}
+
+// Batched form: persistent blocks over (system, WPB-walker tile) pairs.
+template <int NE, int NUP, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+                                                       const BatchRec* __restrict__ recs,
+                                                       const BatchCtl* __restrict__ ctl) {
+    __shared__ SysH<T> S;
+    const BatchCtl c = *ctl;
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            __syncthreads();
+            load_sysh(&S, static_cast<const SysH<T>*>(recs[tl.rec].tab_s), (int)sizeof(SysH<T>));
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)(threadIdx.x >> 5);
+        if (w < R.W)
+            khw_sweep_walker<NE, NUP, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, w, R.Wcap, c.n_sweeps, c.step,
+                                               (T)c.step_size, (T)c.tau, (T)c.max_drift,
+                                               batch_system_seed(c.seed, R.index), R.acc, R.flags);
+    }
+}
+
 // FP64 (or FP32) full evaluation: complex Gauss-Jordan, kinetic terms, Ewald.
-template <int NE, int NUP, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
-                                                        const TS* __restrict__ gpos,
-                                                        TS* __restrict__ gdinv, double* __restrict__ glog,
-                                                        int* __restrict__ gsign, double* __restrict__ gel, int W,
-                                                        int Wcap, int write_state, double* __restrict__ out_grad,
-                                                        double* __restrict__ out_lap, double* partial, int* flags) {
+template <int NE, int NUP, class TC, class TS>
+__device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KTable* __restrict__ KT, TC* Mr,
+                                                     const TS* __restrict__ gpos, TS* __restrict__ gdinv,
+                                                     double* __restrict__ glog, int* __restrict__ gsign,
+                                                     double* __restrict__ gel, int w, bool act, int Wcap,
+                                                     int write_state, double* __restrict__ out_grad,
+                                                     double* __restrict__ out_lap, int* flags) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
-    extern __shared__ __align__(16) unsigned char hsm[];
-    SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
-    TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
-    load_sysh(&S, Sg, (int)sizeof(SysH<TC>));
     const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int w = blockIdx.x * WPB + wib;
-    const bool act = w < W;
-    TC* Mr = rows + (size_t)wib * 2 * NM * 32;        // [re|im][row][lane]
-    TC* Mi = Mr + NM * 32;
+    TC* Mi = Mr + NM * 32;                            // Mr: [re|im][row][lane]
     double e_l = 0.0;
     if (act) {
         HLanePos<TC, NE> P;
@@ -612,16 +638,67 @@ __global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restri
             if (write_state) { glog[w] = logdet + (double)u; gsign[w] = 1; gel[w] = e_l; }
         }
     }
-    if (partial) {
-        __shared__ double ps[WPB];
-        if (lane == 0) ps[wib] = act ? e_l : 0.0;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            Comp c{0.0, 0.0};
-            for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
-            partial[2 * blockIdx.x] = c.s;
-            partial[2 * blockIdx.x + 1] = c.c;
+    return act ? e_l : 0.0;
+}
+
+template <int WPB>
+__device__ __forceinline__ void hwarp_block_partial(double v, double* partial, int slot) {
+    __shared__ double ps[WPB];
+    if ((threadIdx.x & 31) == 0) ps[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp c{0.0, 0.0};
+        for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
+        partial[2 * slot] = c.s;
+        partial[2 * slot + 1] = c.c;
+    }
+    __syncthreads();
+}
+
+template <int NE, int NUP, class TC, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
+                                                        const TS* __restrict__ gpos,
+                                                        TS* __restrict__ gdinv, double* __restrict__ glog,
+                                                        int* __restrict__ gsign, double* __restrict__ gel, int W,
+                                                        int Wcap, int write_state, double* __restrict__ out_grad,
+                                                        double* __restrict__ out_lap, double* partial, int* flags) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
+    TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
+    load_sysh(&S, Sg, (int)sizeof(SysH<TC>));
+    const int wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wib;
+    double e_l = khw_measure_walker<NE, NUP, TC, TS>(S, KT, rows + (size_t)wib * 2 * NM * 32, gpos, gdinv, glog, gsign,
+                                                     gel, w, w < W, Wcap, write_state, out_grad, out_lap, flags);
+    if (partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
+}
+
+// Batched form (FP64 evaluation, state written, per-tile E_L partials).
+template <int NE, int NUP, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) khwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
+                                                         const BatchRec* __restrict__ recs, double* tile_partial) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    SysH<double>& S = *reinterpret_cast<SysH<double>*>(hsm);
+    double* rows = reinterpret_cast<double*>(hsm + ((sizeof(SysH<double>) + 15) / 16) * 16);
+    const int wib = threadIdx.x >> 5;
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            load_sysh(&S, static_cast<const SysH<double>*>(recs[tl.rec].tab_d), (int)sizeof(SysH<double>));
+            cur = tl.rec;
         }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + wib;
+        double e_l = khw_measure_walker<NE, NUP, double, TS>(S, static_cast<const KTable*>(R.ktab),
+                                                             rows + (size_t)wib * 2 * NM * 32, (const TS*)R.pos,
+                                                             (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap,
+                                                             1, nullptr, nullptr, R.flags);
+        hwarp_block_partial<WPB>(e_l, tile_partial, ti);
     }
 }
 
@@ -650,6 +727,65 @@ struct HegShapeOps {
         *out = static_cast<const SysH<T>*>(hs.dev_table[slot]);
         if (kt) *kt = reinterpret_cast<const KTable*>(static_cast<const unsigned char*>(hs.dev_table[slot]) + off);
         return 0;
+    }
+
+    // ---- batched launches ---------------------------------------------------
+    static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
+        const SysH<double>* d;
+        const KTable* kt;
+        int rc = table<double>(hs, &d, &kt);
+        if (rc) return rc;
+        r.tab_d = d;
+        r.tab_s = d;
+        r.ktab = kt;
+        if (prec == 1) {
+            const SysH<float>* f;
+            rc = table<float>(hs, &f);
+            if (rc) return rc;
+            r.tab_s = f;
+        }
+        return 0;
+    }
+
+    template <class T, int MOVE>
+    static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
+        auto kern = khwb_sweep<NE, NUP, T, MOVE, WPB>;
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, 0) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
+        kern<<<grid, 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    // The electron-gas sweep has no fixed-node form: batches of it run VMC only.
+    static int batch_sweep(const BatchClass& bc, int mk, const BatchCtl* ctl, cudaStream_t st, int* occ = nullptr) {
+        if (mk == MOVE_ONE_GAUSS)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_GAUSS>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_GAUSS>(bc, ctl, st, occ);
+        if (mk == MOVE_ONE_DRIFT)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_DRIFT>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_DRIFT>(bc, ctl, st, occ);
+        return 7;
+    }
+
+    template <class TS>
+    static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
+        const size_t smem = ((sizeof(SysH<double>) + 15) / 16) * 16 + sizeof(double) * WPB * 2 * NM * 32;
+        auto kern = khwb_measure<NE, NUP, TS, WPB>;
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid =
+            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
+        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
+        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
     }
 
     static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {

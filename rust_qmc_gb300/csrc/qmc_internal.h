@@ -121,6 +121,88 @@ int launch_flush(void* buf, size_t bytes, cudaStream_t st);
 int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, int nmax, double e_ref,
                   double tau, uint64_t seed, uint64_t step, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Uneven batches: many systems, each with its own walker set, advanced by one
+// persistent launch per shape class over a list of (system, walker tile).
+// ---------------------------------------------------------------------------
+#if defined(__CUDACC__)
+#define QMC_HD __host__ __device__
+#else
+#define QMC_HD
+#endif
+
+// Philox key of system s in a batch driven with `seed` (SplitMix64 of the
+// seed offset by the golden-ratio increment per system): a batched sweep of
+// system s is the standalone sweep of its walker set with this seed.
+QMC_HD inline uint64_t batch_system_seed(uint64_t seed, int s) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(s + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// One system of a batch (device-resident).
+struct BatchRec {
+    const void* tab_d = nullptr;         // system table, FP64 form (shape-specific type)
+    const void* tab_s = nullptr;         // system table in the walkers' precision
+    const void* ktab = nullptr;          // reciprocal-space table (electron gas), else null
+    void* pos = nullptr;
+    void* dinv = nullptr;
+    int* sign = nullptr;
+    double* logabs = nullptr;
+    double* el = nullptr;
+    unsigned long long* acc = nullptr;
+    int* flags = nullptr;
+    int W = 0, Wcap = 0;
+    int index = 0;                       // position in the batch (selects the Philox key)
+    int fixed_node = 0;
+};
+
+// A tile: walkers [w0, w0 + tile width) of record `rec`; tiles of one record
+// are contiguous in the list.
+struct BatchTile {
+    int rec;
+    int w0;
+};
+
+// Per-call scalars, read by the kernels from device memory so that a
+// captured graph replays with new values and advances its own step counter.
+struct BatchCtl {
+    unsigned long long step = 0;         // sweep counter of the next sweep
+    unsigned long long seed = 0;
+    double step_size = 0, tau = 0, max_drift = 0;
+    int n_sweeps = 0;
+    int row = 0;                         // energy-series row of the next measurement
+};
+
+// One shape class of a batch.
+struct BatchClass {
+    int shape = -1;
+    int prec = 0;
+    const BatchTile* tiles = nullptr;    // device
+    int ntiles = 0;
+    const BatchRec* recs = nullptr;      // device, indexed by BatchTile::rec
+    int nrec = 0;
+    const int* tile_begin = nullptr;     // device [nrec + 1]
+    double* tile_partial = nullptr;      // device [ntiles][2]
+    int grid_sweep = 0, grid_measure = 0;   // persistent grid sizes (0: one block per tile)
+};
+
+// Walkers per tile for a shape (threads per walker block or walkers per warp block).
+int batch_tile_width(int shape);
+// Persistent launches for one class; `ctl` is device-resident.
+int launch_batch_sweep(const BatchClass& bc, int move_kind, const BatchCtl* ctl, cudaStream_t st);
+int launch_batch_measure(const BatchClass& bc, cudaStream_t st);
+// Resident blocks per SM of the class's batch kernels (occupancy query).
+int batch_occupancy(int shape, int prec, int move_kind, bool measure);
+// Device tables of a system for batched launches (cached in the HostSys).
+int batch_tables(const HostSys& hs, int prec, BatchRec& rec);
+// Per-system mean E_L of the class: sum of its tiles' partials / W, written to
+// series[ctl->row * n_total + rec.index].
+int launch_batch_energy(const BatchClass& bc, const BatchCtl* ctl, double* series, int n_total, cudaStream_t st);
+// ctl->step += n_sweeps, ctl->row += 1 (one thread; ends a captured step).
+int launch_batch_advance(BatchCtl* ctl, cudaStream_t st);
+
 extern long long g_launch_count;
 
 }  // namespace qmc

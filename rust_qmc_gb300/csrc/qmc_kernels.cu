@@ -27,6 +27,17 @@ static int cuda_status(cudaError_t e) {
     int shape_step_all_##NAME(const HostSys&, DevWalkers&, int, int, uint64_t, double, uint64_t, cudaStream_t,\
                               double*);                                                                      \
     int shape_nmax_##NAME();
+#define QMC_DECLARE_BATCH(NAME)                                                                               \
+    int shape_batch_sweep_##NAME(const BatchClass&, int, const BatchCtl*, cudaStream_t, int*);                \
+    int shape_batch_measure_##NAME(const BatchClass&, cudaStream_t, int*);                                    \
+    int shape_batch_tables_##NAME(const HostSys&, int, BatchRec&);                                            \
+    int shape_batch_width_##NAME();
+QMC_DECLARE_BATCH(h2)
+QMC_DECLARE_BATCH(li)
+QMC_DECLARE_BATCH(ch4)
+QMC_DECLARE_BATCH(ch4min)
+QMC_DECLARE_BATCH(c6h6)
+QMC_DECLARE_BATCH(heg)
 QMC_DECLARE_SHAPE(h2)
 QMC_DECLARE_SHAPE(li)
 QMC_DECLARE_SHAPE(ch4)
@@ -221,6 +232,93 @@ int launch_gather_positions(const DevWalkers& dw, double* dst, const int* d_perm
     int n = N * dw.W, tpb = 256;
     if (dw.prec == 0) k_gather<double><<<(n + tpb - 1) / tpb, tpb, 0, st>>>((const double*)dw.pos, dst, d_perm, N, dw.W, dw.Wcap);
     else k_gather<float><<<(n + tpb - 1) / tpb, tpb, 0, st>>>((const float*)dw.pos, dst, d_perm, N, dw.W, dw.Wcap);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Uneven batches: dispatch by shape class, per-system energies, step counter.
+// ---------------------------------------------------------------------------
+int batch_tile_width(int shape) {
+#define C_(n) shape_batch_width_##n()
+    QMC_SHAPE_SWITCH(shape, C_)
+#undef C_
+}
+
+int batch_tables(const HostSys& hs, int prec, BatchRec& rec) {
+#define C_(n) shape_batch_tables_##n(hs, prec, rec)
+    QMC_SHAPE_SWITCH(hs.shape, C_)
+#undef C_
+}
+
+int launch_batch_sweep(const BatchClass& bc, int move_kind, const BatchCtl* ctl, cudaStream_t st) {
+#define C_(n) shape_batch_sweep_##n(bc, move_kind, ctl, st, nullptr)
+    QMC_SHAPE_SWITCH(bc.shape, C_)
+#undef C_
+}
+
+int launch_batch_measure(const BatchClass& bc, cudaStream_t st) {
+#define C_(n) shape_batch_measure_##n(bc, st, nullptr)
+    QMC_SHAPE_SWITCH(bc.shape, C_)
+#undef C_
+}
+
+int batch_occupancy(int shape, int prec, int move_kind, bool measure) {
+    BatchClass bc;
+    bc.shape = shape;
+    bc.prec = prec;
+    int occ = 0, rc = 7;
+#define C_(n) (measure ? shape_batch_measure_##n(bc, nullptr, &occ) : shape_batch_sweep_##n(bc, move_kind, nullptr, nullptr, &occ))
+    switch (shape) {
+        case SHAPE_H2: rc = C_(h2); break;
+        case SHAPE_LI: rc = C_(li); break;
+        case SHAPE_CH4: rc = C_(ch4); break;
+        case SHAPE_CH4MIN: rc = C_(ch4min); break;
+        case SHAPE_C6H6: rc = C_(c6h6); break;
+        case SHAPE_HEG54: rc = C_(heg); break;
+    }
+#undef C_
+    return rc ? -rc : occ;
+}
+
+// One warp per system: the system's tile partials (contiguous, fixed order)
+// summed with compensation, divided by its walker count.
+__global__ void k_batch_energy(const BatchRec* __restrict__ recs, int nrec, const int* __restrict__ tile_begin,
+                               const double* __restrict__ tile_partial, const BatchCtl* __restrict__ ctl,
+                               double* __restrict__ series, int n_total) {
+    const int r = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= nrec) return;
+    Comp c{0.0, 0.0};
+    for (int t = tile_begin[r] + lane; t < tile_begin[r + 1]; t += 32)
+        c = comp_add(c, Comp{tile_partial[2 * t], tile_partial[2 * t + 1]});
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Comp d{__shfl_down_sync(0xffffffffu, c.s, o), __shfl_down_sync(0xffffffffu, c.c, o)};
+        c = comp_add(c, d);
+    }
+    if (lane == 0) {
+        const BatchRec& R = recs[r];
+        series[(size_t)ctl->row * n_total + R.index] = (c.s + c.c) / (double)R.W;
+    }
+}
+
+int launch_batch_energy(const BatchClass& bc, const BatchCtl* ctl, double* series, int n_total, cudaStream_t st) {
+    if (bc.nrec == 0) return 0;
+    const int wpb = 4;
+    k_batch_energy<<<(bc.nrec + wpb - 1) / wpb, 32 * wpb, 0, st>>>(bc.recs, bc.nrec, bc.tile_begin, bc.tile_partial,
+                                                                   ctl, series, n_total);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+__global__ void k_batch_advance(BatchCtl* ctl) {
+    ctl->step += (unsigned long long)ctl->n_sweeps;
+    ctl->row += 1;
+}
+
+int launch_batch_advance(BatchCtl* ctl, cudaStream_t st) {
+    k_batch_advance<<<1, 1, 0, st>>>(ctl);
     ++g_launch_count;
     return cuda_status(cudaGetLastError());
 }

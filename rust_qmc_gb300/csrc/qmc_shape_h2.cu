@@ -5,4 +5,6 @@ namespace qmc {
 QMC_DEFINE_SHAPE_MEASURE(h2, ShapeH2)
 QMC_DEFINE_SHAPE_ONE(h2, ShapeH2)
 QMC_DEFINE_SHAPE_ALL(h2, ShapeH2)
+QMC_DEFINE_SHAPE_BATCH_SWEEP(h2, ShapeH2)
+QMC_DEFINE_SHAPE_BATCH_MEASURE(h2, ShapeH2)
 }  // namespace qmc

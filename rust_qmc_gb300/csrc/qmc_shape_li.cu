@@ -5,4 +5,6 @@ namespace qmc {
 QMC_DEFINE_SHAPE_MEASURE(li, ShapeLi)
 QMC_DEFINE_SHAPE_ONE(li, ShapeLi)
 QMC_DEFINE_SHAPE_ALL(li, ShapeLi)
+QMC_DEFINE_SHAPE_BATCH_SWEEP(li, ShapeLi)
+QMC_DEFINE_SHAPE_BATCH_MEASURE(li, ShapeLi)
 }  // namespace qmc

@@ -415,7 +415,7 @@ __global__ void k_init(const __grid_constant__ SysT<SH, double> S, TS* __restric
 }
 
 template <int TPB>
-__device__ __forceinline__ void block_partial(double v, double* partial, int* flags) {
+__device__ __forceinline__ void block_partial(double v, double* partial, int slot) {
     __shared__ double ss[TPB], sc[TPB];
     ss[threadIdx.x] = v;
     sc[threadIdx.x] = 0.0;
@@ -430,17 +430,19 @@ __device__ __forceinline__ void block_partial(double v, double* partial, int* fl
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { partial[2 * blockIdx.x] = ss[0]; partial[2 * blockIdx.x + 1] = sc[0]; }
+    if (threadIdx.x == 0) { partial[2 * slot] = ss[0]; partial[2 * slot + 1] = sc[0]; }
+    __syncthreads();
 }
 
-template <class SH, class TC, class TS, int TPB, int NR>
-__global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH, TC> S,
-                                                 const TS* __restrict__ pos, TS* __restrict__ dinv,
-                                                 double* __restrict__ logabs, int* __restrict__ sign,
-                                                 double* __restrict__ el, int W, int Wcap, int write_state,
-                                                 MeasureOut out, int P, double* partial, int* flags) {
-    const int w = blockIdx.x * TPB + threadIdx.x;
-    const bool act = w < W;
+// Full evaluation of walker w (refresh of the inverse, log|psi|, E_L and the
+// requested extras); returns E_L (0 for an inactive lane, which still runs the
+// arithmetic on a dummy configuration so that the block stays converged).
+template <class SH, class TC, class TS, int NR>
+__device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS* __restrict__ pos,
+                                                 TS* __restrict__ dinv, double* __restrict__ logabs,
+                                                 int* __restrict__ sign, double* __restrict__ el, int w, bool act,
+                                                 int Wcap, int write_state, const MeasureOut& out, int P,
+                                                 int* flags) {
     TC r[SH::NE][3];
 #pragma unroll
     for (int e = 0; e < SH::NE; ++e)
@@ -517,7 +519,19 @@ __global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH
             for (int i = 0; i < 3 * SH::NNUC; ++i) out.omega[(size_t)w * 3 * SH::NNUC + i] = omega[i];
         }
     }
-    if (partial) block_partial<TPB>(act ? e_l : 0.0, partial, flags);
+    return act ? e_l : 0.0;
+}
+
+template <class SH, class TC, class TS, int TPB, int NR>
+__global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH, TC> S,
+                                                 const TS* __restrict__ pos, TS* __restrict__ dinv,
+                                                 double* __restrict__ logabs, int* __restrict__ sign,
+                                                 double* __restrict__ el, int W, int Wcap, int write_state,
+                                                 MeasureOut out, int P, double* partial, int* flags) {
+    const int w = blockIdx.x * TPB + threadIdx.x;
+    double e_l = measure_walker<SH, TC, TS, NR>(S, pos, dinv, logabs, sign, el, w, w < W, Wcap, write_state, out, P,
+                                                flags);
+    if (partial) block_partial<TPB>(e_l, partial, blockIdx.x);
 }
 
 // Single-electron sweeps.  Shared memory holds the block's walkers as
@@ -611,21 +625,15 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
 #undef DI
 }
 
-// Occupancy target: all walkers of the 65 536-walker workload resident in
-// one wave (152 SMs x 8 blocks x 64 threads), i.e. <= 128 registers/thread.
+// n_sweeps single-electron sweeps of walker w, staged through the calling
+// thread's shared-memory columns sp / sd.
 template <class SH, class T, int MOVE, int TPB>
-__global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
-                                                   T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
-                                                   int n_sweeps, uint64_t step0, T step, T tau, T maxd,
-                                                   uint64_t seed, unsigned long long* acc_out, int* flags,
-                                                   int fixed_node) {
-    extern __shared__ __align__(16) unsigned char smraw[];
+__device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, T* __restrict__ gpos,
+                                             T* __restrict__ gdinv, int* __restrict__ gsign, int w, int Wcap,
+                                             int n_sweeps, uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+                                             unsigned long long* acc_out, int* flags, int fixed_node) {
     constexpr int NM = SH::NMAX;
-    T* sp = reinterpret_cast<T*>(smraw);
-    T* sd = sp + 3 * SH::NE * TPB;
     const int t = threadIdx.x;
-    const int w = blockIdx.x * TPB + t;
-    if (w >= W) return;
 #pragma unroll
     for (int i = 0; i < 3 * SH::NE; ++i) sp[i * TPB + t] = gpos[(size_t)i * Wcap + w];
 #pragma unroll
@@ -645,6 +653,84 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
     gsign[w] = sgn;
     if (acc) atomicAdd(acc_out, (unsigned long long)acc);
     if (flg) atomicOr(flags, flg);
+}
+
+// Occupancy target: all walkers of the 65 536-walker workload resident in
+// one wave (152 SMs x 8 blocks x 64 threads), i.e. <= 128 registers/thread.
+template <class SH, class T, int MOVE, int TPB>
+__global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_sweep_one(const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos,
+                                                   T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
+                                                   int n_sweeps, uint64_t step0, T step, T tau, T maxd,
+                                                   uint64_t seed, unsigned long long* acc_out, int* flags,
+                                                   int fixed_node) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* sp = reinterpret_cast<T*>(smraw);
+    T* sd = sp + 3 * SH::NE * TPB;
+    const int w = blockIdx.x * TPB + threadIdx.x;
+    if (w >= W) return;
+    sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, gpos, gdinv, gsign, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
+                                   acc_out, flags, fixed_node);
+}
+
+// Batched form: persistent blocks over (system, TPB-walker tile) pairs; the
+// system table is staged into shared memory ahead of the walker columns.
+template <class SH, class T>
+__host__ __device__ constexpr size_t batch_table_bytes() {
+    return (sizeof(SysT<SH, T>) + 15) / 16 * 16;
+}
+
+template <class SH, class T, int MOVE, int TPB>
+__global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) kb_sweep_one(
+    const BatchTile* __restrict__ tiles, int ntiles, const BatchRec* __restrict__ recs,
+    const BatchCtl* __restrict__ ctl) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    SysT<SH, T>& S = *reinterpret_cast<SysT<SH, T>*>(smraw);
+    T* sp = reinterpret_cast<T*>(smraw + batch_table_bytes<SH, T>());
+    T* sd = sp + 3 * SH::NE * TPB;
+    const BatchCtl c = *ctl;
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            __syncthreads();
+            stage_table(&S, recs[tl.rec].tab_s);
+            __syncthreads();
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)threadIdx.x;
+        if (w < R.W)
+            sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, (T*)R.pos, (T*)R.dinv, R.sign, w, R.Wcap, c.n_sweeps, c.step,
+                                           (T)c.step_size, (T)c.tau, (T)c.max_drift,
+                                           batch_system_seed(c.seed, R.index), R.acc, R.flags, R.fixed_node);
+    }
+}
+
+// Batched FP64 refresh + E_L with one compensated partial per tile.
+template <class SH, class TS, int TPB>
+__global__ void __launch_bounds__(TPB) kb_measure(const BatchTile* __restrict__ tiles, int ntiles,
+                                                  const BatchRec* __restrict__ recs, double* tile_partial) {
+    __shared__ __align__(16) unsigned char sraw[batch_table_bytes<SH, double>()];
+    SysT<SH, double>& S = *reinterpret_cast<SysT<SH, double>*>(sraw);
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            stage_table(&S, recs[tl.rec].tab_d);   // block_partial ended the previous tile with a barrier
+            __syncthreads();
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)threadIdx.x;
+        MeasureOut none;
+        double e_l = measure_walker<SH, double, TS, 0>(S, (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w,
+                                                       w < R.W, R.Wcap, 1, none, 0, R.flags);
+        block_partial<TPB>(e_l, tile_partial, ti);
+    }
 }
 
 // All-electron Metropolis steps (src/sampling/vmc.rs:95-119): every step
@@ -705,7 +791,7 @@ __global__ void __launch_bounds__(TPB) k_step_all(const __grid_constant__ SysT<S
             ++acc;
             if (!isfinite(el)) flg |= FLAG_NONFINITE;
         }
-        if (partial) block_partial<TPB>(act ? el : 0.0, partial + (size_t)it * 2 * nblk, flags);
+        if (partial) block_partial<TPB>(act ? el : 0.0, partial + (size_t)it * 2 * nblk, blockIdx.x);
     }
     if (act) {
 #pragma unroll
@@ -808,6 +894,90 @@ struct ShapeOps {
         return cuda_status(cudaGetLastError());
     }
 
+    // ---- batched launches ---------------------------------------------------
+    static constexpr int BTPB = 64;
+
+    // Device copy of the system table (slot 0 FP64, slot 1 FP32), cached in
+    // the HostSys and rebuilt when its parameters or nuclei change.
+    template <class T>
+    static int table(const HostSys& hs, const SysT<SH, T>** out) {
+        const int slot = sizeof(T) == 8 ? 0 : 1;
+        if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
+            SysT<SH, T> h;
+            if (!fill_sys(hs, h)) return 7;
+            if (!hs.dev_table[slot] && cudaMalloc(&hs.dev_table[slot], sizeof(h)) != cudaSuccess) return 8;
+            if (cudaMemcpy(hs.dev_table[slot], &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess) return 2;
+            hs.dev_table_version[slot] = hs.version;
+        }
+        *out = static_cast<const SysT<SH, T>*>(hs.dev_table[slot]);
+        return 0;
+    }
+
+    static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
+        const SysT<SH, double>* d;
+        int rc = table<double>(hs, &d);
+        if (rc) return rc;
+        r.tab_d = d;
+        r.tab_s = d;
+        r.ktab = nullptr;
+        if (prec == 1) {
+            const SysT<SH, float>* f;
+            rc = table<float>(hs, &f);
+            if (rc) return rc;
+            r.tab_s = f;
+        }
+        return 0;
+    }
+
+    template <class T>
+    static size_t batch_sweep_smem() {
+        return batch_table_bytes<SH, T>() + sizeof(T) * BTPB * (3 * SH::NE + 2 * SH::NMAX * SH::NMAX);
+    }
+
+    template <class T, int MOVE>
+    static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
+        const size_t smem = batch_sweep_smem<T>();
+        auto kern = kb_sweep_one<SH, T, MOVE, BTPB>;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr = true;
+        }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, BTPB, smem) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
+        kern<<<grid, BTPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
+    // occ != nullptr: report resident blocks per SM instead of launching.
+    static int batch_sweep(const BatchClass& bc, int mk, const BatchCtl* ctl, cudaStream_t st, int* occ = nullptr) {
+        if (mk == MOVE_ONE_GAUSS)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_GAUSS>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_GAUSS>(bc, ctl, st, occ);
+        if (mk == MOVE_ONE_DRIFT)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_DRIFT>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_DRIFT>(bc, ctl, st, occ);
+        return 7;
+    }
+
+    template <class TS>
+    static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
+        auto kern = kb_measure<SH, TS, BTPB>;
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, BTPB, 0) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid =
+            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
+        kern<<<grid, BTPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
+    static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
+        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
+    }
+
     template <bool ALL>
     static int sweep_part(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,
                           double maxd, uint64_t seed, cudaStream_t st, double* partial) {
@@ -841,6 +1011,20 @@ struct ShapeOps {
                                double tau, double maxd, uint64_t seed, cudaStream_t st) {                     \
         return ShapeOps<SHAPE>::template sweep_part<false>(hs, dw, mk, n, s0, step, tau, maxd, seed, st, nullptr);                 \
     }
+
+#define QMC_DEFINE_SHAPE_BATCH_SWEEP(NAME, SHAPE)                                                              \
+    int shape_batch_sweep_##NAME(const BatchClass& bc, int mk, const BatchCtl* ctl, cudaStream_t st, int* occ) { \
+        return ShapeOps<SHAPE>::batch_sweep(bc, mk, ctl, st, occ);                                            \
+    }
+
+#define QMC_DEFINE_SHAPE_BATCH_MEASURE(NAME, SHAPE)                                                            \
+    int shape_batch_measure_##NAME(const BatchClass& bc, cudaStream_t st, int* occ) {                         \
+        return ShapeOps<SHAPE>::batch_measure(bc, st, occ);                                                   \
+    }                                                                                                         \
+    int shape_batch_tables_##NAME(const HostSys& hs, int prec, BatchRec& r) {                                 \
+        return ShapeOps<SHAPE>::batch_tables(hs, prec, r);                                                    \
+    }                                                                                                         \
+    int shape_batch_width_##NAME() { return ShapeOps<SHAPE>::BTPB; }
 
 #define QMC_DEFINE_SHAPE_ALL(NAME, SHAPE)                                                                      \
     int shape_step_all_##NAME(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step,    \

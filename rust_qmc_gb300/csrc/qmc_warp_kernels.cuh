@@ -278,19 +278,14 @@ __device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, N
 }
 
 // Single-electron sweeps, one warp per walker, WPB walkers per block.
-template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__ Sg, T* __restrict__ gpos,
-                                                     T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
-                                                     int n_sweeps, uint64_t step0, T step, T tau, T maxd,
-                                                     uint64_t seed, unsigned long long* acc_out, int* flags,
-                                                     int fixed_node) {
+template <int NE, int NUP, int NNUC, class T, int MOVE>
+__device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict__ gpos, T* __restrict__ gdinv,
+                                                int* __restrict__ gsign, int w, int Wcap, int n_sweeps,
+                                                uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+                                                unsigned long long* acc_out, int* flags, int fixed_node) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
-    __shared__ SysW<T> S;
-    load_sysw(&S, Sg);
     const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
-    if (w >= W) return;                        // whole warps only; no block barrier below
     LanePos<T, NE> P;
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
@@ -415,24 +410,58 @@ __global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__
     }
 }
 
+template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__ Sg, T* __restrict__ gpos,
+                                                     T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
+                                                     int n_sweeps, uint64_t step0, T step, T tau, T maxd,
+                                                     uint64_t seed, unsigned long long* acc_out, int* flags,
+                                                     int fixed_node) {
+    __shared__ SysW<T> S;
+    load_sysw(&S, Sg);
+    const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
+    if (w >= W) return;                        // whole warps only; no block barrier below
+    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, gpos, gdinv, gsign, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
+                                            acc_out, flags, fixed_node);
+}
+
+// Batched form: persistent blocks over (system, WPB-walker tile) pairs.
+template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+                                                      const BatchRec* __restrict__ recs,
+                                                      const BatchCtl* __restrict__ ctl) {
+    __shared__ SysW<T> S;
+    const BatchCtl c = *ctl;
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            __syncthreads();
+            load_sysw(&S, static_cast<const SysW<T>*>(recs[tl.rec].tab_s));
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)(threadIdx.x >> 5);
+        if (w < R.W)
+            kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, R.sign, w, R.Wcap, c.n_sweeps, c.step,
+                                                    (T)c.step_size, (T)c.tau, (T)c.max_drift,
+                                                    batch_system_seed(c.seed, R.index), R.acc, R.flags, R.fixed_node);
+    }
+}
+
 // Full evaluation from positions (refresh + E_L), one warp per walker.
 // Per-warp shared scratch holds the sector's D, grad D and lap D rows.
-template <int NE, int NUP, int NNUC, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restrict__ Sg, const TS* __restrict__ gpos,
-                                                       TS* __restrict__ gdinv, double* __restrict__ glog,
-                                                       int* __restrict__ gsign, double* __restrict__ gel, int W,
-                                                       int Wcap, int write_state, double* __restrict__ out_grad,
-                                                       double* __restrict__ out_lap, double* partial, int* flags) {
+template <int NE, int NUP, int NNUC, class TC, class TS>
+__device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow, const TS* __restrict__ gpos,
+                                                    TS* __restrict__ gdinv, double* __restrict__ glog,
+                                                    int* __restrict__ gsign, double* __restrict__ gel, int w,
+                                                    bool act, int Wcap, int write_state,
+                                                    double* __restrict__ out_grad, double* __restrict__ out_lap,
+                                                    int* flags) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
-    __shared__ SysW<TC> S;
-    extern __shared__ __align__(16) unsigned char wsm[];
-    load_sysw(&S, Sg);
     const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int w = blockIdx.x * WPB + wib;
-    const bool act = w < W;
-    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;   // [5][NM rows][32 lanes]
     double e_l = 0.0;
     if (act) {
         LanePos<TC, NE> P;
@@ -601,17 +630,67 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
             if (write_state) { glog[w] = logdet + (double)u; gsign[w] = sg; gel[w] = e_l; }
         }
     }
-    if (partial) {
-        // block partial of E_L over the block's walkers (lane 0 of each warp)
-        __shared__ double ps[WPB];
-        if (lane == 0) ps[wib] = act ? e_l : 0.0;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            Comp c{0.0, 0.0};
-            for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
-            partial[2 * blockIdx.x] = c.s;
-            partial[2 * blockIdx.x + 1] = c.c;
+    return act ? e_l : 0.0;
+}
+
+// Compensated sum of the block's per-warp values (lane 0 of each warp) into
+// partial[2 slot], partial[2 slot + 1]; ends with a block barrier.
+template <int WPB>
+__device__ __forceinline__ void warp_block_partial(double v, double* partial, int slot) {
+    __shared__ double ps[WPB];
+    if ((threadIdx.x & 31) == 0) ps[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp c{0.0, 0.0};
+        for (int i = 0; i < WPB; ++i) c = comp_add(c, Comp{ps[i], 0.0});
+        partial[2 * slot] = c.s;
+        partial[2 * slot + 1] = c.c;
+    }
+    __syncthreads();
+}
+
+template <int NE, int NUP, int NNUC, class TC, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restrict__ Sg, const TS* __restrict__ gpos,
+                                                       TS* __restrict__ gdinv, double* __restrict__ glog,
+                                                       int* __restrict__ gsign, double* __restrict__ gel, int W,
+                                                       int Wcap, int write_state, double* __restrict__ out_grad,
+                                                       double* __restrict__ out_lap, double* partial, int* flags) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    __shared__ SysW<TC> S;
+    extern __shared__ __align__(16) unsigned char wsm[];
+    load_sysw(&S, Sg);
+    const int wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * WPB + wib;
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;   // [5][NM rows][32 lanes]
+    double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, gpos, gdinv, glog, gsign, gel, w, w < W, Wcap,
+                                                          write_state, out_grad, out_lap, flags);
+    if (partial) warp_block_partial<WPB>(e_l, partial, blockIdx.x);
+}
+
+// Batched form (FP64 evaluation, state written, per-tile E_L partials).
+template <int NE, int NUP, int NNUC, class TS, int WPB>
+__global__ void __launch_bounds__(32 * WPB) kwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
+                                                        const BatchRec* __restrict__ recs, double* tile_partial) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+    __shared__ SysW<double> S;
+    extern __shared__ __align__(16) unsigned char wsm[];
+    const int wib = threadIdx.x >> 5;
+    double* Mrow = reinterpret_cast<double*>(wsm) + (size_t)wib * 5 * NM * 32;
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            load_sysw(&S, static_cast<const SysW<double>*>(recs[tl.rec].tab_d));
+            cur = tl.rec;
         }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + wib;
+        double e_l = kw_measure_walker<NE, NUP, NNUC, double, TS>(S, Mrow, (const TS*)R.pos, (TS*)R.dinv, R.logabs,
+                                                                  R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr,
+                                                                  nullptr, R.flags);
+        warp_block_partial<WPB>(e_l, tile_partial, ti);
     }
 }
 
@@ -693,6 +772,63 @@ struct WarpShapeOps {
                                                                      dw.acc, dw.flags, dw.fixed_node);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    // ---- batched launches ---------------------------------------------------
+    static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
+        const SysW<double>* d;
+        int rc = table<double>(hs, &d);
+        if (rc) return rc;
+        r.tab_d = d;
+        r.tab_s = d;
+        r.ktab = nullptr;
+        if (prec == 1) {
+            const SysW<float>* f;
+            rc = table<float>(hs, &f);
+            if (rc) return rc;
+            r.tab_s = f;
+        }
+        return 0;
+    }
+
+    template <class T, int MOVE>
+    static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
+        auto kern = kwb_sweep<NE, NUP, NNUC, T, MOVE, WPB>;
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, 0) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
+        kern<<<grid, 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    static int batch_sweep(const BatchClass& bc, int mk, const BatchCtl* ctl, cudaStream_t st, int* occ = nullptr) {
+        if (mk == MOVE_ONE_GAUSS)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_GAUSS>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_GAUSS>(bc, ctl, st, occ);
+        if (mk == MOVE_ONE_DRIFT)
+            return bc.prec == 0 ? batch_sweep_t<double, MOVE_ONE_DRIFT>(bc, ctl, st, occ)
+                                : batch_sweep_t<float, MOVE_ONE_DRIFT>(bc, ctl, st, occ);
+        return 7;
+    }
+
+    template <class TS>
+    static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
+        const size_t smem = sizeof(double) * WPB * 5 * NM * 32;
+        auto kern = kwb_measure<NE, NUP, NNUC, TS, WPB>;
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int grid =
+            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
+        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
+    static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
+        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
     }
 
     static int sweep(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,

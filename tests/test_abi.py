@@ -17,13 +17,15 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     text = open(os.path.join(ROOT, "include", "qmc.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(qmc_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|uint64_t)\s+(qmc_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_expected_surface():
     names = header_functions()
     for n in ["qmc_init", "qmc_system_create", "qmc_eval_batch", "qmc_logderiv_batch", "qmc_forces_batch",
-              "qmc_walkers_sweep", "qmc_walkers_refresh", "qmc_vmc_run"]:
+              "qmc_walkers_sweep", "qmc_walkers_refresh", "qmc_vmc_run", "qmc_dmc_run", "qmc_batch_create",
+              "qmc_batch_sweep", "qmc_batch_refresh", "qmc_batch_run_steps", "qmc_batch_run",
+              "qmc_batch_system_seed"]:
         assert n in names
 
 
@@ -88,3 +90,19 @@ def test_no_gpu_is_an_error_not_a_fallback(qmc_lib):
     assert not h.value
     with pytest.raises(Q.QMCError):
         Q.Context(0)
+
+
+def test_batch_system_seed_is_splitmix64(qmc_lib):
+    """Per-system Philox keys of a batch: SplitMix64 of seed + (i+1) x golden."""
+    M = (1 << 64) - 1
+
+    def splitmix(seed, i):
+        z = (seed + 0x9E3779B97F4A7C15 * (i + 1)) & M
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        return z ^ (z >> 31)
+
+    for seed in (0, 1, 0x51A7E5, M):
+        keys = [Q.batch_system_seed(seed, i) for i in range(64)]
+        assert keys == [splitmix(seed, i) for i in range(64)]
+        assert len(set(keys)) == 64

@@ -533,8 +533,7 @@ void free_sys(qmc_sys_s* s) {
     free_walkers(s->scratch[0]);
     free_walkers(s->scratch[1]);
     cudaFree(s->d_perm);
-    cudaFree(s->hs.dev_table[0]);
-    cudaFree(s->hs.dev_table[1]);
+    for (void* t : s->hs.dev_table) cudaFree(t);
     delete s;
     if (--c->n_children == 0 && c->released) free_ctx(c);
 }

@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
+#include "qmc_ff.cuh"
 
 namespace qmc {
 

@@ -713,7 +713,7 @@ struct HegShapeOps {
     // when the parameters change (HostSys::version).
     template <class T>
     static int table(const HostSys& hs, const SysH<T>** out, const KTable** kt = nullptr) {
-        int slot = sizeof(T) == 8 ? 0 : 1;
+        const int slot = std::is_same<T, double>::value ? 0 : (std::is_same<T, float>::value ? 1 : 2);
         const size_t off = ((sizeof(SysH<T>) + 255) / 256) * 256;
         if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
             std::vector<unsigned char> buf(off + sizeof(KTable));

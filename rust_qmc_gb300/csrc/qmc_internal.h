@@ -51,8 +51,10 @@ struct HostSys {
     double box_L = 0.0;                  // periodic electron gas: box side
     std::vector<double> kvec;            // periodic electron gas: [n_mo*3] orbital wave vectors
     int version = 0;                     // bumped when parameters or nuclei change
-    mutable void* dev_table[2] = {nullptr, nullptr};     // cached device tables (warp kernels)
-    mutable int dev_table_version[2] = {-1, -1};
+    // cached device copies of the system table per arithmetic type:
+    // [0] FP64, [1] FP32, [2] float-float
+    mutable void* dev_table[3] = {nullptr, nullptr, nullptr};
+    mutable int dev_table_version[3] = {-1, -1, -1};
 
     int n_params() const { return 8 + (int)rot_occ.size(); }
     // Effective (rotated) MO coefficients in caller AO order.

@@ -467,17 +467,17 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
         if (out.grad) {
 #pragma unroll
             for (int e = 0; e < SH::NE; ++e) {
-                out.grad[((size_t)w * SH::NE + e) * 3 + 0] = ev.gx[e];
-                out.grad[((size_t)w * SH::NE + e) * 3 + 1] = ev.gy[e];
-                out.grad[((size_t)w * SH::NE + e) * 3 + 2] = ev.gz[e];
+                out.grad[((size_t)w * SH::NE + e) * 3 + 0] = (double)ev.gx[e];
+                out.grad[((size_t)w * SH::NE + e) * 3 + 1] = (double)ev.gy[e];
+                out.grad[((size_t)w * SH::NE + e) * 3 + 2] = (double)ev.gz[e];
             }
         }
         if (out.lap) {
 #pragma unroll
-            for (int e = 0; e < SH::NE; ++e) out.lap[(size_t)w * SH::NE + e] = ev.lap[e];
+            for (int e = 0; e < SH::NE; ++e) out.lap[(size_t)w * SH::NE + e] = (double)ev.lap[e];
         }
         if (out.O) {
-            for (int p = 0; p < P; ++p) out.O[(size_t)w * P + p] = ev.O[p];
+            for (int p = 0; p < P; ++p) out.O[(size_t)w * P + p] = (double)ev.O[p];
         }
         if (out.fhf) {
 #pragma unroll
@@ -496,9 +496,9 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
                     TC d = fsqrt(dx * dx + dy * dy + dz * dz);
                     if (d > TC(1e-10)) { TC f = S.Z[I] * S.Z[J] / (d * d * d); fx -= f * dx; fy -= f * dy; fz -= f * dz; }
                 }
-                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 0] = fx;
-                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 1] = fy;
-                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 2] = fz;
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 0] = (double)fx;
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 1] = (double)fy;
+                out.fhf[((size_t)w * SH::NNUC + I) * 3 + 2] = (double)fz;
             }
         }
         if (out.omega) {
@@ -516,7 +516,7 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
                     }
             }
 #pragma unroll
-            for (int i = 0; i < 3 * SH::NNUC; ++i) out.omega[(size_t)w * 3 * SH::NNUC + i] = omega[i];
+            for (int i = 0; i < 3 * SH::NNUC; ++i) out.omega[(size_t)w * 3 * SH::NNUC + i] = (double)omega[i];
         }
     }
     return act ? e_l : 0.0;
@@ -708,12 +708,12 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) kb_sw
     }
 }
 
-// Batched FP64 refresh + E_L with one compensated partial per tile.
-template <class SH, class TS, int TPB>
+// Batched refresh + E_L (compute type TC) with one compensated partial per tile.
+template <class SH, class TC, class TS, int TPB>
 __global__ void __launch_bounds__(TPB) kb_measure(const BatchTile* __restrict__ tiles, int ntiles,
                                                   const BatchRec* __restrict__ recs, double* tile_partial) {
-    __shared__ __align__(16) unsigned char sraw[batch_table_bytes<SH, double>()];
-    SysT<SH, double>& S = *reinterpret_cast<SysT<SH, double>*>(sraw);
+    __shared__ __align__(16) unsigned char sraw[batch_table_bytes<SH, TC>()];
+    SysT<SH, TC>& S = *reinterpret_cast<SysT<SH, TC>*>(sraw);
     int t0, t1;
     batch_tile_range(ntiles, t0, t1);
     int cur = -1;
@@ -727,8 +727,8 @@ __global__ void __launch_bounds__(TPB) kb_measure(const BatchTile* __restrict__ 
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + (int)threadIdx.x;
         MeasureOut none;
-        double e_l = measure_walker<SH, double, TS, 0>(S, (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w,
-                                                       w < R.W, R.Wcap, 1, none, 0, R.flags);
+        double e_l = measure_walker<SH, TC, TS, 0>(S, (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w,
+                                                   w < R.W, R.Wcap, 1, none, 0, R.flags);
         block_partial<TPB>(e_l, tile_partial, ti);
     }
 }
@@ -855,7 +855,7 @@ struct ShapeOps {
         }
         if (cp == 0) {
             if (dw.prec == 0) return measure2<double, double, 0>(hs, dw, ws, out, st);
-            return measure2<double, float, 0>(hs, dw, ws, out, st);
+            return measure2<ff, float, 0>(hs, dw, ws, out, st);   // FP64-class refresh on the FP32 pipe
         }
         if (dw.prec == 1) return measure2<float, float, 0>(hs, dw, ws, out, st);
         return 7;
@@ -901,7 +901,7 @@ struct ShapeOps {
     // the HostSys and rebuilt when its parameters or nuclei change.
     template <class T>
     static int table(const HostSys& hs, const SysT<SH, T>** out) {
-        const int slot = sizeof(T) == 8 ? 0 : 1;
+        const int slot = std::is_same<T, double>::value ? 0 : (std::is_same<T, float>::value ? 1 : 2);
         if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
             SysT<SH, T> h;
             if (!fill_sys(hs, h)) return 7;
@@ -913,19 +913,24 @@ struct ShapeOps {
         return 0;
     }
 
+    // tab_s: the sweep table (walker precision); tab_d: the refresh table
+    // (FP64 for FP64 walkers, float-float for FP32 walkers).
     static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
-        const SysT<SH, double>* d;
-        int rc = table<double>(hs, &d);
-        if (rc) return rc;
-        r.tab_d = d;
-        r.tab_s = d;
         r.ktab = nullptr;
-        if (prec == 1) {
-            const SysT<SH, float>* f;
-            rc = table<float>(hs, &f);
+        if (prec == 0) {
+            const SysT<SH, double>* d;
+            int rc = table<double>(hs, &d);
             if (rc) return rc;
-            r.tab_s = f;
+            r.tab_d = r.tab_s = d;
+            return 0;
         }
+        const SysT<SH, ff>* m;
+        const SysT<SH, float>* f;
+        int rc = table<ff>(hs, &m);
+        if (!rc) rc = table<float>(hs, &f);
+        if (rc) return rc;
+        r.tab_d = m;
+        r.tab_s = f;
         return 0;
     }
 
@@ -962,9 +967,9 @@ struct ShapeOps {
         return 7;
     }
 
-    template <class TS>
+    template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        auto kern = kb_measure<SH, TS, BTPB>;
+        auto kern = kb_measure<SH, TC, TS, BTPB>;
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, BTPB, 0) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
         const int grid =
@@ -975,7 +980,7 @@ struct ShapeOps {
     }
 
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
-        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
+        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_t<ff, float>(bc, st, occ);
     }
 
     template <bool ALL>

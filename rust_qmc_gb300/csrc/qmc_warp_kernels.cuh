@@ -706,7 +706,7 @@ struct WarpShapeOps {
     static int table(const HostSys& hs, const SysW<T>** out) {
         // device copies of the table, cached per system and rebuilt when the
         // parameters or nuclei change (HostSys::version)
-        int slot = sizeof(T) == 8 ? 0 : 1;
+        const int slot = std::is_same<T, double>::value ? 0 : (std::is_same<T, float>::value ? 1 : 2);
         if (!hs.dev_table[slot] || hs.dev_table_version[slot] != hs.version) {
             SysW<T>* h = new SysW<T>;
             if (!fill_sysw<T>(hs, NE, NUP, NNUC, *h)) { delete h; return 7; }

@@ -74,10 +74,12 @@ def test_init_matches_oracle(ctx, oracle, precision):
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 if precision == L.QMC_FP64 else 1e-6)
 
 
-@pytest.mark.parametrize("name", ["ch4_min", "ch4_gto", "li_ref"])
+@pytest.mark.parametrize("name", ["ch4_min", "ch4_gto", "li_ref", "h2"])
 def test_fp32_walkers_refresh_energy_within_1e6(ctx, oracle, name):
-    """FP32 walkers after sweeps: the FP64 refresh E_L equals the oracle's
-    E_L of the same (float) configuration to <= 1e-6 Ha."""
+    """FP32 walkers after sweeps: the refresh E_L (float-float arithmetic,
+    48-bit significand) equals the oracle's FP64 E_L of the same (float)
+    configuration to <= 1e-6 Ha -- the error budget -- and in fact to
+    FP64-class accuracy: 1e-9 relative on E_L, 1e-10 on log|psi|."""
     spec = BUILDERS[name]()
     sysh = Q.System(ctx, spec)
     W = 512
@@ -86,10 +88,14 @@ def test_fp32_walkers_refresh_energy_within_1e6(ctx, oracle, name):
     wk.refresh()
     wk.sweep(L.QMC_MOVE_ONE_GAUSS, 16, 0, seed=5, step=0.3)
     _, el = wk.refresh(want_energies=True)
+    logabs, sign, _ = wk.state()
     pos = wk.get_positions()
     o = oracle.evaluate(spec, pos)
     err = np.abs(el - o["e_local"])
     assert np.max(err) <= 1e-6, np.max(err)
+    assert rel(el, o["e_local"]) < 1e-9
+    assert rel(logabs, o["logabs"]) < 1e-10
+    assert np.array_equal(sign, o["sign"])
 
 
 @pytest.mark.parametrize("name,move", [("ch4_min", L.QMC_MOVE_ONE_GAUSS), ("ch4_min", L.QMC_MOVE_ONE_DRIFT),

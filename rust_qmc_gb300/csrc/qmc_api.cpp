@@ -243,7 +243,7 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
 
 void free_dev(DevWalkers& dw) {
     cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
-    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial);
+    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(dw.rows);
     dw = DevWalkers();
 }
 
@@ -265,6 +265,8 @@ int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cuda
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.flags, 4);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.acc, 8);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.partial, 8 * (size_t)dw.partial_cap);
+    const size_t rb = prec == QMC_FP32_REFINE ? refresh_rows_bytes(hs.shape) : 0;
+    if (e == cudaSuccess && rb) e = cudaMalloc((void**)&dw.rows, rb * Wc);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.flags, 0, 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, st);
@@ -1198,6 +1200,8 @@ int batch_build(qmc_ctx_s* ctx, const std::vector<qmc_walkers_s*>& wk, bool owns
             rec.Wcap = w->dw.Wcap;
             rec.index = c.members[r];
             rec.fixed_node = w->dw.fixed_node;
+            rec.rows = w->dw.rows;
+            if (c.bc.prec == QMC_FP32_REFINE && refresh_rows_bytes(c.bc.shape) && !rec.rows) return QMC_ERR_ARG;
             c.recs.push_back(rec);
             begin.push_back((int)tiles.size());
             for (int w0 = 0; w0 < rec.W; w0 += width) tiles.push_back(BatchTile{(int)r, w0});

@@ -357,13 +357,13 @@ __device__ __forceinline__ void pade_ab(T a, T b, T d, T rinv, T& u, T& upr, T& 
 // 828-829).  A is destroyed; Ainv = A^-1.  Row swaps use selects so that
 // all indices stay compile-time.
 // ---------------------------------------------------------------------------
-template <int N, class T>
-__device__ __forceinline__ bool gj_inverse(T (&A)[N][N], T (&Ainv)[N][N], double& logdet, int& sign) {
+// on_pivot(|pivot|) receives each pivot magnitude for the determinant.
+template <int N, class T, class OnPivot>
+__device__ __forceinline__ bool gj_inverse_core(T (&A)[N][N], T (&Ainv)[N][N], int& sign, OnPivot on_pivot) {
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
         for (int j = 0; j < N; ++j) Ainv[i][j] = (i == j) ? T(1) : T(0);
-    logdet = 0.0;
     sign = 1;
     bool ok = true;
 #pragma unroll
@@ -390,7 +390,7 @@ __device__ __forceinline__ bool gj_inverse(T (&A)[N][N], T (&Ainv)[N][N], double
         T piv = A[k][k];
         if (!(piv != T(0))) { ok = false; piv = T(1); }
         if (piv < 0) sign = -sign;
-        logdet += log(fabs((double)piv));
+        on_pivot(fabs(piv));
         T ip = T(1) / piv;
 #pragma unroll
         for (int j = 0; j < N; ++j) { A[k][j] *= ip; Ainv[k][j] *= ip; }
@@ -403,6 +403,22 @@ __device__ __forceinline__ bool gj_inverse(T (&A)[N][N], T (&Ainv)[N][N], double
         }
     }
     return ok;
+}
+
+template <int N, class T>
+__device__ __forceinline__ bool gj_inverse(T (&A)[N][N], T (&Ainv)[N][N], double& logdet, int& sign) {
+    logdet = 0.0;
+    return gj_inverse_core<N, T>(A, Ainv, sign, [&](T p) { logdet += log((double)p); });
+}
+
+// Float-float form: |det| accumulated as a rescaled product (one logarithm
+// per caller instead of one FP64 logarithm per pivot).
+template <int N>
+__device__ __forceinline__ bool gj_inverse_prod(ff (&A)[N][N], ff (&Ainv)[N][N], ff& pm, int& pe, int& sign) {
+    return gj_inverse_core<N, ff>(A, Ainv, sign, [&](ff p) {
+        pm = pm * p;
+        ff_rescale(pm, pe);
+    });
 }
 
 // Neumaier-compensated pair (s, c): value = s + c.

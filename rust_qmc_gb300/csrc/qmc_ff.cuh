@@ -149,6 +149,26 @@ __device__ __forceinline__ ff fexp(ff a) {
     return ff(__fmul_rn(p.hi, s), __fmul_rn(p.lo, s));
 }
 
+// A running product kept as mantissa * 2^e: the mantissa is brought back to
+// [0.5, 1) by exact power-of-two multiplies read off its exponent bits.
+// Zero, subnormal, infinite and NaN mantissas are left unchanged.
+__device__ __forceinline__ void ff_rescale(ff& m, int& e) {
+    const int be = (__float_as_int(m.hi) >> 23) & 0xff;
+    if (be == 0 || be == 0xff) return;
+    const int k = be - 126;                      // in [-125, 128]
+    const int k1 = k / 2, k2 = k - k1;           // two normal factors 2^-k1, 2^-k2
+    const float s1 = __int_as_float((127 - k1) << 23), s2 = __int_as_float((127 - k2) << 23);
+    m = ff(__fmul_rn(__fmul_rn(m.hi, s1), s2), __fmul_rn(__fmul_rn(m.lo, s1), s2));
+    e += k;
+}
+
+// Float-float values in memory as float2 (hi, lo).
+__device__ __forceinline__ void ff_store(float2* p, ff v) { *p = make_float2(v.hi, v.lo); }
+__device__ __forceinline__ ff ff_load(const float2* p) {
+    const float2 t = *p;
+    return ff(t.x, t.y);
+}
+
 // Warp shuffle of a float-float value (two FP32 shuffles).
 __device__ __forceinline__ ff wshfl(ff v, int src) {
     return ff(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));

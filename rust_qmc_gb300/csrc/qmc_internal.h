@@ -77,6 +77,7 @@ struct DevWalkers {
     double* partial = nullptr;           // reduction scratch
     int partial_cap = 0;
     int fixed_node = 0;                  // sweeps refuse sign-changing proposals (DMC)
+    float2* rows = nullptr;              // two-pass refresh scratch [N][row quantities][Wcap] (FP32 walkers)
 };
 
 // Device buffers of the DMC branching step (population control).
@@ -97,6 +98,8 @@ struct MeasureOut {
 };
 
 int nmax_of_shape(int shape);
+// Bytes per walker of the two-pass refresh scratch (0: the shape has none).
+size_t refresh_rows_bytes(int shape);
 // Scalars per walker in the inverse-matrix block (2 x nmax^2, doubled for
 // complex determinants).
 int dinv_elems_of_shape(int shape);
@@ -158,6 +161,7 @@ struct BatchRec {
     int W = 0, Wcap = 0;
     int index = 0;                       // position in the batch (selects the Philox key)
     int fixed_node = 0;
+    float2* rows = nullptr;              // two-pass refresh scratch of FP32 walkers
 };
 
 // A tile: walkers [w0, w0 + tile width) of record `rec`; tiles of one record

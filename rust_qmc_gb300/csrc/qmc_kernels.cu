@@ -45,6 +45,18 @@ QMC_DECLARE_SHAPE(ch4min)
 QMC_DECLARE_SHAPE(c6h6)
 QMC_DECLARE_SHAPE(heg)
 
+size_t refresh_rows_bytes(int shape) {
+    // N electrons x (5 NMAX + 7) float-float quantities (see RowLayout)
+    auto b = [](int ne, int nm) { return (size_t)8 * ne * (5 * nm + 7); };
+    switch (shape) {
+        case SHAPE_H2: return b(ShapeH2::NE, ShapeH2::NMAX);
+        case SHAPE_LI: return b(ShapeLi::NE, ShapeLi::NMAX);
+        case SHAPE_CH4: return b(ShapeCH4::NE, ShapeCH4::NMAX);
+        case SHAPE_CH4MIN: return b(ShapeCH4Min::NE, ShapeCH4Min::NMAX);
+    }
+    return 0;
+}
+
 int dinv_elems_of_shape(int shape) {
     int nm = nmax_of_shape(shape);
     return 2 * nm * nm * (shape == SHAPE_HEG54 ? 2 : 1);

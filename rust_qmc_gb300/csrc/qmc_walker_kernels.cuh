@@ -534,6 +534,244 @@ __global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH
     if (partial) block_partial<TPB>(e_l, partial, blockIdx.x);
 }
 
+// Bytes of a system table staged in shared memory (16-byte multiple).
+template <class SH, class T>
+__host__ __device__ constexpr size_t batch_table_bytes() {
+    return (sizeof(SysT<SH, T>) + 15) / 16 * 16;
+}
+
+// ---------------------------------------------------------------------------
+// Two-pass refresh of FP32 walkers in float-float arithmetic.
+// Pass 1, one thread per (walker, electron): the electron's MO row (values,
+// gradients, Laplacians) and its Jastrow and Coulomb sums (pairs seen from
+// both ends, halved), stored as float-float pairs in rows[e][quantity][Wcap].
+// Pass 2, one thread per walker: Gauss-Jordan inverse of each sector's
+// Slater matrix from the stored rows, the inverse written back for the
+// sweeps, the kinetic contractions and E_L.  Each pass is a short
+// instruction stream, so the FP32 pipe is not starved by instruction fetch
+// as a single fully unrolled per-walker kernel is.
+// ---------------------------------------------------------------------------
+template <class SH>
+struct RowLayout {
+    static constexpr int NM = SH::NMAX;
+    // v, d/dx, d/dy, d/dz, lap (NM each), then Jastrow gx, gy, gz, lap u,
+    // |grad u_pair|^2 sum, u (halved pairs), V (halved pairs)
+    static constexpr int QN = 5 * NM + 7;
+    static constexpr int J0 = 5 * NM;
+};
+
+template <class SH, class TS, int SIG>
+__device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* __restrict__ pos,
+                                             float2* __restrict__ rows, int e, int w, int Wcap) {
+    using RL = RowLayout<SH>;
+    constexpr int NM = RL::NM;
+    const size_t st = (size_t)Wcap;
+    float2* out = rows + (size_t)e * RL::QN * st + w;
+    const ff x = ff((float)pos[(3 * e + 0) * st + w]), y = ff((float)pos[(3 * e + 1) * st + w]),
+             z = ff((float)pos[(3 * e + 2) * st + w]);
+    MOEval<SH, ff, SIG, 2, 0> m;
+    m.run(S, x, y, z);
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        ff_store(out + (0 * NM + k) * st, m.v[k]);
+        ff_store(out + (1 * NM + k) * st, m.gx[k]);
+        ff_store(out + (2 * NM + k) * st, m.gy[k]);
+        ff_store(out + (3 * NM + k) * st, m.gz[k]);
+        ff_store(out + (4 * NM + k) * st, m.l[k]);
+    }
+    ff gx = 0, gy = 0, gz = 0, lu = 0, gsq = 0, u = 0, V = 0;
+#pragma unroll 1
+    for (int j = 0; j < SH::NE; ++j) {
+        if (j == e) continue;
+        const ff dx = x - ff((float)pos[(3 * j + 0) * st + w]), dy = y - ff((float)pos[(3 * j + 1) * st + w]),
+                 dz = z - ff((float)pos[(3 * j + 2) * st + w]);
+        ff d, ri;
+        dist(dx * dx + dy * dy + dz * dz, d, ri);
+        V += ff(0.5f) * ri;
+        if (SH::JAS == JAS_NONE) continue;
+        ff uu, upr, lt;
+        if (SH::JAS == JAS_PADE_F) {
+            pade_f(S.F, S.invF, d, ri, uu, upr, lt);
+        } else {
+            const int c = ((j < SH::NUP) == (e < SH::NUP)) ? 1 : 0;
+            pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+        }
+        u += ff(0.5f) * uu;
+        const bool skip = (SH::JAS == JAS_PADE_EEN) ? (d < ff(1e-10)) : (d == ff(0));
+        if (!skip) {
+            gx += upr * dx; gy += upr * dy; gz += upr * dz;
+            lu += lt;
+            const ff up = upr * d;
+            gsq += up * up;
+        }
+    }
+#pragma unroll
+    for (int I = 0; I < SH::NNUC; ++I) {
+        const ff dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+        ff d, ri;
+        dist(dx * dx + dy * dy + dz * dz, d, ri);
+        V -= S.Z[I] * ri;
+        if (SH::JAS != JAS_PADE_EEN) continue;
+        ff uu, upr, lt;
+        pade_ab(S.enA[I], S.enB[I], d, ri, uu, upr, lt);
+        u -= uu;
+        if (!(d < ff(1e-10))) {
+            gx -= upr * dx; gy -= upr * dy; gz -= upr * dz;
+            lu -= lt;
+        }
+    }
+    ff_store(out + (RL::J0 + 0) * st, gx);
+    ff_store(out + (RL::J0 + 1) * st, gy);
+    ff_store(out + (RL::J0 + 2) * st, gz);
+    ff_store(out + (RL::J0 + 3) * st, lu);
+    ff_store(out + (RL::J0 + 4) * st, gsq);
+    ff_store(out + (RL::J0 + 5) * st, u);
+    ff_store(out + (RL::J0 + 6) * st, V);
+}
+
+template <class SH, class TS, int SIG>
+__device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const float2* __restrict__ rows,
+                                                TS* __restrict__ dinv, int w, int wr, bool act, int Wcap,
+                                                int write_state, ff& pm, int& pe, int& sg, bool& ok, ff& kin,
+                                                ff& ut, ff& vt) {
+    using RL = RowLayout<SH>;
+    constexpr int NM = RL::NM;
+    constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
+    if (NS == 0) return;
+    constexpr int NSa = NS > 0 ? NS : 1;
+    const size_t st = (size_t)Wcap;
+    ff D[NSa][NSa], Di[NSa][NSa];
+#pragma unroll
+    for (int q = 0; q < NS; ++q)
+#pragma unroll
+        for (int k = 0; k < NS; ++k) D[q][k] = ff_load(rows + ((size_t)(SIG * SH::NUP + q) * RL::QN + k) * st + wr);
+    int s = 1;
+    ok = gj_inverse_prod<NSa>(D, Di, pm, pe, s) && ok;
+    sg *= s;
+    if (act && write_state) {
+#pragma unroll
+        for (int k = 0; k < NS; ++k)
+#pragma unroll
+            for (int j = 0; j < NS; ++j) dinv[((size_t)(SIG * NM * NM + k * NM + j)) * Wcap + w] = (TS)Di[k][j];
+    }
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        const float2* r = rows + (size_t)(SIG * SH::NUP + q) * RL::QN * st + wr;
+        ff gdx = 0, gdy = 0, gdz = 0, ld = 0;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            const ff dk = Di[k][q];
+            gdx += ff_load(r + (1 * NM + k) * st) * dk;
+            gdy += ff_load(r + (2 * NM + k) * st) * dk;
+            gdz += ff_load(r + (3 * NM + k) * st) * dk;
+            ld += ff_load(r + (4 * NM + k) * st) * dk;
+        }
+        const ff gjx = ff_load(r + (RL::J0 + 0) * st), gjy = ff_load(r + (RL::J0 + 1) * st),
+                 gjz = ff_load(r + (RL::J0 + 2) * st), lu = ff_load(r + (RL::J0 + 3) * st),
+                 gsq = ff_load(r + (RL::J0 + 4) * st);
+        const ff ax = S.qa * gjx, ay = S.qa * gjy, az = S.qa * gjz;
+        const ff lj = S.quirk_lap ? (lu + gsq) : (lu + gjx * gjx + gjy * gjy + gjz * gjz);
+        kin += ld + 2 * (gdx * ax + gdy * ay + gdz * az) + lj;
+        ut += ff_load(r + (RL::J0 + 5) * st);
+        vt += ff_load(r + (RL::J0 + 6) * st);
+    }
+}
+
+// Pass 2 for walker w (inactive lanes read walker 0's rows and store nothing).
+template <class SH, class TS>
+__device__ __forceinline__ double assemble_walker(const SysT<SH, ff>& S, const float2* __restrict__ rows,
+                                                  TS* __restrict__ dinv, double* __restrict__ logabs,
+                                                  int* __restrict__ sign, double* __restrict__ el, int w, bool act,
+                                                  int Wcap, int write_state, int* flags) {
+    const int wr = act ? w : 0;
+    ff pm = ff(1.0f), kin = 0, ut = 0, vt = 0;
+    int pe = 0, sg = 1;
+    bool ok = true;
+    assemble_sector<SH, TS, 0>(S, rows, dinv, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+    assemble_sector<SH, TS, 1>(S, rows, dinv, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+    const double logdet = log((double)pm) + (double)pe * 0.6931471805599453;
+    const double e_l = (double)(ff(-0.5f) * kin + vt + S.v_nn);
+    if (!act) return 0.0;
+    int fl = 0;
+    if (!ok) fl |= FLAG_SINGULAR;
+    if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
+    if (fl) atomicOr(flags, fl);
+    if (write_state) { logabs[w] = logdet + (double)ut; sign[w] = sg; el[w] = e_l; }
+    return e_l;
+}
+
+template <class SH, class TS>
+__global__ void __launch_bounds__(128) k_rows(const __grid_constant__ SysT<SH, ff> S, const TS* __restrict__ pos,
+                                              float2* __restrict__ rows, int W, int Wcap) {
+    const int w = blockIdx.x * 128 + threadIdx.x;
+    const int e = blockIdx.y;
+    if (w >= W) return;
+    if (e < SH::NUP) rows_electron<SH, TS, 0>(S, pos, rows, e, w, Wcap);
+    else rows_electron<SH, TS, 1>(S, pos, rows, e, w, Wcap);
+}
+
+template <class SH, class TS, int TPB>
+__global__ void __launch_bounds__(TPB) k_assemble(const __grid_constant__ SysT<SH, ff> S,
+                                                  const float2* __restrict__ rows, TS* __restrict__ dinv,
+                                                  double* __restrict__ logabs, int* __restrict__ sign,
+                                                  double* __restrict__ el, int W, int Wcap, int write_state,
+                                                  double* partial, int* flags) {
+    const int w = blockIdx.x * TPB + threadIdx.x;
+    const double e_l = assemble_walker<SH, TS>(S, rows, dinv, logabs, sign, el, w, w < W, Wcap, write_state, flags);
+    if (partial) block_partial<TPB>(e_l, partial, blockIdx.x);
+}
+
+// Batched forms.  Pass 1 runs over (tile, electron) items in tile-major
+// order so consecutive items of a block share their system's table.
+template <class SH, class TS, int TPB>
+__global__ void __launch_bounds__(TPB) kb_rows(const BatchTile* __restrict__ tiles, int ntiles,
+                                               const BatchRec* __restrict__ recs) {
+    __shared__ __align__(16) unsigned char sraw[batch_table_bytes<SH, ff>()];
+    SysT<SH, ff>& S = *reinterpret_cast<SysT<SH, ff>*>(sraw);
+    int t0, t1;
+    batch_tile_range(ntiles * SH::NE, t0, t1);
+    int cur = -1;
+    for (int it = t0; it < t1; ++it) {
+        const int ti = it / SH::NE, e = it - ti * SH::NE;
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            __syncthreads();
+            stage_table(&S, recs[tl.rec].tab_d);
+            __syncthreads();
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)threadIdx.x;
+        if (w < R.W) {
+            if (e < SH::NUP) rows_electron<SH, TS, 0>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
+            else rows_electron<SH, TS, 1>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
+        }
+    }
+}
+
+template <class SH, class TS, int TPB>
+__global__ void __launch_bounds__(TPB) kb_assemble(const BatchTile* __restrict__ tiles, int ntiles,
+                                                   const BatchRec* __restrict__ recs, double* tile_partial) {
+    __shared__ __align__(16) unsigned char sraw[batch_table_bytes<SH, ff>()];
+    SysT<SH, ff>& S = *reinterpret_cast<SysT<SH, ff>*>(sraw);
+    int t0, t1;
+    batch_tile_range(ntiles, t0, t1);
+    int cur = -1;
+    for (int ti = t0; ti < t1; ++ti) {
+        const BatchTile tl = tiles[ti];
+        if (tl.rec != cur) {
+            stage_table(&S, recs[tl.rec].tab_d);   // block_partial ended the previous tile with a barrier
+            __syncthreads();
+            cur = tl.rec;
+        }
+        const BatchRec& R = recs[tl.rec];
+        const int w = tl.w0 + (int)threadIdx.x;
+        const double e_l = assemble_walker<SH, TS>(S, R.rows, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W,
+                                                   R.Wcap, 1, R.flags);
+        block_partial<TPB>(e_l, tile_partial, ti);
+    }
+}
+
 // Single-electron sweeps.  Shared memory holds the block's walkers as
 // structure-of-arrays columns: positions [3 NE][TPB], inverse Slater
 // matrices [2][NMAX^2][TPB]; each thread only touches its own column, so no
@@ -674,10 +912,6 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
 
 // Batched form: persistent blocks over (system, TPB-walker tile) pairs; the
 // system table is staged into shared memory ahead of the walker columns.
-template <class SH, class T>
-__host__ __device__ constexpr size_t batch_table_bytes() {
-    return (sizeof(SysT<SH, T>) + 15) / 16 * 16;
-}
 
 template <class SH, class T, int MOVE, int TPB>
 __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) kb_sweep_one(
@@ -848,6 +1082,27 @@ struct ShapeOps {
         return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
     }
 
+    static int measure_split(const HostSys& hs, DevWalkers& dw, bool write_state, cudaStream_t st) {
+        SysT<SH, ff> S;
+        if (!fill_sys(hs, S)) return 7;
+        if (dw.W == 0) return 0;
+        dim3 g1((dw.W + 127) / 128, SH::NE);
+        k_rows<SH, float><<<g1, 128, 0, st>>>(S, (const float*)dw.pos, dw.rows, dw.W, dw.Wcap);
+        ++g_launch_count;
+        int rc = cuda_status(cudaGetLastError());
+        if (rc) return rc;
+        constexpr int TPB = 64;
+        const int nb = (dw.W + TPB - 1) / TPB;
+        double* partial = nullptr;
+        if (write_state && dw.partial && dw.partial_cap >= 2 * nb + 1) partial = dw.partial;
+        k_assemble<SH, float, TPB><<<nb, TPB, 0, st>>>(S, dw.rows, (float*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W,
+                                                       dw.Wcap, write_state ? 1 : 0, partial, dw.flags);
+        ++g_launch_count;
+        rc = cuda_status(cudaGetLastError());
+        if (rc || !partial) return rc;
+        return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
+    }
+
     static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
         if (out.O) {
             if (SH::JAS != JAS_PADE_EEN || cp != 0 || dw.prec != 0) return 7;
@@ -855,7 +1110,10 @@ struct ShapeOps {
         }
         if (cp == 0) {
             if (dw.prec == 0) return measure2<double, double, 0>(hs, dw, ws, out, st);
-            return measure2<ff, float, 0>(hs, dw, ws, out, st);   // FP64-class refresh on the FP32 pipe
+            // FP64-class refresh on the FP32 pipe: the two-pass form when only
+            // the walker state is wanted, else the single-kernel form
+            if (dw.rows && !out.grad && !out.lap && !out.fhf && !out.omega) return measure_split(hs, dw, ws, st);
+            return measure2<ff, float, 0>(hs, dw, ws, out, st);
         }
         if (dw.prec == 1) return measure2<float, float, 0>(hs, dw, ws, out, st);
         return 7;
@@ -979,8 +1237,35 @@ struct ShapeOps {
         return cuda_status(cudaGetLastError());
     }
 
+    // FP32 walkers: the two-pass float-float refresh (rows, then assembly).
+    static int batch_measure_split(const BatchClass& bc, cudaStream_t st, int* occ) {
+        auto k1 = kb_rows<SH, float, BTPB>;
+        auto k2 = kb_assemble<SH, float, BTPB>;
+        static int occ1 = 0, nsm = 0;
+        if (!occ1) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 2;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k1, BTPB, 0) != cudaSuccess) return 2;
+            if (occ1 < 1) occ1 = 1;
+        }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k2, BTPB, 0) == cudaSuccess ? 0 : 2;
+        if (bc.ntiles == 0) return 0;
+        const int items = bc.ntiles * SH::NE;
+        const int g1 = occ1 * nsm < items ? occ1 * nsm : items;
+        k1<<<g1, BTPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs);
+        ++g_launch_count;
+        int rc = cuda_status(cudaGetLastError());
+        if (rc) return rc;
+        const int g2 =
+            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
+        k2<<<g2, BTPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        ++g_launch_count;
+        return cuda_status(cudaGetLastError());
+    }
+
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
-        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_t<ff, float>(bc, st, occ);
+        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_split(bc, st, occ);
     }
 
     template <bool ALL>

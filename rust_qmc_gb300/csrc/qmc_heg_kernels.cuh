@@ -534,9 +534,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             }
             __syncwarp();
         }
-        // Jastrow and real-space Ewald for this lane's electrons (pairs from both ends)
+        // Jastrow for this lane's electrons (pairs from both ends)
         TC u = 0, kin = 0;
-        double vreal = 0.0;
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             const int NS = sig == 0 ? NUP : NDN;
@@ -560,18 +559,6 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     gx += f * dx; gy += f * dy; gz += f * dz;
                     lu += l;
                 }
-                if (S.real_images) {
-                    for (int ia = -1; ia <= 1; ++ia)
-                        for (int ib = -1; ib <= 1; ++ib)
-                            for (int ic = -1; ic <= 1; ++ic) {
-                                double ex = (double)dx + ia * (double)S.L, ey = (double)dy + ib * (double)S.L,
-                                       ez = (double)dz + ic * (double)S.L;
-                                double d = sqrt(ex * ex + ey * ey + ez * ez);
-                                if (d < (double)S.rcut) vreal += 0.5 * erfc((double)S.alpha * d) / d;
-                            }
-                } else if (r > TC(1e-10)) {
-                    vreal += 0.5 * erfc((double)S.alpha * (double)r) / (double)r;
-                }
             }
             if (own) {
                 TC cx = S.quirk_cross ? gqx[sig] : gdx[sig], cy = S.quirk_cross ? gqy[sig] : gdy[sig],
@@ -584,6 +571,57 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     out_grad[((size_t)w * NE + i) * 3 + 2] = gdz[sig] + gz;
                 }
                 if (out_lap) out_lap[(size_t)w * NE + i] = lp;
+            }
+        }
+        // Real-space Ewald, each unordered pair once, spread evenly over the
+        // lanes: pair p < NE (NE-1)/2 pairs electron i = p mod NE with
+        // i + p / NE + 1 (mod NE) for the first NE floor((NE-1)/2) pairs and
+        // i = p - that with i + NE/2 for the rest (even NE).  The minimum
+        // image term is FP64; the other 26 images lie beyond L/2, where each
+        // term is below erfc(alpha L/2)/(L/2), and are summed in FP32.
+        double vreal = 0.0;
+        {
+            TC* ps = Mr;                                  // the rows buffer is free again
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int j = lane + 32 * r;
+                if (j < NE) { ps[3 * j] = P.x[r]; ps[3 * j + 1] = P.y[r]; ps[3 * j + 2] = P.z[r]; }
+            }
+            __syncwarp();
+            constexpr int NPAIR = NE * (NE - 1) / 2, HALF = (NE - 1) / 2, FULL = NE * HALF;
+            const float Lf = (float)S.L, af = (float)S.alpha, rc2 = (float)S.rcut * (float)S.rcut;
+            for (int p = lane; p < NPAIR; p += 32) {
+                int i, j;
+                if (p < FULL) {
+                    i = p % NE;
+                    j = i + p / NE + 1;
+                } else {
+                    i = p - FULL;
+                    j = i + NE / 2;
+                }
+                if (j >= NE) j -= NE;
+                const TC dx = min_img(ps[3 * i] - ps[3 * j], S), dy = min_img(ps[3 * i + 1] - ps[3 * j + 1], S),
+                         dz = min_img(ps[3 * i + 2] - ps[3 * j + 2], S);
+                const double r = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
+                if (r > 1e-10) vreal += erfc((double)S.alpha * r) / r;
+                if (S.real_images) {
+                    const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+                    float acc = 0.0f;
+                    for (int ia = -1; ia <= 1; ++ia)
+                        for (int ib = -1; ib <= 1; ++ib)
+#pragma unroll
+                            for (int ic = -1; ic <= 1; ++ic) {
+                                if (!ia && !ib && !ic) continue;
+                                const float ex = fx + ia * Lf, ey = fy + ib * Lf, ez = fz + ic * Lf;
+                                const float d2 = ex * ex + ey * ey + ez * ez;
+                                if (d2 < rc2) {
+                                    const float d = sqrtf(d2);
+                                    acc += erfcf(af * d) / d;
+                                }
+                            }
+                    vreal += (double)acc;
+                }
             }
         }
         // reciprocal Ewald: rho_k = sum_i e^{i k.r_i}.  Each lane owns electrons

@@ -126,9 +126,34 @@ __device__ __forceinline__ void load_sysh(SysH<T>* dst, const SysH<T>* __restric
 
 __device__ __forceinline__ void fsincos(double x, double* s, double* c) { sincos(x, s, c); }
 __device__ __forceinline__ void fsincos(float x, float* s, float* c) { __sincosf(x, s, c); }
+// float-float phases through one FP64 sincos
+__device__ __forceinline__ void fsincos(ff x, ff* s, ff* c) {
+    double sd, cd;
+    sincos((double)x, &sd, &cd);
+    *s = ff(sd);
+    *c = ff(cd);
+}
+
+// Nearest integer of a float-float value (ties resolved by the leading part).
+using ::rint;
+__device__ __forceinline__ ff rint(ff x) {
+    float r = rintf(x.hi);
+    const float d = __fadd_rn(__fsub_rn(x.hi, r), x.lo);   // x.hi - r is exact
+    if (d > 0.5f) r += 1.0f;
+    else if (d < -0.5f) r -= 1.0f;
+    return ff(r);
+}
 
 template <class T>
 __device__ __forceinline__ T min_img(T d, const SysH<T>& S) { return d - S.L * rint(d * S.invL); }
+
+// Warp shuffles for every compute type of the electron-gas kernels.
+__device__ __forceinline__ float hshfl(float v, int s) { return __shfl_sync(0xffffffffu, v, s); }
+__device__ __forceinline__ double hshfl(double v, int s) { return __shfl_sync(0xffffffffu, v, s); }
+__device__ __forceinline__ ff hshfl(ff v, int s) { return wshfl(v, s); }
+__device__ __forceinline__ float hshfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double hshfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ ff hshfl_xor(ff v, int m) { return shfl_xor(v, m); }
 
 // Jastrow pair (src/systems/heg.rs:352-444): u, u'(r) and u'' + 2u'/r;
 // zero outside (1e-10, L/2).
@@ -161,17 +186,17 @@ struct HLanePos {
     T x[2], y[2], z[2];
     __device__ __forceinline__ void get(int e, T& ex, T& ey, T& ez) const {
         T a = e < 32 ? x[0] : x[1], b = e < 32 ? y[0] : y[1], c = e < 32 ? z[0] : z[1];
-        ex = __shfl_sync(0xffffffffu, a, e & 31);
-        ey = __shfl_sync(0xffffffffu, b, e & 31);
-        ez = __shfl_sync(0xffffffffu, c, e & 31);
+        ex = hshfl(a, e & 31);
+        ey = hshfl(b, e & 31);
+        ez = hshfl(c, e & 31);
     }
     // Same, for an index that differs between lanes: the source lane cannot know which
     // half the reading lane wants, so both halves travel and the reader selects.
     __device__ __forceinline__ void get_own(int e, T& ex, T& ey, T& ez) const {
         const int s = e & 31;
-        T x0 = __shfl_sync(0xffffffffu, x[0], s), x1 = __shfl_sync(0xffffffffu, x[1], s);
-        T y0 = __shfl_sync(0xffffffffu, y[0], s), y1 = __shfl_sync(0xffffffffu, y[1], s);
-        T z0 = __shfl_sync(0xffffffffu, z[0], s), z1 = __shfl_sync(0xffffffffu, z[1], s);
+        T x0 = hshfl(x[0], s), x1 = hshfl(x[1], s);
+        T y0 = hshfl(y[0], s), y1 = hshfl(y[1], s);
+        T z0 = hshfl(z[0], s), z1 = hshfl(z[1], s);
         ex = e < 32 ? x0 : x1; ey = e < 32 ? y0 : y1; ez = e < 32 ? z0 : z1;
     }
 };
@@ -179,7 +204,7 @@ struct HLanePos {
 template <class T>
 __device__ __forceinline__ T hsum(T v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += hshfl_xor(v, o);
     return v;
 }
 
@@ -445,6 +470,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             P.z[r] = ok ? (TC)gpos[(3 * j + 2) * (size_t)Wcap + w] : TC(0);
         }
         double logdet = 0.0;
+        ff pmag = ff(1.0f);                       // float-float form: |det|^2 = pmag 2^pexp
+        int pexp = 0;
         bool ok = true;
         TC gdx[2] = {0, 0}, gdy[2] = {0, 0}, gdz[2] = {0, 0}, gqx[2] = {0, 0}, gqy[2] = {0, 0}, gqz[2] = {0, 0};
         TC ldet[2] = {0, 0};
@@ -490,10 +517,15 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     a = Ir[k]; b = Ir[i]; Ir[k] = sw ? b : a; Ir[i] = sw ? a : b;
                     a = Ii[k]; b = Ii[i]; Ii[k] = sw ? b : a; Ii[i] = sw ? a : b;
                 }
-                TC pr = __shfl_sync(0xffffffffu, Ar[k], k), pi = __shfl_sync(0xffffffffu, Ai[k], k);
+                TC pr = hshfl(Ar[k], k), pi = hshfl(Ai[k], k);
                 TC pa = pr * pr + pi * pi;
                 if (!(pa > TC(0))) { ok = false; pr = 1; pi = 0; pa = 1; }
-                logdet += 0.5 * log((double)pa);
+                if constexpr (std::is_same<TC, ff>::value) {
+                    pmag = pmag * pa;                  // |det|^2 as a rescaled product
+                    ff_rescale(pmag, pexp);
+                } else {
+                    logdet += 0.5 * log((double)pa);
+                }
                 TC ipr = pr / pa, ipi = -pi / pa;
                 TC t;
                 t = Ar[k] * ipr - Ai[k] * ipi; Ai[k] = Ar[k] * ipi + Ai[k] * ipr; Ar[k] = t;
@@ -501,7 +533,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
 #pragma unroll
                 for (int i = 0; i < NM; ++i) {
                     if (i == k || i >= NS) continue;
-                    TC fr = __shfl_sync(0xffffffffu, Ar[i], k), fi = __shfl_sync(0xffffffffu, Ai[i], k);
+                    TC fr = hshfl(Ar[i], k), fi = hshfl(Ai[i], k);
                     Ar[i] -= fr * Ar[k] - fi * Ai[k]; Ai[i] -= fr * Ai[k] + fi * Ar[k];
                     Ir[i] -= fr * Ir[k] - fi * Ii[k]; Ii[i] -= fr * Ii[k] + fi * Ir[k];
                 }
@@ -534,6 +566,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             }
             __syncwarp();
         }
+        if constexpr (std::is_same<TC, ff>::value)
+            logdet = 0.5 * (log((double)pmag) + (double)pexp * 0.6931471805599453);
         // Jastrow for this lane's electrons (pairs from both ends)
         TC u = 0, kin = 0;
 #pragma unroll
@@ -566,11 +600,11 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 TC lp = ldet[sig] + lu + gx * gx + gy * gy + gz * gz + 2 * (cx * gx + cy * gy + cz * gz);
                 kin += lp;
                 if (out_grad) {
-                    out_grad[((size_t)w * NE + i) * 3 + 0] = gdx[sig] + gx;
-                    out_grad[((size_t)w * NE + i) * 3 + 1] = gdy[sig] + gy;
-                    out_grad[((size_t)w * NE + i) * 3 + 2] = gdz[sig] + gz;
+                    out_grad[((size_t)w * NE + i) * 3 + 0] = (double)(gdx[sig] + gx);
+                    out_grad[((size_t)w * NE + i) * 3 + 1] = (double)(gdy[sig] + gy);
+                    out_grad[((size_t)w * NE + i) * 3 + 2] = (double)(gdz[sig] + gz);
                 }
-                if (out_lap) out_lap[(size_t)w * NE + i] = lp;
+                if (out_lap) out_lap[(size_t)w * NE + i] = (double)lp;
             }
         }
         // Real-space Ewald, each unordered pair once, spread evenly over the
@@ -712,14 +746,14 @@ __global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restri
     if (partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
-// Batched form (FP64 evaluation, state written, per-tile E_L partials).
-template <int NE, int NUP, class TS, int WPB>
+// Batched form (compute type TC, state written, per-tile E_L partials).
+template <int NE, int NUP, class TC, class TS, int WPB>
 __global__ void __launch_bounds__(32 * WPB) khwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
                                                          const BatchRec* __restrict__ recs, double* tile_partial) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     extern __shared__ __align__(16) unsigned char hsm[];
-    SysH<double>& S = *reinterpret_cast<SysH<double>*>(hsm);
-    double* rows = reinterpret_cast<double*>(hsm + ((sizeof(SysH<double>) + 15) / 16) * 16);
+    SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
+    TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
     const int wib = threadIdx.x >> 5;
     int t0, t1;
     batch_tile_range(ntiles, t0, t1);
@@ -727,12 +761,12 @@ __global__ void __launch_bounds__(32 * WPB) khwb_measure(const BatchTile* __rest
     for (int ti = t0; ti < t1; ++ti) {
         const BatchTile tl = tiles[ti];
         if (tl.rec != cur) {
-            load_sysh(&S, static_cast<const SysH<double>*>(recs[tl.rec].tab_d), (int)sizeof(SysH<double>));
+            load_sysh(&S, static_cast<const SysH<TC>*>(recs[tl.rec].tab_d), (int)sizeof(SysH<TC>));
             cur = tl.rec;
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + wib;
-        double e_l = khw_measure_walker<NE, NUP, double, TS>(S, static_cast<const KTable*>(R.ktab),
+        double e_l = khw_measure_walker<NE, NUP, TC, TS>(S, static_cast<const KTable*>(R.ktab),
                                                              rows + (size_t)wib * 2 * NM * 32, (const TS*)R.pos,
                                                              (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap,
                                                              1, nullptr, nullptr, R.flags);
@@ -768,20 +802,26 @@ struct HegShapeOps {
     }
 
     // ---- batched launches ---------------------------------------------------
+    // tab_s: the sweep table (walker precision); tab_d: the refresh table
+    // (FP64 for FP64 walkers, float-float for FP32 walkers).
     static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
-        const SysH<double>* d;
         const KTable* kt;
-        int rc = table<double>(hs, &d, &kt);
-        if (rc) return rc;
-        r.tab_d = d;
-        r.tab_s = d;
-        r.ktab = kt;
-        if (prec == 1) {
-            const SysH<float>* f;
-            rc = table<float>(hs, &f);
+        if (prec == 0) {
+            const SysH<double>* d;
+            int rc = table<double>(hs, &d, &kt);
             if (rc) return rc;
-            r.tab_s = f;
+            r.tab_d = r.tab_s = d;
+            r.ktab = kt;
+            return 0;
         }
+        const SysH<ff>* m;
+        const SysH<float>* f;
+        int rc = table<ff>(hs, &m, &kt);
+        if (!rc) rc = table<float>(hs, &f);
+        if (rc) return rc;
+        r.tab_d = m;
+        r.tab_s = f;
+        r.ktab = kt;
         return 0;
     }
 
@@ -807,10 +847,10 @@ struct HegShapeOps {
         return 7;
     }
 
-    template <class TS>
+    template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = ((sizeof(SysH<double>) + 15) / 16) * 16 + sizeof(double) * WPB * 2 * NM * 32;
-        auto kern = khwb_measure<NE, NUP, TS, WPB>;
+        const size_t smem = ((sizeof(SysH<TC>) + 15) / 16) * 16 + sizeof(TC) * WPB * 2 * NM * 32;
+        auto kern = khwb_measure<NE, NUP, TC, TS, WPB>;
         static bool attr = false;
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
@@ -823,7 +863,7 @@ struct HegShapeOps {
     }
 
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
-        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
+        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_t<ff, float>(bc, st, occ);
     }
 
     static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
@@ -859,8 +899,9 @@ struct HegShapeOps {
 
     static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
         if (out.O || out.fhf || out.omega) return 7;
+        // FP32 walkers refresh in float-float arithmetic on the FP32 pipe
         if (cp == 0) return dw.prec == 0 ? measure2<double, double>(hs, dw, ws, out, st)
-                                         : measure2<double, float>(hs, dw, ws, out, st);
+                                         : measure2<ff, float>(hs, dw, ws, out, st);
         if (dw.prec == 1) return measure2<float, float>(hs, dw, ws, out, st);
         return 7;
     }

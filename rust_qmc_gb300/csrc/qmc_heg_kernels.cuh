@@ -35,6 +35,8 @@ struct SysH {
     T k2sum;                       // (1/2) sum over occupied |k|^2 of both sectors
     T kvec[2][32][3];              // [sector][column][xyz]
     int nk;
+    int kmax;                      // reciprocal cutoff |n| <= kmax (sphere) or |n_i| <= kmax (cube)
+    int kcube;                     // 1: the reference's full cube of integer vectors
     int perm[64];                  // internal -> caller electron index
 };
 
@@ -42,6 +44,7 @@ struct SysH {
 struct KTable {
     int kint[HMAX_K][3];
     double kw[HMAX_K];
+    float2 kwf[HMAX_K];            // kw as a float-float pair (hi, lo)
 };
 
 template <class T>
@@ -75,10 +78,14 @@ static bool fill_sysh(const HostSys& hs, int NE, int NUP, SysH<T>& S, KTable& KT
                 double k2 = dk * dk * (nx * nx + ny * ny + nz * nz);
                 KT.kint[nk][0] = nx; KT.kint[nk][1] = ny; KT.kint[nk][2] = nz;
                 KT.kw[nk] = 4.0 * M_PI / V * std::exp(-k2 / (4.0 * alpha * alpha)) / k2;
+                KT.kwf[nk].x = (float)KT.kw[nk];
+                KT.kwf[nk].y = (float)(KT.kw[nk] - (double)KT.kwf[nk].x);
                 wsum += KT.kw[nk];
                 ++nk;
             }
     S.nk = nk;
+    S.kmax = K;
+    S.kcube = qe ? 1 : 0;
     const int N = hs.N;
     if (qe) {
         // heg.rs:526-581: (1/2) sum_k f_k (|rho_k|^2 - N) and -0.448 N / r_s
@@ -120,7 +127,11 @@ template <class T>
 __device__ __forceinline__ void load_sysh(SysH<T>* dst, const SysH<T>* __restrict__ src, int bytes) {
     const int4* s = reinterpret_cast<const int4*>(src);
     int4* d = reinterpret_cast<int4*>(dst);
-    for (int i = threadIdx.x; i < bytes / (int)sizeof(int4); i += blockDim.x) d[i] = s[i];
+    const int n16 = bytes / (int)sizeof(int4);
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+    // tail words when the size is not a multiple of 16 bytes
+    for (int i = n16 * 4 + threadIdx.x; i < bytes / 4; i += blockDim.x)
+        reinterpret_cast<int*>(dst)[i] = reinterpret_cast<const int*>(src)[i];
     __syncthreads();
 }
 
@@ -200,6 +211,15 @@ struct HLanePos {
         ex = e < 32 ? x0 : x1; ey = e < 32 ? y0 : y1; ez = e < 32 ? z0 : z1;
     }
 };
+
+// Ewald weight of table entry t in the compute type.
+template <class T>
+__device__ __forceinline__ T kweight(const KTable* __restrict__ KT, int t) { return (T)KT->kw[t]; }
+template <>
+__device__ __forceinline__ ff kweight<ff>(const KTable* __restrict__ KT, int t) {
+    const float2 w = KT->kwf[t];
+    return ff(w.x, w.y);
+}
 
 template <class T>
 __device__ __forceinline__ T hsum(T v) {
@@ -658,44 +678,85 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 }
             }
         }
-        // reciprocal Ewald: rho_k = sum_i e^{i k.r_i}.  Each lane owns electrons
-        // lane and lane+32 and builds e^{i m dk x} (m = 0..KM) by repeated
-        // multiplication; negative m are conjugates.  One warp reduction per k.
+        // reciprocal Ewald: rho_k = sum_i e^{i k.r_i} over the half space of
+        // integer vectors n (k = 2 pi n / L), visited in the order of the
+        // host's weight table (nx, then ny, then nz ascending).  For each of
+        // its electrons a lane keeps the running phase e^{i k.r}, advanced by
+        // one complex multiply per step; one warp reduction per k.  Electrons
+        // a lane does not own start from zero phase and contribute nothing.
         double vk = 0.0;
         {
-            constexpr int KM = 14;
             const double dk = 2.0 * M_PI / (double)S.L;
-            double Exr[2][KM + 1], Exi[2][KM + 1], Eyr[2][KM + 1], Eyi[2][KM + 1], Ezr[2][KM + 1], Ezi[2][KM + 1];
+            const int K = S.kmax;
+            TC exr[2], exi[2], eyr[2], eyi[2], ezr[2], ezi[2], ymr[2], ymi[2], zmr[2], zmi[2], pxr[2], pxi[2];
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
-                double bxs, bxc, bys, byc, bzs, bzc;
-                sincos(dk * (double)P.x[r], &bxs, &bxc);
-                sincos(dk * (double)P.y[r], &bys, &byc);
-                sincos(dk * (double)P.z[r], &bzs, &bzc);
-                Exr[r][0] = 1; Exi[r][0] = 0; Eyr[r][0] = 1; Eyi[r][0] = 0; Ezr[r][0] = 1; Ezi[r][0] = 0;
-                for (int m = 1; m <= KM; ++m) {
-                    Exr[r][m] = Exr[r][m - 1] * bxc - Exi[r][m - 1] * bxs; Exi[r][m] = Exr[r][m - 1] * bxs + Exi[r][m - 1] * bxc;
-                    Eyr[r][m] = Eyr[r][m - 1] * byc - Eyi[r][m - 1] * bys; Eyi[r][m] = Eyr[r][m - 1] * bys + Eyi[r][m - 1] * byc;
-                    Ezr[r][m] = Ezr[r][m - 1] * bzc - Ezi[r][m - 1] * bzs; Ezi[r][m] = Ezr[r][m - 1] * bzs + Ezi[r][m - 1] * bzc;
+                const bool own = lane + 32 * r < NE;
+                double s, c;
+                sincos(dk * (double)P.x[r], &s, &c);
+                exr[r] = own ? TC(c) : TC(0); exi[r] = own ? TC(s) : TC(0);
+                sincos(dk * (double)P.y[r], &s, &c);
+                eyr[r] = own ? TC(c) : TC(0); eyi[r] = own ? TC(s) : TC(0);
+                sincos(dk * (double)P.z[r], &s, &c);
+                ezr[r] = own ? TC(c) : TC(0); ezi[r] = own ? TC(s) : TC(0);
+                // e^{-i K dk y}, e^{-i K dk z}: K multiplications by the conjugate
+                ymr[r] = own ? TC(1) : TC(0); ymi[r] = TC(0);
+                zmr[r] = own ? TC(1) : TC(0); zmi[r] = TC(0);
+                for (int m = 0; m < K; ++m) {
+                    TC t = ymr[r] * eyr[r] + ymi[r] * eyi[r];
+                    ymi[r] = ymi[r] * eyr[r] - ymr[r] * eyi[r]; ymr[r] = t;
+                    t = zmr[r] * ezr[r] + zmi[r] * ezi[r];
+                    zmi[r] = zmi[r] * ezr[r] - zmr[r] * ezi[r]; zmr[r] = t;
                 }
+                pxr[r] = TC(1); pxi[r] = TC(0);
             }
-            for (int t = 0; t < S.nk; ++t) {
-                const int nx = KT->kint[t][0], ny = KT->kint[t][1], nz = KT->kint[t][2];
-                const int ay = ny < 0 ? -ny : ny, az = nz < 0 ? -nz : nz;
-                double rr = 0.0, ri = 0.0;
+            TC vkt = TC(0);
+            int t = 0;
+            for (int nx = 0; nx <= K; ++nx) {
+                TC qr[2], qi[2];                              // e^{i (nx x + ny y) dk}, ny = -K
 #pragma unroll
                 for (int r = 0; r < 2; ++r) {
-                    if (lane + 32 * r >= NE) continue;
-                    double xr = Exr[r][nx], xi = Exi[r][nx];
-                    double yr = Eyr[r][ay], yi = ny < 0 ? -Eyi[r][ay] : Eyi[r][ay];
-                    double zr = Ezr[r][az], zi = nz < 0 ? -Ezi[r][az] : Ezi[r][az];
-                    double pr = xr * yr - xi * yi, pi = xr * yi + xi * yr;
-                    rr += pr * zr - pi * zi;
-                    ri += pr * zi + pi * zr;
+                    qr[r] = pxr[r] * ymr[r] - pxi[r] * ymi[r];
+                    qi[r] = pxr[r] * ymi[r] + pxi[r] * ymr[r];
                 }
-                rr = hsum(rr); ri = hsum(ri);
-                vk += KT->kw[t] * (rr * rr + ri * ri);
+                for (int ny = -K; ny <= K; ++ny) {
+                    const int rest = K * K - nx * nx - ny * ny;
+                    if (!(nx == 0 && ny < 0) && (S.kcube || rest >= 0)) {
+                        TC tr[2], ti[2];                      // nz = -K
+#pragma unroll
+                        for (int r = 0; r < 2; ++r) {
+                            tr[r] = qr[r] * zmr[r] - qi[r] * zmi[r];
+                            ti[r] = qr[r] * zmi[r] + qi[r] * zmr[r];
+                        }
+                        for (int nz = -K; nz <= K; ++nz) {
+                            if (!(nx == 0 && ny == 0 && nz <= 0) && (S.kcube || nz * nz <= rest)) {
+                                TC rr = hsum(tr[0] + tr[1]), ri = hsum(ti[0] + ti[1]);
+                                vkt += kweight<TC>(KT, t) * (rr * rr + ri * ri);
+                                ++t;
+                            }
+#pragma unroll
+                            for (int r = 0; r < 2; ++r) {
+                                TC x = tr[r] * ezr[r] - ti[r] * ezi[r];
+                                ti[r] = tr[r] * ezi[r] + ti[r] * ezr[r];
+                                tr[r] = x;
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        TC x = qr[r] * eyr[r] - qi[r] * eyi[r];
+                        qi[r] = qr[r] * eyi[r] + qi[r] * eyr[r];
+                        qr[r] = x;
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    TC x = pxr[r] * exr[r] - pxi[r] * exi[r];
+                    pxi[r] = pxr[r] * exi[r] + pxi[r] * exr[r];
+                    pxr[r] = x;
+                }
             }
+            vk = (double)vkt;
         }
         u = hsum(u);
         kin = hsum(kin);

@@ -100,9 +100,14 @@ static bool fill_sysw(const HostSys& hs, int NE, int NUP, int NNUC, SysW<T>& S) 
 // Copy the table from global to shared memory (whole block).
 template <class T>
 __device__ __forceinline__ void load_sysw(SysW<T>* dst, const SysW<T>* __restrict__ src) {
+    static_assert(sizeof(SysW<T>) % 4 == 0, "table size must be a multiple of 4 bytes");
     const int4* s = reinterpret_cast<const int4*>(src);
     int4* d = reinterpret_cast<int4*>(dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(SysW<T>) / sizeof(int4)); i += blockDim.x) d[i] = s[i];
+    constexpr int n16 = (int)(sizeof(SysW<T>) / sizeof(int4));
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+    // tail words when the size is not a multiple of 16 bytes
+    for (int i = n16 * 4 + threadIdx.x; i < (int)(sizeof(SysW<T>) / 4); i += blockDim.x)
+        reinterpret_cast<int*>(dst)[i] = reinterpret_cast<const int*>(src)[i];
     __syncthreads();
 }
 

@@ -65,6 +65,8 @@ static bool fill_sysh(const HostSys& hs, int NE, int NUP, SysH<T>& S, KTable& KT
     S.alpha = (T)alpha;
     S.real_images = qe ? 0 : 1;
     S.rcut = (T)(5.6 / alpha);
+    // the device sums the 27 nearest images: the cutoff must stay below 1.5 L
+    if (!qe && 5.6 / alpha >= 1.5 * L) return false;
     // reciprocal half space; weight (4 pi / V) e^{-k^2 / 4 alpha^2} / k^2
     int nk = 0;
     double wsum = 0.0;

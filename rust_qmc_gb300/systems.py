@@ -392,14 +392,16 @@ def heg_k_vectors(n, L):
 HEG_FORMS = {"pade": 0, "rpa": 1, "yukawa": 2}
 
 
-def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, alpha_L=5.0, kmax=8):
+def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, alpha_L=4.0, kmax=6):
     """Homogeneous electron gas (src/systems/heg.rs:119-170): box
     L = (4 pi N / 3)^(1/3) r_s, closed-shell plane-wave determinants (N/2 per
     spin, same k set), Jastrow u = A r/(1 + r/F + 0.2 r^2/F^2) (RPA form) with
     the reference's amplitudes A_same = 0.5, A_anti = 0.25, minimum image and
     cutoff at L/2.  With ``reference_quirks`` the Ewald sum and cross term are
     the reference's; otherwise the one-component-plasma Ewald sum with
-    alpha = alpha_L / L and |n| <= kmax reciprocal vectors."""
+    alpha = alpha_L / L (alpha_L >= 3.74: real-space images within 5.6/alpha
+    < 1.5 L) and |n| <= kmax reciprocal vectors.  The default (4, 6) keeps the
+    Ewald energy within 1e-10 Ha of the converged value with 462 vectors."""
     box = (4.0 * math.pi / 3.0 * n_elec) ** (1.0 / 3.0) * rs
     nup = n_elec // 2
     k = heg_k_vectors(nup, box)

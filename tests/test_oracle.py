@@ -223,7 +223,7 @@ def test_heg_madelung_constant(oracle):
     assert abs(e - (-2.837297479 / (2 * spec.box_L))) < 1e-8
 
 
-@pytest.mark.parametrize("alphaL,kmax", [(4.0, 7), (6.0, 11), (7.0, 13)])
+@pytest.mark.parametrize("alphaL,kmax", [(4.0, 6), (4.0, 7), (6.0, 11), (7.0, 13)])
 def test_heg_ewald_alpha_invariance(oracle, alphaL, kmax):
     """The one-component-plasma Ewald energy does not depend on the splitting
     parameter to 1e-8 Ha (the 54-electron workload's convergence target)."""

@@ -159,10 +159,13 @@ __device__ __forceinline__ void ao_lane(const SysW<T>& S, T x, T y, T z, int lan
 __device__ __forceinline__ float wshfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ double wshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ int wshfl(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float wshfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double wshfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ ff wshfl_xor(ff v, int m) { return shfl_xor(v, m); }
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += wshfl_xor(v, o);
     return v;
 }
 
@@ -479,6 +482,8 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
             P.z[r] = ok ? (TC)gpos[(3 * j + 2) * (size_t)Wcap + w] : TC(0);
         }
         double logdet = 0.0;
+        ff pmag = ff(1.0f);                       // float-float form: |det| = pmag 2^pexp
+        int pexp = 0;
         int sg = 1;
         bool ok = true;
         // per-lane electron results: lane owns electron (sig*NUP + lane) of each sector
@@ -532,7 +537,12 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
                 TC piv = wshfl(Dc[k], k);
                 if (!(piv != TC(0))) { ok = false; piv = TC(1); }
                 if (piv < 0) sg = -sg;
-                logdet += log(fabs((double)piv));
+                if constexpr (std::is_same<TC, ff>::value) {
+                    pmag = pmag * fabs(piv);           // |det| as a rescaled product
+                    ff_rescale(pmag, pexp);
+                } else {
+                    logdet += log(fabs((double)piv));
+                }
                 TC ip = TC(1) / piv;
                 Dc[k] *= ip;
                 Ic[k] *= ip;
@@ -616,16 +626,18 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
                 kin += lp;
                 const int ecall = i;   // internal index; host permutes to caller order
                 if (out_grad) {
-                    out_grad[((size_t)w * NE + ecall) * 3 + 0] = gdx[sig] + ax;
-                    out_grad[((size_t)w * NE + ecall) * 3 + 1] = gdy[sig] + ay;
-                    out_grad[((size_t)w * NE + ecall) * 3 + 2] = gdz[sig] + az;
+                    out_grad[((size_t)w * NE + ecall) * 3 + 0] = (double)(gdx[sig] + ax);
+                    out_grad[((size_t)w * NE + ecall) * 3 + 1] = (double)(gdy[sig] + ay);
+                    out_grad[((size_t)w * NE + ecall) * 3 + 2] = (double)(gdz[sig] + az);
                 }
-                if (out_lap) out_lap[(size_t)w * NE + ecall] = lp;
+                if (out_lap) out_lap[(size_t)w * NE + ecall] = (double)lp;
             }
         }
         u = wsum(u);
         V = wsum(V);
         kin = wsum(kin);
+        if constexpr (std::is_same<TC, ff>::value)
+            logdet = log((double)pmag) + (double)pexp * 0.6931471805599453;
         e_l = (double)(TC(-0.5) * kin + V + S.v_nn);
         if (lane == 0) {
             int fl = 0;
@@ -672,27 +684,27 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
     if (partial) warp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
-// Batched form (FP64 evaluation, state written, per-tile E_L partials).
-template <int NE, int NUP, int NNUC, class TS, int WPB>
+// Batched form (compute type TC, state written, per-tile E_L partials).
+template <int NE, int NUP, int NNUC, class TC, class TS, int WPB>
 __global__ void __launch_bounds__(32 * WPB) kwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
                                                         const BatchRec* __restrict__ recs, double* tile_partial) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
-    __shared__ SysW<double> S;
+    __shared__ SysW<TC> S;
     extern __shared__ __align__(16) unsigned char wsm[];
     const int wib = threadIdx.x >> 5;
-    double* Mrow = reinterpret_cast<double*>(wsm) + (size_t)wib * 5 * NM * 32;
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;
     int t0, t1;
     batch_tile_range(ntiles, t0, t1);
     int cur = -1;
     for (int ti = t0; ti < t1; ++ti) {
         const BatchTile tl = tiles[ti];
         if (tl.rec != cur) {
-            load_sysw(&S, static_cast<const SysW<double>*>(recs[tl.rec].tab_d));
+            load_sysw(&S, static_cast<const SysW<TC>*>(recs[tl.rec].tab_d));
             cur = tl.rec;
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + wib;
-        double e_l = kw_measure_walker<NE, NUP, NNUC, double, TS>(S, Mrow, (const TS*)R.pos, (TS*)R.dinv, R.logabs,
+        double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, (const TS*)R.pos, (TS*)R.dinv, R.logabs,
                                                                   R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr,
                                                                   nullptr, R.flags);
         warp_block_partial<WPB>(e_l, tile_partial, ti);
@@ -759,8 +771,9 @@ struct WarpShapeOps {
 
     static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
         if (out.O || out.fhf || out.omega) return 7;
+        // FP32 walkers refresh in float-float arithmetic on the FP32 pipe
         if (cp == 0) return dw.prec == 0 ? measure2<double, double>(hs, dw, ws, out, st)
-                                         : measure2<double, float>(hs, dw, ws, out, st);
+                                         : measure2<ff, float>(hs, dw, ws, out, st);
         if (dw.prec == 1) return measure2<float, float>(hs, dw, ws, out, st);
         return 7;
     }
@@ -780,19 +793,24 @@ struct WarpShapeOps {
     }
 
     // ---- batched launches ---------------------------------------------------
+    // tab_s: the sweep table (walker precision); tab_d: the refresh table
+    // (FP64 for FP64 walkers, float-float for FP32 walkers).
     static int batch_tables(const HostSys& hs, int prec, BatchRec& r) {
-        const SysW<double>* d;
-        int rc = table<double>(hs, &d);
-        if (rc) return rc;
-        r.tab_d = d;
-        r.tab_s = d;
         r.ktab = nullptr;
-        if (prec == 1) {
-            const SysW<float>* f;
-            rc = table<float>(hs, &f);
+        if (prec == 0) {
+            const SysW<double>* d;
+            int rc = table<double>(hs, &d);
             if (rc) return rc;
-            r.tab_s = f;
+            r.tab_d = r.tab_s = d;
+            return 0;
         }
+        const SysW<ff>* m;
+        const SysW<float>* f;
+        int rc = table<ff>(hs, &m);
+        if (!rc) rc = table<float>(hs, &f);
+        if (rc) return rc;
+        r.tab_d = m;
+        r.tab_s = f;
         return 0;
     }
 
@@ -817,10 +835,10 @@ struct WarpShapeOps {
         return 7;
     }
 
-    template <class TS>
+    template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = sizeof(double) * WPB * 5 * NM * 32;
-        auto kern = kwb_measure<NE, NUP, NNUC, TS, WPB>;
+        const size_t smem = sizeof(TC) * WPB * 5 * NM * 32;
+        auto kern = kwb_measure<NE, NUP, NNUC, TC, TS, WPB>;
         static bool attr = false;
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
@@ -833,7 +851,7 @@ struct WarpShapeOps {
     }
 
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
-        return bc.prec == 0 ? batch_measure_t<double>(bc, st, occ) : batch_measure_t<float>(bc, st, occ);
+        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_t<ff, float>(bc, st, occ);
     }
 
     static int sweep(const HostSys& hs, DevWalkers& dw, int mk, int n, uint64_t s0, double step, double tau,

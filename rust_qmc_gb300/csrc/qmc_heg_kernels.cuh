@@ -646,7 +646,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             }
             __syncwarp();
             constexpr int NPAIR = NE * (NE - 1) / 2, HALF = (NE - 1) / 2, FULL = NE * HALF;
-            const float Lf = (float)S.L, af = (float)S.alpha, rc2 = (float)S.rcut * (float)S.rcut;
+            const float aLf = (float)((double)S.alpha * (double)S.L);
+            const float rcu = (float)((double)S.rcut * (double)S.invL), rc2u = rcu * rcu;
             for (int p = lane; p < NPAIR; p += 32) {
                 int i, j;
                 if (p < FULL) {
@@ -662,21 +663,26 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 const double r = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
                 if (r > 1e-10) vreal += erfc((double)S.alpha * r) / r;
                 if (S.real_images) {
-                    const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+                    // box units: the image shift is an exact integer, alpha L is
+                    // exact in FP32 for the usual splittings, and sqrt and the
+                    // quotient are correctly rounded, so the rounding of each
+                    // term is unbiased; the sum is scaled by 1/L in FP64
+                    const float sx = (float)((double)dx * (double)S.invL), sy = (float)((double)dy * (double)S.invL),
+                                sz = (float)((double)dz * (double)S.invL);
                     float acc = 0.0f;
                     for (int ia = -1; ia <= 1; ++ia)
                         for (int ib = -1; ib <= 1; ++ib)
 #pragma unroll
                             for (int ic = -1; ic <= 1; ++ic) {
                                 if (!ia && !ib && !ic) continue;
-                                const float ex = fx + ia * Lf, ey = fy + ib * Lf, ez = fz + ic * Lf;
-                                const float d2 = ex * ex + ey * ey + ez * ez;
-                                if (d2 < rc2) {
-                                    const float d = sqrtf(d2);
-                                    acc += erfcf(af * d) / d;
+                                const float ex = sx + (float)ia, ey = sy + (float)ib, ez = sz + (float)ic;
+                                const float d2 = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+                                if (d2 < rc2u) {
+                                    const float d = __fsqrt_rn(d2);
+                                    acc += __fdiv_rn(erfcf(__fmul_rn(aLf, d)), d);
                                 }
                             }
-                    vreal += (double)acc;
+                    vreal += (double)acc * (double)S.invL;
                 }
             }
         }

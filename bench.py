@@ -354,7 +354,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (moves) + f64 (refresh, E_L)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (moves) + f64-class float-float (refresh, E_L)",
         "data": "synthetic (seeded CH4, QR-orthonormal MOs)",
         "config": {"workload": "CH4 9-AO single-electron VMC, FP32+refine", "walkers": W,
                    "sweeps_per_step": SW, "refresh_every": SW, "moves_per_step": moves_per_step,

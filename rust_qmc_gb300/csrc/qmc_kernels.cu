@@ -134,17 +134,32 @@ int launch_step_all_recorded(const HostSys& hs, DevWalkers& dw, int move_kind, i
 }
 
 // Final reduction of block partial pairs: out[j] = sum over blocks of
-// partial[j][b] (pairs (s,c)), one thread per row j, fixed order.
-__global__ void k_sum_partials(const double* __restrict__ partial, int nblk, int nrows, double* __restrict__ out) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
+// partial[j][b] (pairs (s,c)).  One block per row: a fixed-order strided pass over the row's compensated
+// block partials, then a fixed-order tree (deterministic for a given nblk).
+__global__ void __launch_bounds__(256) k_sum_partials(const double* __restrict__ partial, int nblk, int nrows,
+                                                      double* __restrict__ out) {
+    const int j = blockIdx.x, t = threadIdx.x;
     if (j >= nrows) return;
+    __shared__ double ss[256], sc[256];
     Comp acc{0.0, 0.0};
     const double* p = partial + (size_t)j * 2 * nblk;
-    for (int b = 0; b < nblk; ++b) {
+    for (int b = t; b < nblk; b += 256) {
         acc = comp_add(acc, Comp{p[2 * b], 0.0});
         acc.c += p[2 * b + 1];
     }
-    out[j] = acc.s + acc.c;
+    ss[t] = acc.s;
+    sc[t] = acc.c;
+    __syncthreads();
+#pragma unroll
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            Comp c = comp_add(Comp{ss[t], sc[t]}, Comp{ss[t + o], sc[t + o]});
+            ss[t] = c.s;
+            sc[t] = c.c;
+        }
+        __syncthreads();
+    }
+    if (t == 0) out[j] = ss[0] + sc[0];
 }
 
 // SR sums: quantity m over the walkers of chunk b, Neumaier-compensated,
@@ -336,7 +351,7 @@ int launch_batch_advance(BatchCtl* ctl, cudaStream_t st) {
 }
 
 int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st) {
-    k_sum_partials<<<(nrows + 127) / 128, 128, 0, st>>>(partial, nblk, nrows, out);
+    k_sum_partials<<<nrows, 256, 0, st>>>(partial, nblk, nrows, out);
     ++g_launch_count;
     return cuda_status(cudaGetLastError());
 }

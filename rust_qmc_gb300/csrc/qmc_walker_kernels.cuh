@@ -629,14 +629,14 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
     ff_store(out + (RL::J0 + 6) * st, V);
 }
 
-template <class SH, class TS, int SIG>
+// One spin sector (NS electrons, runtime sector index sig) of pass 2.
+template <class SH, class TS, int NS>
 __device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const float2* __restrict__ rows,
-                                                TS* __restrict__ dinv, int w, int wr, bool act, int Wcap,
+                                                TS* __restrict__ dinv, int SIG, int w, int wr, bool act, int Wcap,
                                                 int write_state, ff& pm, int& pe, int& sg, bool& ok, ff& kin,
                                                 ff& ut, ff& vt) {
     using RL = RowLayout<SH>;
     constexpr int NM = RL::NM;
-    constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
     if (NS == 0) return;
     constexpr int NSa = NS > 0 ? NS : 1;
     const size_t st = (size_t)Wcap;
@@ -687,8 +687,17 @@ __device__ __forceinline__ double assemble_walker(const SysT<SH, ff>& S, const f
     ff pm = ff(1.0f), kin = 0, ut = 0, vt = 0;
     int pe = 0, sg = 1;
     bool ok = true;
-    assemble_sector<SH, TS, 0>(S, rows, dinv, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
-    assemble_sector<SH, TS, 1>(S, rows, dinv, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+    if constexpr (SH::NUP == SH::NDN) {
+        // equal sectors share one copy of the sector code (a short
+        // instruction stream keeps the FP32 pipe fed from the cache)
+#pragma unroll 1
+        for (int sig = 0; sig < 2; ++sig)
+            assemble_sector<SH, TS, SH::NUP>(S, rows, dinv, sig, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin,
+                                             ut, vt);
+    } else {
+        assemble_sector<SH, TS, SH::NUP>(S, rows, dinv, 0, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+        assemble_sector<SH, TS, SH::NDN>(S, rows, dinv, 1, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+    }
     const double logdet = log((double)pm) + (double)pe * 0.6931471805599453;
     const double e_l = (double)(ff(-0.5f) * kin + vt + S.v_nn);
     if (!act) return 0.0;

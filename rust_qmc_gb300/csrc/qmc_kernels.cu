@@ -207,7 +207,7 @@ int launch_sr_sums(const double* E, const double* O, int W, int P, double* d_out
     if (tpb > 1024) return 1;
     k_sr_partials<<<nblk, tpb, 0, st>>>(E, O, W, P, M, chunk, d_scratch, nblk);
     ++g_launch_count;
-    k_sum_partials<<<(M + 127) / 128, 128, 0, st>>>(d_scratch, nblk, M, d_out);
+    k_sum_partials<<<M, 256, 0, st>>>(d_scratch, nblk, M, d_out);
     ++g_launch_count;
     return cuda_status(cudaGetLastError());
 }

@@ -117,25 +117,6 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def sweep_flops_per_move(n_prim, n_ao, acc_rate):
-    """Algorithmic FP32 operations of one single-electron Gaussian proposal of
-    the CH4 system (transcendentals counted as one operation):
-      RNG + Box-Muller + accept: 30
-      AO values: 8 per centre (dx,dy,dz,r^2) + 5 per primitive
-      MO contraction: 2 n_ao n;  ratio: 2 n
-      Jastrow old+new: 2 x 12 x (N-1 + N_nuc)
-      Sherman-Morrison on acceptance: 4 n^2 + n."""
-    n = N_UP
-    return (30 + 8 * N_NUC + 5 * n_prim + 2 * n_ao * n + 2 * n + 2 * 12 * (N_ELEC - 1 + N_NUC)
-            + acc_rate * (4 * n * n + n))
-
-
-def state_bytes_per_walker(sz):
-    """Walker state read and written once per sweep launch: positions, both
-    inverse Slater matrices and the sign."""
-    return 2 * ((3 * N_ELEC + 2 * N_UP * N_UP) * sz + 4)
-
-
 def cpu_baseline(spec, seconds, threads=1, walkers_hint=8):
     """Oracle (reference algorithm) single-electron sweeps on the host."""
     from oracle import oracle as O
@@ -326,13 +307,14 @@ def main():
     pin_el.free()
 
     # ---------------- roofline of the dominant kernel (the sweep) -------------
-    n_prim, n_ao = 18, 9
+    # algorithmic counts from the library's formulas (qmc_roofline_model)
+    counts = Q.roofline_model(spec, L.QMC_FP32_REFINE, acc_rate)
     launch_s = statistics.mean(sweep_ms) / 1e3
-    bytes_launch = W * state_bytes_per_walker(4)
+    bytes_launch = W * counts["sweep_state_bytes"]
     achieved_gbs = bytes_launch / launch_s / 1e9
     peak_hbm, peak_kind = measured_peak_hbm()
     fp32_peak, fp64_peak = ctx.measure_peaks()
-    flops_launch = moves_per_step * sweep_flops_per_move(n_prim, n_ao, acc_rate)
+    flops_launch = moves_per_step * counts["sweep_flops_per_move"]
     achieved_tf = flops_launch / launch_s / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_ch4_sweep.json")
@@ -349,7 +331,7 @@ def main():
     roofline_fp32 = {"bound": "fp32_simt", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak if fp32_peak else None,
                      "peak_source": "measured FMA-chain kernel on this GPU",
-                     "flops_per_move": sweep_flops_per_move(n_prim, n_ao, acc_rate)}
+                     "flops_per_move": counts["sweep_flops_per_move"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -279,6 +279,27 @@ int qmc_vmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed,
 int qmc_dmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed, qmc_run_result* result,
                 double* energies);
 
+/* ---- single-electron ratio (MultiWfn evaluate twice, src/sampling/vmc.rs:356-370) ---- */
+/* ratio[w] = psi(R_w with electron e at r_new[w]) / psi(R_w) for W
+ * configurations pos (W x n_elec x 3, caller order; e in caller order), and
+ * grad_ln_new[w] (may be NULL) = grad_e ln psi at the moved configuration,
+ * the drift of the reference's Langevin proposal.  FP64 evaluation. */
+int qmc_ratio_batch(qmc_sys_t sys, int W, const double* pos, int e, const double* r_new, double* ratio,
+                    double* grad_ln_new);
+
+/* ---- algorithmic counts (no reference counterpart; the benchmark's roofline) ---- */
+typedef struct {
+    double sweep_flops_per_move;  /* FP32 operations of one single-electron Gaussian proposal
+                                     (transcendentals count one) at the given acceptance */
+    double sweep_state_bytes;     /* walker state read + written by one sweep launch, per walker */
+    double refresh_flops;         /* FP64-class operations of one refresh, per walker */
+    double refresh_bytes;         /* HBM bytes of one refresh, per walker (state + two-pass scratch) */
+    double reserved[4];
+} qmc_roofline_counts;
+/* Host-only (no device needed): the counts for a system description and a
+ * walker precision. */
+int qmc_roofline_model(const qmc_system_desc* desc, int precision, double acceptance, qmc_roofline_counts* out);
+
 /* ---- uneven batches (no reference counterpart: rust_qmc runs one system
  * per process, src/main.rs) ---------------------------------------------------
  * A batch binds walker sets of one context -- any mix of systems, shapes,

@@ -48,6 +48,14 @@ class RunParams(C.Structure):
     ]
 
 
+class RooflineCounts(C.Structure):
+    """Mirror of ``qmc_roofline_counts``."""
+    _fields_ = [
+        ("sweep_flops_per_move", C.c_double), ("sweep_state_bytes", C.c_double),
+        ("refresh_flops", C.c_double), ("refresh_bytes", C.c_double), ("reserved", C.c_double * 4),
+    ]
+
+
 class RunResult(C.Structure):
     """Mirror of ``qmc_run_result``."""
     _fields_ = [
@@ -107,6 +115,8 @@ PROTOTYPES = {
     "qmc_host_alloc": [C.c_size_t, C.POINTER(_vp)],
     "qmc_host_free": [_vp],
     "qmc_sr_sums_noalloc": [_dp, _dp, C.c_int, C.c_int, _dp, _vp],
+    "qmc_ratio_batch": [_vp, C.c_int, _dp, C.c_int, _dp, _dp, _dp],
+    "qmc_roofline_model": [C.POINTER(SystemDesc), C.c_int, C.c_double, C.POINTER(RooflineCounts)],
     "qmc_batch_system_seed": [_u64, C.c_int],
     "qmc_batch_create": [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)],
     "qmc_batch_destroy": [_vp],

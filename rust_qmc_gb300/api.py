@@ -162,6 +162,17 @@ class System:
             return O, E, S, f, em.value
         return O, E
 
+    def ratio_batch(self, pos, e, r_new):
+        """psi(moved)/psi for electron e moved to r_new[w] in each configuration,
+        and grad_e ln psi at the moved configuration (qmc_ratio_batch)."""
+        pos = self._pos(pos)
+        W = pos.shape[0]
+        r_new = np.ascontiguousarray(r_new, dtype=np.float64).reshape(W, 3)
+        ratio, grad = np.zeros(W), np.zeros((W, 3))
+        L.check(self.lib.qmc_ratio_batch(self.h, W, _d(pos), int(e), _d(r_new), _d(ratio), _d(grad)),
+                "qmc_ratio_batch")
+        return ratio, grad
+
     def forces_batch(self, pos):
         pos = self._pos(pos)
         W = pos.shape[0]
@@ -349,6 +360,18 @@ class Batch:
         L.check(self.lib.qmc_batch_run_steps(self.h, move_kind, n_steps, sweeps_per_step, step0, step, tau,
                                              max_drift, seed, _d(e)), "qmc_batch_run_steps")
         return e
+
+
+def roofline_model(spec, precision=L.QMC_FP32_REFINE, acceptance=0.5):
+    """Algorithmic counts of the walker kernels for a system (qmc_roofline_model,
+    host only): sweep operations per proposal, sweep state bytes per walker and
+    launch, refresh operations and HBM bytes per walker."""
+    desc = spec.desc()
+    out = L.RooflineCounts()
+    L.check(L.load_library().qmc_roofline_model(C.byref(desc), precision, acceptance, C.byref(out)),
+            "qmc_roofline_model")
+    return dict(sweep_flops_per_move=out.sweep_flops_per_move, sweep_state_bytes=out.sweep_state_bytes,
+                refresh_flops=out.refresh_flops, refresh_bytes=out.refresh_bytes)
 
 
 def batch_system_seed(seed, i):

@@ -22,7 +22,7 @@ CU_SOURCES = ["qmc_kernels.cu", "qmc_shape_h2.cu", "qmc_shape_li.cu", "qmc_shape
               "qmc_shape_ch4min_sweep.cu", "qmc_shape_c6h6.cu", "qmc_shape_heg.cu",
               "qmc_shape_ch4_batch.cu", "qmc_shape_ch4min_batch.cu", "qmc_shape_c6h6_batch.cu",
               "qmc_shape_heg_batch.cu", "qmc_noalloc.cu"]
-CPP_SOURCES = ["qmc_api.cpp"]
+CPP_SOURCES = ["qmc_api.cpp", "qmc_roofline.cpp"]
 
 
 def _nvcc():

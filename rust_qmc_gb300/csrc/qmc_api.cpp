@@ -578,6 +578,22 @@ int qmc_system_check(const qmc_system_desc* desc, int* shape) {
     return rc;
 }
 
+int qmc_roofline_model(const qmc_system_desc* desc, int precision, double acceptance, qmc_roofline_counts* out) {
+    if (!desc || !out || (precision != QMC_FP64 && precision != QMC_FP32_REFINE) || !(acceptance >= 0) ||
+        acceptance > 1)
+        return QMC_ERR_ARG;
+    HostSys hs;
+    CK(build_hostsys(desc, hs));
+    double c[4];
+    roofline_counts(hs, precision == QMC_FP64 ? 0 : 1, acceptance, c);
+    std::memset(out, 0, sizeof(*out));
+    out->sweep_flops_per_move = c[0];
+    out->sweep_state_bytes = c[1];
+    out->refresh_flops = c[2];
+    out->refresh_bytes = c[3];
+    return QMC_OK;
+}
+
 int qmc_system_destroy(qmc_sys_t s) {
     if (!s || s->released) return QMC_ERR_ARG;
     if (s->n_children > 0) {
@@ -656,6 +672,26 @@ int qmc_eval_batch(qmc_sys_t s, int W, const double* pos, int precision, double*
     int fl = 0;
     CU(cudaMemcpy(&fl, wk->dw.flags, 4, cudaMemcpyDeviceToHost));
     CU(cudaMemset(wk->dw.flags, 0, 4));
+    return QMC_OK;
+}
+
+int qmc_ratio_batch(qmc_sys_t s, int W, const double* pos, int e, const double* r_new, double* ratio,
+                    double* grad_ln_new) {
+    if (!s || W <= 0 || !pos || !r_new || !ratio || e < 0 || e >= s->hs.N) return QMC_ERR_ARG;
+    const int N = s->hs.N;
+    std::vector<double> moved(pos, pos + (size_t)W * N * 3);
+    for (int w = 0; w < W; ++w)
+        for (int c = 0; c < 3; ++c) moved[((size_t)w * N + e) * 3 + c] = r_new[(size_t)w * 3 + c];
+    std::vector<double> l0(W), l1(W), g(grad_ln_new ? (size_t)W * N * 3 : 0);
+    std::vector<int> s0(W), s1(W);
+    CK(qmc_eval_batch(s, W, pos, QMC_FP64, l0.data(), s0.data(), nullptr, nullptr, nullptr));
+    CK(qmc_eval_batch(s, W, moved.data(), QMC_FP64, l1.data(), s1.data(), grad_ln_new ? g.data() : nullptr, nullptr,
+                      nullptr));
+    for (int w = 0; w < W; ++w) {
+        ratio[w] = (double)(s0[w] * s1[w]) * std::exp(l1[w] - l0[w]);
+        if (grad_ln_new)
+            for (int c = 0; c < 3; ++c) grad_ln_new[(size_t)w * 3 + c] = g[((size_t)w * N + e) * 3 + c];
+    }
     return QMC_OK;
 }
 

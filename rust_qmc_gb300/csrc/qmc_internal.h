@@ -209,6 +209,11 @@ int launch_batch_energy(const BatchClass& bc, const BatchCtl* ctl, double* serie
 // ctl->step += n_sweeps, ctl->row += 1 (one thread; ends a captured step).
 int launch_batch_advance(BatchCtl* ctl, cudaStream_t st);
 
+// Algorithmic counts of the walker kernels (qmc_roofline.cpp): [0] sweep
+// operations per proposal, [1] sweep state bytes per walker and launch,
+// [2] refresh operations per walker, [3] refresh HBM bytes per walker.
+void roofline_counts(const HostSys& hs, int prec, double acceptance, double out[4]);
+
 extern long long g_launch_count;
 
 }  // namespace qmc

@@ -106,3 +106,26 @@ def test_batch_system_seed_is_splitmix64(qmc_lib):
         keys = [Q.batch_system_seed(seed, i) for i in range(64)]
         assert keys == [splitmix(seed, i) for i in range(64)]
         assert len(set(keys)) == 64
+
+
+def test_roofline_model_counts(qmc_lib):
+    """Host-only algorithmic counts (qmc_roofline_model) for the 9-AO CH4
+    workload: 596 FP32 operations per proposal plus 105 per accepted move
+    (Sherman-Morrison), 648 bytes of FP32 walker state read and written per
+    sweep launch, and the two-pass refresh scratch in the refresh bytes."""
+    spec = Q.methane_minimal()
+    c = Q.roofline_model(spec, L.QMC_FP32_REFINE, 0.0)
+    assert c["sweep_flops_per_move"] == pytest.approx(596.0)
+    c = Q.roofline_model(spec, L.QMC_FP32_REFINE, 1.0)
+    assert c["sweep_flops_per_move"] == pytest.approx(701.0)
+    assert c["sweep_state_bytes"] == pytest.approx(2 * ((3 * 10 + 50) * 4 + 4))
+    rows = 2 * 8 * 10 * (5 * 5 + 7)
+    assert c["refresh_bytes"] == pytest.approx(3 * 10 * 4 + 50 * 4 + 20 + rows)
+    c64 = Q.roofline_model(spec, L.QMC_FP64, 0.5)
+    assert c64["sweep_state_bytes"] == pytest.approx(2 * ((3 * 10 + 50) * 8 + 4))
+    assert c64["refresh_bytes"] == pytest.approx(3 * 10 * 8 + 50 * 8 + 20)
+    for spec in (Q.h2_mo(), Q.lithium_atom(), Q.benzene_minimal(), Q.electron_gas()):
+        c = Q.roofline_model(spec, L.QMC_FP32_REFINE, 0.5)
+        assert all(v > 0 for v in c.values())
+    with pytest.raises(Q.QMCError):
+        Q.roofline_model(Q.methane_minimal(), L.QMC_FP32_REFINE, 1.5)

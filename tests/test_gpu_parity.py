@@ -441,3 +441,22 @@ def test_handles_release_in_any_order(qmc_lib):
     assert np.isfinite(e0) and np.isfinite(e1) and e1 != e0
     assert qmc_lib.qmc_walkers_destroy(wk.h) == L.QMC_OK
     wk.h = None
+
+
+@pytest.mark.parametrize("name", ["h2", "li_ref", "ch4_min"])
+def test_ratio_batch_matches_oracle(ctx, oracle, name):
+    """qmc_ratio_batch: psi ratio of a single-electron move and the drift at
+    the moved configuration, against the oracle's two evaluations (1e-10)."""
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 33, seed=11)
+    rng = np.random.default_rng(12)
+    for e in range(spec.n_elec):
+        r_new = cfg[:, e, :] + 0.3 * rng.standard_normal((cfg.shape[0], 3))
+        ratio, grad = sysh.ratio_batch(cfg, e, r_new)
+        moved = cfg.copy()
+        moved[:, e, :] = r_new
+        o0, o1 = oracle.evaluate(spec, cfg), oracle.evaluate(spec, moved)
+        want = o0["sign"] * o1["sign"] * np.exp(o1["logabs"] - o0["logabs"])
+        assert rel(ratio, want) < 1e-10
+        assert rel(grad, o1["grad"][:, e, :]) < 1e-10

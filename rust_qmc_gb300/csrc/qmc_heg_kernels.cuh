@@ -510,16 +510,22 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 Mi[q * 32 + lane] = s;
             }
             __syncwarp();
-            // complex Gauss-Jordan: lane j carries column j of [D | I]
-            TC Ar[NM], Ai[NM], Ir[NM], Ii[NM];
+            // complex Gauss-Jordan in place: lane j carries column j of D and
+            // ends with column j of D^-1.  Step k: pivot row p by |D[i][k]|,
+            // rows k and p interchanged; with a = D[k][k], row k is divided by
+            // a, column k becomes -D[i][k]/a (and 1/a on the diagonal), the rest
+            // loses D[i][k] x row k.  Lane k's own update is the same form with
+            // t = 1 + 1/a.  The row interchanges are undone at the end as column
+            // interchanges in reverse order: lane j gathers column src(j),
+            // src = tau_{n-1}( ... tau_0(j)), tau_k the swap of k and p_k.
+            TC Ar[NM], Ai[NM];
 #pragma unroll
             for (int i = 0; i < NM; ++i) {
                 bool in = i < NS && lane < NS;
                 Ar[i] = in ? Mr[i * 32 + lane] : TC(i == lane ? 1 : 0);
                 Ai[i] = in ? Mi[i * 32 + lane] : TC(0);
-                Ir[i] = (i == lane) ? TC(1) : TC(0);
-                Ii[i] = 0;
             }
+            int src = lane;
 #pragma unroll
             for (int k = 0; k < NM; ++k) {
                 if (k >= NS) break;
@@ -536,9 +542,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     bool sw = (i == p);
                     TC a = Ar[k], b = Ar[i]; Ar[k] = sw ? b : a; Ar[i] = sw ? a : b;
                     a = Ai[k]; b = Ai[i]; Ai[k] = sw ? b : a; Ai[i] = sw ? a : b;
-                    a = Ir[k]; b = Ir[i]; Ir[k] = sw ? b : a; Ir[i] = sw ? a : b;
-                    a = Ii[k]; b = Ii[i]; Ii[k] = sw ? b : a; Ii[i] = sw ? a : b;
                 }
+                src = (src == k) ? p : ((src == p) ? k : src);
                 TC pr = hshfl(Ar[k], k), pi = hshfl(Ai[k], k);
                 TC pa = pr * pr + pi * pi;
                 if (!(pa > TC(0))) { ok = false; pr = 1; pi = 0; pa = 1; }
@@ -548,18 +553,31 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 } else {
                     logdet += 0.5 * log((double)pa);
                 }
-                TC ipr = pr / pa, ipi = -pi / pa;
-                TC t;
-                t = Ar[k] * ipr - Ai[k] * ipi; Ai[k] = Ar[k] * ipi + Ai[k] * ipr; Ar[k] = t;
-                t = Ir[k] * ipr - Ii[k] * ipi; Ii[k] = Ir[k] * ipi + Ii[k] * ipr; Ir[k] = t;
+                const TC ipr = pr / pa, ipi = -pi / pa;           // 1/a
+                TC tr, ti;
+                if (lane == k) {
+                    tr = TC(1) + ipr; ti = ipi;
+                    Ar[k] = ipr; Ai[k] = ipi;
+                } else {
+                    tr = Ar[k] * ipr - Ai[k] * ipi; ti = Ar[k] * ipi + Ai[k] * ipr;
+                    Ar[k] = tr; Ai[k] = ti;
+                }
 #pragma unroll
                 for (int i = 0; i < NM; ++i) {
                     if (i == k || i >= NS) continue;
                     TC fr = hshfl(Ar[i], k), fi = hshfl(Ai[i], k);
-                    Ar[i] -= fr * Ar[k] - fi * Ai[k]; Ai[i] -= fr * Ai[k] + fi * Ar[k];
-                    Ir[i] -= fr * Ir[k] - fi * Ii[k]; Ii[i] -= fr * Ii[k] + fi * Ir[k];
+                    Ar[i] -= fr * tr - fi * ti; Ai[i] -= fr * ti + fi * tr;
                 }
             }
+            // unscramble: lane j takes column src(j)
+#pragma unroll
+            for (int i = 0; i < NM; ++i) {
+                if (i >= NS) break;
+                Ar[i] = hshfl(Ar[i], src);
+                Ai[i] = hshfl(Ai[i], src);
+            }
+            TC (&Ir)[NM] = Ar;
+            TC (&Ii)[NM] = Ai;
             if (write_state && lane < NS) {
 #pragma unroll
                 for (int k = 0; k < NM; ++k) {
@@ -797,7 +815,7 @@ __device__ __forceinline__ void hwarp_block_partial(double v, double* partial, i
 }
 
 template <int NE, int NUP, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
+__global__ void __launch_bounds__(32 * WPB, 2) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
                                                         const TS* __restrict__ gpos,
                                                         TS* __restrict__ gdinv, double* __restrict__ glog,
                                                         int* __restrict__ gsign, double* __restrict__ gel, int W,
@@ -817,7 +835,7 @@ __global__ void __launch_bounds__(32 * WPB) khw_measure(const SysH<TC>* __restri
 
 // Batched form (compute type TC, state written, per-tile E_L partials).
 template <int NE, int NUP, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
+__global__ void __launch_bounds__(32 * WPB, 2) khwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
                                                          const BatchRec* __restrict__ recs, double* tile_partial) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     extern __shared__ __align__(16) unsigned char hsm[];

@@ -254,7 +254,8 @@ int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cuda
     size_t ts = prec == QMC_FP64 ? 8 : 4;
     size_t nd = (size_t)dinv_elems_of_shape(hs.shape);
     size_t Wc = dw.Wcap;
-    int nblk = (int)((Wc + 63) / 64);
+    // block partials of the refresh: up to one block per 4 walkers (warp-per-walker shapes)
+    int nblk = (int)((Wc + 3) / 4);
     dw.partial_cap = 2 * nblk + 64;
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = cudaMalloc(&dw.pos, ts * 3 * hs.N * Wc);

@@ -460,3 +460,19 @@ def test_ratio_batch_matches_oracle(ctx, oracle, name):
         want = o0["sign"] * o1["sign"] * np.exp(o1["logabs"] - o0["logabs"])
         assert rel(ratio, want) < 1e-10
         assert rel(grad, o1["grad"][:, e, :]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["h2", "li_ref", "ch4_min", "c6h6", "heg"])
+def test_refresh_energy_sum_matches_walker_energies(ctx, name):
+    """The compensated E_L sum returned by a refresh equals the sum of the
+    per-walker energies, for every kernel family and enough walkers that the
+    warp-per-walker kernels launch hundreds of blocks."""
+    builders = dict(BUILDERS, c6h6=lambda: Q.benzene_minimal(), heg=lambda: Q.electron_gas())
+    sysh = Q.System(ctx, builders[name]())
+    for prec in (L.QMC_FP32_REFINE, L.QMC_FP64):
+        wk = Q.Walkers(sysh, 512, prec)
+        wk.init(seed=19)
+        e_sum, el = wk.refresh(want_energies=True)
+        assert np.all(np.isfinite(el))
+        assert abs(e_sum - el.sum()) <= 1e-12 * max(1.0, abs(el).sum())
+        wk.close()

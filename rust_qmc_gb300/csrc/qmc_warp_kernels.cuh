@@ -750,23 +750,68 @@ struct WarpShapeOps {
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
 
-    template <class TC, class TS>
-    static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
+    template <class TC, class TS, int WB>
+    static int measure_w(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
         const SysW<TC>* S;
         int rc = table<TC>(hs, &S);
         if (rc) return rc;
-        int nb = (dw.W + WPB - 1) / WPB;
-        size_t smem = sizeof(TC) * WPB * 5 * NM * 32;
-        auto kern = kw_measure<NE, NUP, NNUC, TC, TS, WPB>;
+        int nb = (dw.W + WB - 1) / WB;
+        size_t smem = sizeof(TC) * WB * 5 * NM * 32;
+        auto kern = kw_measure<NE, NUP, NNUC, TC, TS, WB>;
         static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
         double* partial = (ws && dw.partial && dw.partial_cap >= 2 * nb + 1) ? dw.partial : nullptr;
-        kern<<<nb, 32 * WPB, smem, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W, dw.Wcap,
-                                         ws ? 1 : 0, out.grad, out.lap, partial, dw.flags);
+        kern<<<nb, 32 * WB, smem, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W, dw.Wcap,
+                                        ws ? 1 : 0, out.grad, out.lap, partial, dw.flags);
         ++g_launch_count;
         if (cudaGetLastError() != cudaSuccess) return 2;
         if (!partial) return 0;
         return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
+    }
+
+    // Walkers per block of the standalone refresh, 4 or 7, chosen by timing.
+    // The row scratch is per warp and the system table per block, so 7
+    // walkers per block keep 7 warps per SM resident where 4 keep 4; which is
+    // faster depends on the arithmetic type.  A refresh recomputes the same
+    // state whatever the block shape, so the first refresh of at least 1024
+    // walkers per arithmetic type (outside stream capture) runs both shapes,
+    // times each once after a warm-up launch, and keeps the faster.
+    static constexpr int WB_A = 4, WB_B = 7;
+
+    template <class TC, class TS>
+    static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
+        static int best = 0;
+        if (best == 0) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if (dw.W < 1024 || cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+                return measure_w<TC, TS, WB_A>(hs, dw, ws, out, st);
+            cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+            int rc = 0;
+            for (auto& e : ev)
+                if (!rc && cudaEventCreate(&e) != cudaSuccess) rc = 2;
+            if (!rc) rc = measure_w<TC, TS, WB_A>(hs, dw, ws, out, st);
+            if (!rc) rc = measure_w<TC, TS, WB_B>(hs, dw, ws, out, st);
+            if (!rc && cudaEventRecord(ev[0], st) != cudaSuccess) rc = 2;
+            if (!rc) rc = measure_w<TC, TS, WB_A>(hs, dw, ws, out, st);
+            if (!rc && cudaEventRecord(ev[1], st) != cudaSuccess) rc = 2;
+            if (!rc) rc = measure_w<TC, TS, WB_B>(hs, dw, ws, out, st);
+            if (!rc && cudaEventRecord(ev[2], st) != cudaSuccess) rc = 2;
+            float ta = 0.0f, tb = 0.0f;
+            if (!rc && cudaEventSynchronize(ev[2]) != cudaSuccess) rc = 2;
+            if (!rc && (cudaEventElapsedTime(&ta, ev[0], ev[1]) != cudaSuccess ||
+                        cudaEventElapsedTime(&tb, ev[1], ev[2]) != cudaSuccess))
+                rc = 2;
+            for (auto e : ev)
+                if (e) cudaEventDestroy(e);
+            if (!rc) best = tb < ta ? WB_B : WB_A;
+            return rc;
+        }
+        return best == WB_B ? measure_w<TC, TS, WB_B>(hs, dw, ws, out, st)
+                            : measure_w<TC, TS, WB_A>(hs, dw, ws, out, st);
     }
 
     static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {

@@ -476,3 +476,21 @@ def test_refresh_energy_sum_matches_walker_energies(ctx, name):
         assert np.all(np.isfinite(el))
         assert abs(e_sum - el.sum()) <= 1e-12 * max(1.0, abs(el).sum())
         wk.close()
+
+
+@pytest.mark.parametrize("prec", [L.QMC_FP32_REFINE, L.QMC_FP64])
+def test_benzene_refresh_block_shapes_agree(ctx, prec):
+    """The benzene refresh picks 4 or 7 walkers per block by timing both on
+    its first call of 1024+ walkers; both shapes compute each walker alike,
+    so the walker state after the tuning call equals the state after a later
+    call with the chosen shape, bit for bit."""
+    sysh = Q.System(ctx, Q.benzene_minimal())
+    wk = Q.Walkers(sysh, 2048, prec)
+    wk.init(seed=23)
+    e1, el1 = wk.refresh(want_energies=True)
+    la1, sg1, _ = wk.state()
+    e2, el2 = wk.refresh(want_energies=True)
+    la2, sg2, _ = wk.state()
+    assert np.array_equal(el1, el2) and np.array_equal(la1, la2) and np.array_equal(sg1, sg2)
+    assert abs(e1 - e2) <= 1e-12 * abs(el1).sum()
+    assert abs(e2 - el2.sum()) <= 1e-12 * abs(el2).sum()

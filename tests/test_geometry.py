@@ -52,8 +52,7 @@ def test_mean_forces_match_reference_estimators(ctx, oracle, name):
 def test_stretched_h2_relaxes_inward(ctx):
     spec = Q.h2_mo()
     R0 = spec.nuc_pos.copy()
-    R0[:, 2] *= 1.4 / (R0[1, 2] - R0[0, 2])          # bond 1.4 bohr -> check ordering below
-    R0[:, 2] = [-0.9, 0.9]                             # stretched to 1.8 bohr
+    R0[:, 2] = [-0.9, 0.9]                             # bond stretched from 1.4 to 1.8 bohr
     sysh = Q.System(ctx, spec.with_nuclei(R0.reshape(-1)))
     res = G.optimize(sysh, n_samples=65536, n_walkers=8192, n_equilibrate=100, step_size=0.05, max_iterations=3,
                      force_threshold=1e-6, mc_step_size=0.5, estimator="zv", seed=3)

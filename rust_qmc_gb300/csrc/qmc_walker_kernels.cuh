@@ -206,6 +206,96 @@ __device__ __forceinline__ T jastrow_delta(const SysT<SH, T>& S, PosFn pos, int 
 }
 
 // ---------------------------------------------------------------------------
+// Electron-pair cache of the Gaussian single-electron sweep.  The sweep keeps
+// u(r_ij) of every pair i > j in shared memory (slot i (i - 1) / 2 + j), so a
+// proposal evaluates only the new pair terms of the moving electron; the old
+// ones are the cached values, which are bit-identical to a recomputation
+// (same expression on the same squared distance).
+// ---------------------------------------------------------------------------
+template <class SH, int MOVE>
+__host__ __device__ constexpr int sweep_pairs() {
+    return (MOVE == MOVE_ONE_GAUSS && SH::JAS != JAS_NONE) ? SH::NE * (SH::NE - 1) / 2 : 0;
+}
+// Shared-memory words per walker of the single-electron sweep: positions,
+// the two inverse Slater matrices, the pair cache.
+template <class SH, int MOVE>
+__host__ __device__ constexpr int sweep_words() {
+    return 3 * SH::NE + 2 * SH::NMAX * SH::NMAX + sweep_pairs<SH, MOVE>();
+}
+
+template <class T>
+__device__ __forceinline__ T sq3(T x, T y, T z) { return x * x + y * y + z * z; }
+
+// Electron-electron u of one pair at squared distance r2 > 0.
+template <class SH, class T>
+__device__ __forceinline__ T pair_u(const SysT<SH, T>& S, bool para, T r2) {
+    T d, ri, u, up, lt;
+    dist(r2, d, ri);
+    if (SH::JAS == JAS_PADE_F) pade_f(S.F, S.invF, d, ri, u, up, lt);
+    else pade_ab(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], d, ri, u, up, lt);
+    return u;
+}
+
+// Fill the pair cache pc (this thread's column, stride TPB) from positions.
+template <class SH, class T, int TPB, class PosFn>
+__device__ __forceinline__ void pair_cache_fill(const SysT<SH, T>& S, PosFn pos, T* pc) {
+#pragma unroll 1
+    for (int i = 1; i < SH::NE; ++i) {
+#pragma unroll 1
+        for (int j = 0; j < i; ++j) {
+            const bool para = (i < SH::NUP) == (j < SH::NUP);
+            T r2 = sq3(pos(i, 0) - pos(j, 0), pos(i, 1) - pos(j, 1), pos(i, 2) - pos(j, 2));
+            pc[(i * (i - 1) / 2 + j) * TPB] = pair_u<SH, T>(S, para, r2);
+        }
+    }
+}
+
+// Change of u when electron e moves from (ox,oy,oz) to (nx,ny,nz), with the
+// old pair terms read from the cache; un[j] receives the new pair terms.
+template <class SH, class T, int SIG, int TPB, class PosFn>
+__device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn pos, const T* pc, int e, T ox, T oy,
+                                                  T oz, T nx, T ny, T nz, T (&un)[SH::NE]) {
+    const int be = e * (e - 1) / 2;
+    T du = 0;
+#pragma unroll
+    for (int j = 0; j < SH::NE; ++j) {
+        const bool para = ((j < SH::NUP) == (SIG == 0));
+        const T m = (j != e) ? T(1) : T(0);
+        T rb = sq3(nx - pos(j, 0), ny - pos(j, 1), nz - pos(j, 2));
+        rb = (j != e) ? rb : T(1);
+        const T ub = pair_u<SH, T>(S, para, rb);
+        un[j] = ub;
+        const int slot = j < e ? be + j : (j > e ? j * (j - 1) / 2 + e : 0);
+        du += m * (ub - pc[slot * TPB]);
+    }
+    if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+        for (int I = 0; I < SH::NNUC; ++I) {
+            T da, ia, db, ib;
+            dist(sq3(ox - S.nuc[I][0], oy - S.nuc[I][1], oz - S.nuc[I][2]), da, ia);
+            dist(sq3(nx - S.nuc[I][0], ny - S.nuc[I][1], nz - S.nuc[I][2]), db, ib);
+            T ua, upa, lta, ub, upb, ltb;
+            pade_ab(S.enA[I], S.enB[I], da, ia, ua, upa, lta);
+            pade_ab(S.enA[I], S.enB[I], db, ib, ub, upb, ltb);
+            du -= ub - ua;
+        }
+    }
+    return du;
+}
+
+// Store the accepted move's pair terms un[j] (j != e) into the cache.
+template <class SH, class T, int TPB>
+__device__ __forceinline__ void pair_cache_store(T* pc, int e, const T (&un)[SH::NE]) {
+    const int be = e * (e - 1) / 2;
+#pragma unroll
+    for (int j = 0; j < SH::NE; ++j) {
+        if (j == e) continue;
+        const int slot = j < e ? be + j : j * (j - 1) / 2 + e;
+        pc[slot * TPB] = un[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Full evaluation of one configuration in precision TC.
 // ---------------------------------------------------------------------------
 template <class SH, class TC, int NR>
@@ -786,11 +876,12 @@ __global__ void __launch_bounds__(TPB) kb_assemble(const BatchTile* __restrict__
 // matrices [2][NMAX^2][TPB]; each thread only touches its own column, so no
 // barrier is needed.
 template <class SH, class T, int SIG, int MOVE, int TPB>
-__device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, int t, uint32_t w, uint64_t st,
-                                             uint64_t seed, T step, T tau, T maxd, int fixed_node, int& sgn,
-                                             unsigned& acc, int& flg) {
+__device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, T* pc, int t, uint32_t w,
+                                             uint64_t st, uint64_t seed, T step, T tau, T maxd, int fixed_node,
+                                             int& sgn, unsigned& acc, int& flg) {
     constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
     constexpr int NM = SH::NMAX;
+    constexpr bool PAIRS = sweep_pairs<SH, MOVE>() > 0;
     auto P = [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; };
 #define DI(k, j) sd[((SIG * NM * NM) + (k) * NM + (j)) * TPB + t]
     for (int q = 0; q < NS; ++q) {
@@ -801,6 +892,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
         const T n0 = md.n0, n1 = md.n1, n2 = md.n2;
         T nx, ny, nz, dlx = 0, dly = 0, dlz = 0;
         T logG = 0, R = 0, du;
+        T un[SH::NE];
         if (MOVE == MOVE_ONE_DRIFT) {
             // drift at the current position: grad ln D (from the current
             // inverse) + grad u; then the Langevin proposal
@@ -839,8 +931,12 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
             mn.run(S, nx, ny, nz);
 #pragma unroll
             for (int k = 0; k < NS; ++k) { R += mn.v[k] * DI(k, q); mv[k] = mn.v[k]; }
-            T g0[3], g1[3];
-            du = jastrow_delta<SH, T, SIG, false>(S, P, e, rx, ry, rz, nx, ny, nz, g0, g1);
+            if constexpr (PAIRS) {
+                du = jastrow_delta_cached<SH, T, SIG, TPB>(S, P, pc, e, rx, ry, rz, nx, ny, nz, un);
+            } else {
+                T g0[3], g1[3];
+                du = jastrow_delta<SH, T, SIG, false>(S, P, e, rx, ry, rz, nx, ny, nz, g0, g1);
+            }
         }
         T ratio = R * fexp(du);
         T prob = ratio * ratio;
@@ -865,6 +961,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
             }
 #pragma unroll
             for (int k = 0; k < NS; ++k) DI(k, q) = cq[k];
+            if constexpr (PAIRS) pair_cache_store<SH, T, TPB>(pc, e, un);
             if (R < 0) sgn = -sgn;
             ++acc;
         }
@@ -885,13 +982,18 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
     for (int i = 0; i < 3 * SH::NE; ++i) sp[i * TPB + t] = gpos[(size_t)i * Wcap + w];
 #pragma unroll
     for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = gdinv[(size_t)i * Wcap + w];
+    T* pc = sd + 2 * NM * NM * TPB + t;
+    if constexpr (sweep_pairs<SH, MOVE>() > 0)
+        pair_cache_fill<SH, T, TPB>(S, [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; }, pc);
     int sgn = gsign[w];
     unsigned acc = 0;
     int flg = 0;
     for (int it = 0; it < n_sweeps; ++it) {
         uint64_t st = step0 + (uint64_t)it;
-        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn, acc, flg);
-        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn, acc, flg);
+        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, pc, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn,
+                                          acc, flg);
+        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, pc, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn,
+                                          acc, flg);
     }
 #pragma unroll
     for (int i = 0; i < 3 * SH::NE; ++i) gpos[(size_t)i * Wcap + w] = sp[i * TPB + t];
@@ -1134,11 +1236,12 @@ struct ShapeOps {
         SysT<SH, T> S;
         if (!fill_sys(hs, S)) return 7;
         constexpr int TPB = 64;
-        size_t smem = sizeof(T) * TPB * (3 * SH::NE + 2 * SH::NMAX * SH::NMAX);
+        size_t smem = sizeof(T) * TPB * sweep_words<SH, MOVE>();
         auto kern = k_sweep_one<SH, T, MOVE, TPB>;
         static bool attr_set = false;
         if (!attr_set) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
             attr_set = true;
         }
         int nb = (dw.W + TPB - 1) / TPB;
@@ -1201,14 +1304,14 @@ struct ShapeOps {
         return 0;
     }
 
-    template <class T>
+    template <class T, int MOVE>
     static size_t batch_sweep_smem() {
-        return batch_table_bytes<SH, T>() + sizeof(T) * BTPB * (3 * SH::NE + 2 * SH::NMAX * SH::NMAX);
+        return batch_table_bytes<SH, T>() + sizeof(T) * BTPB * sweep_words<SH, MOVE>();
     }
 
     template <class T, int MOVE>
     static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
-        const size_t smem = batch_sweep_smem<T>();
+        const size_t smem = batch_sweep_smem<T, MOVE>();
         auto kern = kb_sweep_one<SH, T, MOVE, BTPB>;
         static bool attr = false;
         if (!attr) {

@@ -68,6 +68,7 @@ struct SysT {
     int sh_p0[SH::NSH], sh_np[SH::NSH];
     int sh_s0[SH::NSH], sh_s1[SH::NSH], sh_p[SH::NSH];
     T pexp[SH::NPRIM];
+    T pexp2[SH::NPRIM];             // -pexp log2(e): FP32 Gaussians as 2^(pexp2 r^2)
     T cs0[SH::NPRIM], cs1[SH::NPRIM], cp[SH::NPRIM];
     int ppow[SH::NPRIM];
     T C[2][SH::NAO][SH::NMAX];      // [sector][internal AO][column]
@@ -97,6 +98,12 @@ __device__ __forceinline__ double frcp(double x) {
     return fma(e, y, y);
 }
 __device__ __forceinline__ float frcp(float x) { return __fdividef(1.0f, x); }
+// 2^x by the PTX approximate base-2 exponential (flush-to-zero).
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and the stream layout of include/qmc.h.
@@ -182,6 +189,15 @@ __device__ __forceinline__ MoveDraw<T> move_draw(uint64_t seed, uint32_t walker,
 // (src/systems/methane.rs:498-590 for Gaussians, src/wavefunction/slater.rs:
 // 91-145 for Slater-type radial functions).
 // ---------------------------------------------------------------------------
+// Gaussian primitive p at squared distance r2: exp(-alpha r^2); FP32 uses
+// the pre-scaled exponent and one base-2 exponential.
+template <class SH, class T>
+__device__ __forceinline__ T gauss_prim(const SysT<SH, T>& S, int p, T r2) { return fexp(-S.pexp[p] * r2); }
+template <class SH>
+__device__ __forceinline__ float gauss_prim(const SysT<SH, float>& S, int p, float r2) {
+    return ex2_approx(S.pexp2[p] * r2);
+}
+
 template <class SH, class T, int SIG, int MODE, int NR>
 struct MOEval {
     static constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
@@ -231,7 +247,7 @@ struct MOEval {
 #pragma unroll
                 for (int p = p0; p < p0 + LY::np(sh); ++p) {
                     T al = S.pexp[p];
-                    T e = fexp(-al * r2);
+                    T e = gauss_prim(S, p, r2);
                     T e0 = S.cs0[p] * e;
                     a0 += e0;
                     if (MODE >= 1) b0 += al * e0;
@@ -263,7 +279,7 @@ struct MOEval {
                     T a0 = 0, a1 = 0, ap = 0, b0 = 0, b1 = 0, bp = 0, c0 = 0, c1 = 0, cpp = 0;
                     for (int p = p0; p < p1; ++p) {
                         T al = S.pexp[p];
-                        T e = fexp(-al * r2);
+                        T e = gauss_prim(S, p, r2);
                         T e0 = S.cs0[p] * e, e1 = S.cs1[p] * e, ep = S.cp[p] * e;
                         a0 += e0; a1 += e1; ap += ep;
                         if (MODE >= 1) { b0 += al * e0; b1 += al * e1; bp += al * ep; }

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <vector>
 #include <algorithm>
+#include <utility>
 #include "qmc_internal.h"
 #include "qmc_device.cuh"
 
@@ -61,6 +62,7 @@ static bool fill_sys(const HostSys& hs, SysT<SH, T>& S) {
         S.sh_p[s] = h.p_ao[0] >= 0 ? hs.ao_int[h.p_ao[0]] : -1;
         for (size_t p = 0; p < h.exps.size(); ++p) {
             S.pexp[np] = (T)h.exps[p];
+            S.pexp2[np] = (T)(-h.exps[p] * 1.4426950408889634);
             S.ppow[np] = h.pows.empty() ? 0 : h.pows[p];
             S.cs0[np] = h.s_ao[0] >= 0 ? (T)h.s_coef[0][p] : (T)0;
             S.cs1[np] = h.s_ao[1] >= 0 ? (T)h.s_coef[1][p] : (T)0;
@@ -210,11 +212,12 @@ __device__ __forceinline__ T jastrow_delta(const SysT<SH, T>& S, PosFn pos, int 
 // u(r_ij) of every pair i > j in shared memory (slot i (i - 1) / 2 + j), so a
 // proposal evaluates only the new pair terms of the moving electron; the old
 // ones are the cached values, which are bit-identical to a recomputation
-// (same expression on the same squared distance).
+// (same expression on the same squared distance).  One extra slot, held at
+// zero, is the in-bounds target of the masked self pair.
 // ---------------------------------------------------------------------------
 template <class SH, int MOVE>
 __host__ __device__ constexpr int sweep_pairs() {
-    return (MOVE == MOVE_ONE_GAUSS && SH::JAS != JAS_NONE) ? SH::NE * (SH::NE - 1) / 2 : 0;
+    return (MOVE == MOVE_ONE_GAUSS && SH::JAS != JAS_NONE) ? SH::NE * (SH::NE - 1) / 2 + 1 : 0;
 }
 // Shared-memory words per walker of the single-electron sweep: positions,
 // the two inverse Slater matrices, the pair cache.
@@ -226,14 +229,24 @@ __host__ __device__ constexpr int sweep_words() {
 template <class T>
 __device__ __forceinline__ T sq3(T x, T y, T z) { return x * x + y * y + z * z; }
 
-// Electron-electron u of one pair at squared distance r2 > 0.
+// 1/r from r^2; +inf at r = 0, so that a / (b + 1/r) gives the r -> 0 limit 0.
+__device__ __forceinline__ float inv_r(float r2) { return rsqrtf(r2); }
+__device__ __forceinline__ double inv_r(double r2) { return r2 > 0.0 ? frsqrt(r2) : (double)INFINITY; }
+
+// Pade a r / (1 + b r) evaluated as a / (b + 1/r).
+template <class T>
+__device__ __forceinline__ T pade_value(T a, T b, T r2) { return a * frcp(b + inv_r(r2)); }
+
+// Electron-electron u of one pair at squared distance r2.
 template <class SH, class T>
 __device__ __forceinline__ T pair_u(const SysT<SH, T>& S, bool para, T r2) {
-    T d, ri, u, up, lt;
-    dist(r2, d, ri);
-    if (SH::JAS == JAS_PADE_F) pade_f(S.F, S.invF, d, ri, u, up, lt);
-    else pade_ab(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], d, ri, u, up, lt);
-    return u;
+    if (SH::JAS == JAS_PADE_F) {
+        T d, ri, u, up, lt;
+        dist(r2, d, ri);
+        pade_f(S.F, S.invF, d, ri, u, up, lt);
+        return u;
+    }
+    return pade_value(S.a_ee[para ? 1 : 0], S.b_ee[para ? 1 : 0], r2);
 }
 
 // Fill the pair cache pc (this thread's column, stride TPB) from positions.
@@ -248,35 +261,55 @@ __device__ __forceinline__ void pair_cache_fill(const SysT<SH, T>& S, PosFn pos,
             pc[(i * (i - 1) / 2 + j) * TPB] = pair_u<SH, T>(S, para, r2);
         }
     }
+    pc[(SH::NE * (SH::NE - 1) / 2) * TPB] = T(0);
 }
 
-// Change of u when electron e moves from (ox,oy,oz) to (nx,ny,nz), with the
-// old pair terms read from the cache; un[j] receives the new pair terms.
+// Cache address of pair (e, j) for the moving electron e of sector SIG:
+// pa = slot row of e (pairs with j < e at pa[j]), pb = column e (pairs with
+// j > e at pb[j (j - 1) / 2]).  Partners of the other sector lie all below
+// (SIG 1) or all above (SIG 0) e, so only same-sector partners select at
+// run time; j == e lands on slot e (e + 1) / 2, a real pair or the zero slot.
+template <class SH, int SIG, int TPB, int J, class T>
+__device__ __forceinline__ T* pair_slot(T* pa, T* pb, int e) {
+    constexpr bool other = (J < SH::NUP) != (SIG == 0);
+    if (other) return SIG == 1 ? pa + J * TPB : pb + (J * (J - 1) / 2) * TPB;
+    return J < e ? pa + J * TPB : pb + (J * (J - 1) / 2) * TPB;
+}
+
+template <int J>
+struct IntC { static constexpr int value = J; };
+template <int N, class F, int... Is>
+__device__ __forceinline__ void unroll_impl(F&& f, std::integer_sequence<int, Is...>) { (f(IntC<Is>{}), ...); }
+// f(IntC<0>{}), ..., f(IntC<N-1>{}) with compile-time indices.
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) { unroll_impl<N>(f, std::make_integer_sequence<int, N>{}); }
+
+// Change of u when electron e of sector SIG moves from (ox,oy,oz) to
+// (nx,ny,nz), with the old pair terms read from the cache; un[j] receives
+// the new pair terms.
 template <class SH, class T, int SIG, int TPB, class PosFn>
-__device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn pos, const T* pc, int e, T ox, T oy,
-                                                  T oz, T nx, T ny, T nz, T (&un)[SH::NE]) {
-    const int be = e * (e - 1) / 2;
+__device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn pos, T* pc, int e, T ox, T oy, T oz,
+                                                  T nx, T ny, T nz, T (&un)[SH::NE]) {
+    T* pa = pc + (e * (e - 1) / 2) * TPB;
+    T* pb = pc + e * TPB;
     T du = 0;
-#pragma unroll
-    for (int j = 0; j < SH::NE; ++j) {
-        const bool para = ((j < SH::NUP) == (SIG == 0));
-        const T m = (j != e) ? T(1) : T(0);
+    static_for<SH::NE>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        constexpr bool other = (j < SH::NUP) != (SIG == 0);
+        const bool self = !other && j == e;
+        const bool para = !other;
         T rb = sq3(nx - pos(j, 0), ny - pos(j, 1), nz - pos(j, 2));
-        rb = (j != e) ? rb : T(1);
+        rb = self ? T(1) : rb;
         const T ub = pair_u<SH, T>(S, para, rb);
         un[j] = ub;
-        const int slot = j < e ? be + j : (j > e ? j * (j - 1) / 2 + e : 0);
-        du += m * (ub - pc[slot * TPB]);
-    }
+        const T ua = *pair_slot<SH, SIG, TPB, j>(pa, pb, e);
+        du += self ? T(0) : ub - ua;
+    });
     if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll
         for (int I = 0; I < SH::NNUC; ++I) {
-            T da, ia, db, ib;
-            dist(sq3(ox - S.nuc[I][0], oy - S.nuc[I][1], oz - S.nuc[I][2]), da, ia);
-            dist(sq3(nx - S.nuc[I][0], ny - S.nuc[I][1], nz - S.nuc[I][2]), db, ib);
-            T ua, upa, lta, ub, upb, ltb;
-            pade_ab(S.enA[I], S.enB[I], da, ia, ua, upa, lta);
-            pade_ab(S.enA[I], S.enB[I], db, ib, ub, upb, ltb);
+            const T ua = pade_value(S.enA[I], S.enB[I], sq3(ox - S.nuc[I][0], oy - S.nuc[I][1], oz - S.nuc[I][2]));
+            const T ub = pade_value(S.enA[I], S.enB[I], sq3(nx - S.nuc[I][0], ny - S.nuc[I][1], nz - S.nuc[I][2]));
             du -= ub - ua;
         }
     }
@@ -284,15 +317,15 @@ __device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn po
 }
 
 // Store the accepted move's pair terms un[j] (j != e) into the cache.
-template <class SH, class T, int TPB>
+template <class SH, class T, int SIG, int TPB>
 __device__ __forceinline__ void pair_cache_store(T* pc, int e, const T (&un)[SH::NE]) {
-    const int be = e * (e - 1) / 2;
-#pragma unroll
-    for (int j = 0; j < SH::NE; ++j) {
-        if (j == e) continue;
-        const int slot = j < e ? be + j : j * (j - 1) / 2 + e;
-        pc[slot * TPB] = un[j];
-    }
+    T* pa = pc + (e * (e - 1) / 2) * TPB;
+    T* pb = pc + e * TPB;
+    static_for<SH::NE>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        constexpr bool other = (j < SH::NUP) != (SIG == 0);
+        if (other || j != e) *pair_slot<SH, SIG, TPB, j>(pa, pb, e) = un[j];
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -961,7 +994,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
             }
 #pragma unroll
             for (int k = 0; k < NS; ++k) DI(k, q) = cq[k];
-            if constexpr (PAIRS) pair_cache_store<SH, T, TPB>(pc, e, un);
+            if constexpr (PAIRS) pair_cache_store<SH, T, SIG, TPB>(pc, e, un);
             if (R < 0) sgn = -sgn;
             ++acc;
         }

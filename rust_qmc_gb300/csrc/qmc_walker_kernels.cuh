@@ -284,12 +284,22 @@ __device__ __forceinline__ void unroll_impl(F&& f, std::integer_sequence<int, Is
 template <int N, class F>
 __device__ __forceinline__ void static_for(F&& f) { unroll_impl<N>(f, std::make_integer_sequence<int, N>{}); }
 
-// Change of u when electron e of sector SIG moves from (ox,oy,oz) to
-// (nx,ny,nz), with the old pair terms read from the cache; un[j] receives
-// the new pair terms.
+// One-body (electron-nucleus) part of u at one position, summed over nuclei.
+template <class SH, class T>
+__device__ __forceinline__ T one_body_u(const SysT<SH, T>& S, T x, T y, T z) {
+    T u = 0;
+#pragma unroll
+    for (int I = 0; I < SH::NNUC; ++I)
+        u += pade_value(S.enA[I], S.enB[I], sq3(x - S.nuc[I][0], y - S.nuc[I][1], z - S.nuc[I][2]));
+    return u;
+}
+
+// Change of u when electron e of sector SIG moves to (nx,ny,nz), with the
+// old pair terms read from the cache and the old one-body term u1_old;
+// un[j] receives the new pair terms, u1_new the new one-body term.
 template <class SH, class T, int SIG, int TPB, class PosFn>
-__device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn pos, T* pc, int e, T ox, T oy, T oz,
-                                                  T nx, T ny, T nz, T (&un)[SH::NE]) {
+__device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn pos, T* pc, int e, T u1_old, T nx,
+                                                  T ny, T nz, T (&un)[SH::NE], T& u1_new) {
     T* pa = pc + (e * (e - 1) / 2) * TPB;
     T* pb = pc + e * TPB;
     T du = 0;
@@ -306,12 +316,8 @@ __device__ __forceinline__ T jastrow_delta_cached(const SysT<SH, T>& S, PosFn po
         du += self ? T(0) : ub - ua;
     });
     if (SH::JAS == JAS_PADE_EEN) {
-#pragma unroll
-        for (int I = 0; I < SH::NNUC; ++I) {
-            const T ua = pade_value(S.enA[I], S.enB[I], sq3(ox - S.nuc[I][0], oy - S.nuc[I][1], oz - S.nuc[I][2]));
-            const T ub = pade_value(S.enA[I], S.enB[I], sq3(nx - S.nuc[I][0], ny - S.nuc[I][1], nz - S.nuc[I][2]));
-            du -= ub - ua;
-        }
+        u1_new = one_body_u(S, nx, ny, nz);
+        du -= u1_new - u1_old;
     }
     return du;
 }
@@ -909,7 +915,7 @@ __global__ void __launch_bounds__(TPB) kb_assemble(const BatchTile* __restrict__
 // matrices [2][NMAX^2][TPB]; each thread only touches its own column, so no
 // barrier is needed.
 template <class SH, class T, int SIG, int MOVE, int TPB>
-__device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, T* pc, int t, uint32_t w,
+__device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd, T* pc, T* u1c, int t, uint32_t w,
                                              uint64_t st, uint64_t seed, T step, T tau, T maxd, int fixed_node,
                                              int& sgn, unsigned& acc, int& flg) {
     constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
@@ -925,7 +931,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
         const T n0 = md.n0, n1 = md.n1, n2 = md.n2;
         T nx, ny, nz, dlx = 0, dly = 0, dlz = 0;
         T logG = 0, R = 0, du;
-        T un[SH::NE];
+        T un[SH::NE], u1n = 0;
         if (MOVE == MOVE_ONE_DRIFT) {
             // drift at the current position: grad ln D (from the current
             // inverse) + grad u; then the Langevin proposal
@@ -965,7 +971,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
 #pragma unroll
             for (int k = 0; k < NS; ++k) { R += mn.v[k] * DI(k, q); mv[k] = mn.v[k]; }
             if constexpr (PAIRS) {
-                du = jastrow_delta_cached<SH, T, SIG, TPB>(S, P, pc, e, rx, ry, rz, nx, ny, nz, un);
+                du = jastrow_delta_cached<SH, T, SIG, TPB>(S, P, pc, e, u1c[e], nx, ny, nz, un, u1n);
             } else {
                 T g0[3], g1[3];
                 du = jastrow_delta<SH, T, SIG, false>(S, P, e, rx, ry, rz, nx, ny, nz, g0, g1);
@@ -994,7 +1000,10 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
             }
 #pragma unroll
             for (int k = 0; k < NS; ++k) DI(k, q) = cq[k];
-            if constexpr (PAIRS) pair_cache_store<SH, T, SIG, TPB>(pc, e, un);
+            if constexpr (PAIRS) {
+                pair_cache_store<SH, T, SIG, TPB>(pc, e, un);
+                if (SH::JAS == JAS_PADE_EEN) u1c[e] = u1n;
+            }
             if (R < 0) sgn = -sgn;
             ++acc;
         }
@@ -1016,17 +1025,26 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
 #pragma unroll
     for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = gdinv[(size_t)i * Wcap + w];
     T* pc = sd + 2 * NM * NM * TPB + t;
-    if constexpr (sweep_pairs<SH, MOVE>() > 0)
+    // one-body terms of the electrons (thread-local; the pair cache fills the
+    // shared-memory budget of a walker)
+    T u1c[SH::NE];
+    if constexpr (sweep_pairs<SH, MOVE>() > 0) {
         pair_cache_fill<SH, T, TPB>(S, [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; }, pc);
+        if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll 1
+            for (int e = 0; e < SH::NE; ++e)
+                u1c[e] = one_body_u(S, sp[(3 * e) * TPB + t], sp[(3 * e + 1) * TPB + t], sp[(3 * e + 2) * TPB + t]);
+        }
+    }
     int sgn = gsign[w];
     unsigned acc = 0;
     int flg = 0;
     for (int it = 0; it < n_sweeps; ++it) {
         uint64_t st = step0 + (uint64_t)it;
-        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, pc, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn,
-                                          acc, flg);
-        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, pc, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node, sgn,
-                                          acc, flg);
+        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node,
+                                          sgn, acc, flg);
+        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node,
+                                          sgn, acc, flg);
     }
 #pragma unroll
     for (int i = 0; i < 3 * SH::NE; ++i) gpos[(size_t)i * Wcap + w] = sp[i * TPB + t];

@@ -689,24 +689,107 @@ struct RowLayout {
     static constexpr int J0 = 5 * NM;
 };
 
+// Values, gradients and Laplacians of the NM orbitals of sector sig at one
+// position, for Gaussian bases, with rolled loops over nuclei, shells,
+// primitives and AOs: a single copy of the AO -> MO contraction, so that the
+// instruction stream of the float-float refresh stays cache-resident.  The
+// AO formulas are MOEval's (src/systems/methane.rs:498-590).
+template <class SH>
+__device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int sig, ff x, ff y, ff z,
+                                                    ff (&v)[SH::NMAX], ff (&gx)[SH::NMAX], ff (&gy)[SH::NMAX],
+                                                    ff (&gz)[SH::NMAX], ff (&l)[SH::NMAX]) {
+    constexpr int NM = SH::NMAX;
+#pragma unroll
+    for (int k = 0; k < NM; ++k) { v[k] = 0; gx[k] = 0; gy[k] = 0; gz[k] = 0; l[k] = 0; }
+#pragma unroll 1
+    for (int I = 0; I < SH::NNUC; ++I) {
+        const ff dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+        const ff r2 = dx * dx + dy * dy + dz * dz;
+#pragma unroll 1
+        for (int sh = S.sh_start[I]; sh < S.sh_start[I + 1]; ++sh) {
+            const int p0 = S.sh_p0[sh], p1 = p0 + S.sh_np[sh];
+            ff a0 = 0, a1 = 0, ap = 0, b0 = 0, b1 = 0, bp = 0, c0 = 0, c1 = 0, cpp = 0;
+#pragma unroll 1
+            for (int p = p0; p < p1; ++p) {
+                const ff al = S.pexp[p];
+                const ff e = fexp(-al * r2);
+                const ff e0 = S.cs0[p] * e, e1 = S.cs1[p] * e, ep = S.cp[p] * e;
+                const ff a0e = al * e0, a1e = al * e1, ape = al * ep;
+                a0 += e0; a1 += e1; ap += ep;
+                b0 += a0e; b1 += a1e; bp += ape;
+                c0 += al * a0e; c1 += al * a1e; cpp += al * ape;
+            }
+            const int s0 = S.sh_s0[sh], s1 = S.sh_s1[sh], pa = S.sh_p[sh];
+            const ff lp = ff(-10.0f) * bp + ff(4.0f) * r2 * cpp;
+#pragma unroll 1
+            for (int m = 0; m < 5; ++m) {
+                const int a = m == 0 ? s0 : (m == 1 ? s1 : (pa >= 0 ? pa + m - 2 : -1));
+                if (a < 0) continue;
+                ff chi, ax, ay, az, la;
+                if (m < 2) {
+                    // s AO: chi = R0, grad = -2 R1 dr, lap = -6 R1 + 4 r^2 R2
+                    const ff A = m == 0 ? a0 : a1, B = m == 0 ? b0 : b1, C = m == 0 ? c0 : c1;
+                    const ff t = ff(-2.0f) * B;
+                    chi = A; ax = t * dx; ay = t * dy; az = t * dz;
+                    la = ff(-6.0f) * B + ff(4.0f) * r2 * C;
+                } else {
+                    // p AO along axis m - 2: chi = x_m R(r), grad = x_m (-2 R1 dr) + e_m R0,
+                    // lap = x_m (-10 R1 + 4 r^2 R2)
+                    const ff xm = m == 2 ? dx : (m == 3 ? dy : dz);
+                    const ff t = ff(-2.0f) * bp * xm;
+                    chi = xm * ap;
+                    ax = t * dx + (m == 2 ? ap : ff(0.0f));
+                    ay = t * dy + (m == 3 ? ap : ff(0.0f));
+                    az = t * dz + (m == 4 ? ap : ff(0.0f));
+                    la = xm * lp;
+                }
+#pragma unroll
+                for (int k = 0; k < NM; ++k) {
+                    const ff c = S.C[sig][a][k];
+                    v[k] += c * chi; gx[k] += c * ax; gy[k] += c * ay; gz[k] += c * az; l[k] += c * la;
+                }
+            }
+        }
+    }
+}
+
 template <class SH, class TS, int SIG>
+__device__ __forceinline__ void rows_orbitals(const SysT<SH, ff>& S, int sig, ff x, ff y, ff z, ff (&v)[SH::NMAX],
+                                              ff (&gx)[SH::NMAX], ff (&gy)[SH::NMAX], ff (&gz)[SH::NMAX],
+                                              ff (&l)[SH::NMAX]) {
+    MOEval<SH, ff, SIG, 2, 0> m;
+    m.run(S, x, y, z);
+#pragma unroll
+    for (int k = 0; k < SH::NMAX; ++k) { v[k] = m.v[k]; gx[k] = m.gx[k]; gy[k] = m.gy[k]; gz[k] = m.gz[k]; l[k] = m.l[k]; }
+}
+
+// Pass 1 for electron e (sector sig) of walker w.
+template <class SH, class TS>
 __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* __restrict__ pos,
                                              float2* __restrict__ rows, int e, int w, int Wcap) {
     using RL = RowLayout<SH>;
     constexpr int NM = RL::NM;
     const size_t st = (size_t)Wcap;
+    const int sig = e < SH::NUP ? 0 : 1;
     float2* out = rows + (size_t)e * RL::QN * st + w;
     const ff x = ff((float)pos[(3 * e + 0) * st + w]), y = ff((float)pos[(3 * e + 1) * st + w]),
              z = ff((float)pos[(3 * e + 2) * st + w]);
-    MOEval<SH, ff, SIG, 2, 0> m;
-    m.run(S, x, y, z);
+    {
+        ff v[NM], ogx[NM], ogy[NM], ogz[NM], ol[NM];
+        if constexpr (SH::BASIS == BASIS_GTO) {
+            orbitals_gto_rolled<SH>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
+        } else {
+            if (sig == 0) rows_orbitals<SH, TS, 0>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
+            else rows_orbitals<SH, TS, 1>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
+        }
 #pragma unroll
-    for (int k = 0; k < NM; ++k) {
-        ff_store(out + (0 * NM + k) * st, m.v[k]);
-        ff_store(out + (1 * NM + k) * st, m.gx[k]);
-        ff_store(out + (2 * NM + k) * st, m.gy[k]);
-        ff_store(out + (3 * NM + k) * st, m.gz[k]);
-        ff_store(out + (4 * NM + k) * st, m.l[k]);
+        for (int k = 0; k < NM; ++k) {
+            ff_store(out + (0 * NM + k) * st, v[k]);
+            ff_store(out + (1 * NM + k) * st, ogx[k]);
+            ff_store(out + (2 * NM + k) * st, ogy[k]);
+            ff_store(out + (3 * NM + k) * st, ogz[k]);
+            ff_store(out + (4 * NM + k) * st, ol[k]);
+        }
     }
     ff gx = 0, gy = 0, gz = 0, lu = 0, gsq = 0, u = 0, V = 0;
 #pragma unroll 1
@@ -734,7 +817,7 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
             gsq += up * up;
         }
     }
-#pragma unroll
+#pragma unroll 1
     for (int I = 0; I < SH::NNUC; ++I) {
         const ff dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
         ff d, ri;
@@ -844,8 +927,7 @@ __global__ void __launch_bounds__(128) k_rows(const __grid_constant__ SysT<SH, f
     const int w = blockIdx.x * 128 + threadIdx.x;
     const int e = blockIdx.y;
     if (w >= W) return;
-    if (e < SH::NUP) rows_electron<SH, TS, 0>(S, pos, rows, e, w, Wcap);
-    else rows_electron<SH, TS, 1>(S, pos, rows, e, w, Wcap);
+    rows_electron<SH, TS>(S, pos, rows, e, w, Wcap);
 }
 
 template <class SH, class TS, int TPB>
@@ -880,10 +962,7 @@ __global__ void __launch_bounds__(TPB) kb_rows(const BatchTile* __restrict__ til
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + (int)threadIdx.x;
-        if (w < R.W) {
-            if (e < SH::NUP) rows_electron<SH, TS, 0>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
-            else rows_electron<SH, TS, 1>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
-        }
+        if (w < R.W) rows_electron<SH, TS>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
     }
 }
 

@@ -16,8 +16,9 @@
 // FMA-based product of Dekker's paper, as collected in the double-double
 // algorithms of Hida, Li & Bailey (QD library, ARITH-15, 2001).  Division,
 // reciprocal and square roots take one Newton correction from the FP32
-// hardware seed; exp uses a Cody-Waite reduction by ln 2, a 2^-5 scaling,
-// a degree-6 Taylor polynomial and five squarings.  Every intrinsic below is
+// hardware seed; exp is table-driven (Tang, ACM TOMS 15 (1989)): a
+// Cody-Waite reduction by ln2/32, a 32-entry table of 2^(j/32) and a short
+// polynomial, with relative error ~1e-13.  Every intrinsic below is
 // an IEEE round-to-nearest FP32 operation (__fadd_rn etc.), which the
 // compiler neither contracts nor reassociates.
 #pragma once
@@ -79,6 +80,21 @@ __device__ __forceinline__ ff operator/(ff a, ff b) {
     const float q2 = __fmul_rn(r.hi, x);
     return ff_fast_two_sum(q1, q2);
 }
+// acc += c x without renormalising (a Dot2 step, Ogita, Rump & Oishi, SIAM J.
+// Sci. Comput. 26 (2005)): the leading parts are summed error-free and every
+// error term gathers in acc.lo; ff_norm(acc) after the last step gives a
+// float pair as accurate as a float-float dot product.
+__device__ __forceinline__ void ff_fma_lazy(ff& acc, ff c, ff x) {
+    const float p = __fmul_rn(c.hi, x.hi);
+    float pe = __fmaf_rn(c.hi, x.hi, -p);
+    pe = __fmaf_rn(c.hi, x.lo, pe);
+    pe = __fmaf_rn(c.lo, x.hi, pe);
+    const ff s = ff_two_sum(acc.hi, p);
+    acc.hi = s.hi;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, pe));
+}
+__device__ __forceinline__ ff ff_norm(ff a) { return ff_fast_two_sum(a.hi, a.lo); }
+
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
 __device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }
@@ -120,33 +136,42 @@ __device__ __forceinline__ ff frsqrt<ff>(ff a) {
 }
 
 // ---- exponential ----------------------------------------------------------------
-// Cody-Waite reduction a = n ln2 + r with ln2 carried as a float pair,
-// r scaled by 2^-5 (|r| <= 0.0109), e^r by the degree-6 Taylor series
-// (truncation < 4e-18), then squared five times and scaled by 2^n.
+// Table-driven (Tang 1989): a = (32 k + j) ln2/32 + r with |r| <= ln2/64,
+// ln2/32 carried as a float pair; e^a = 2^k 2^(j/32) e^r.  e^r = 1 + r +
+// r^2/2 + tail: r^2/2 as a float pair, tail = r^3/6 + r^4/24 + r^5/120 in
+// FP32 (|tail| < 2e-7, so its rounding is below 2^-46); the truncated r^6/720
+// is < 2e-15.  The table entries are 2^(j/32) rounded to float pairs.
 // Arguments below -87 underflow FP32 and return 0.
+__device__ const ff kExp2Frac[32] = {
+    ff(1.0), ff(1.0218971486541166), ff(1.0442737824274138), ff(1.0671404006768237),
+    ff(1.0905077326652577), ff(1.1143867425958924), ff(1.1387886347566916), ff(1.1637248587775775),
+    ff(1.189207115002721), ff(1.215247359980469), ff(1.241857812073484), ff(1.2690509571917332),
+    ff(1.2968395546510096), ff(1.3252366431597413), ff(1.3542555469368927), ff(1.383909881963832),
+    ff(1.4142135623730951), ff(1.4451808069770467), ff(1.4768261459394993), ff(1.5091644275934228),
+    ff(1.5422108254079407), ff(1.5759808451078865), ff(1.6104903319492543), ff(1.6457554781539649),
+    ff(1.681792830507429), ff(1.7186192981224779), ff(1.7562521603732995), ff(1.7947090750031072),
+    ff(1.8340080864093424), ff(1.8741676341103), ff(1.9152065613971474), ff(1.9571441241754002),
+};
+
 __device__ __forceinline__ ff fexp(ff a) {
     if (a.hi < -87.0f) return ff(0.0f);
-    constexpr double LN2 = 0.6931471805599453094172321;
-    constexpr ff ln2 = ff(LN2);
-    const float nf = rintf(__fmul_rn(a.hi, 1.44269504088896341f));
-    const ff ln2n = ff_fast_two_sum(__fmul_rn(ln2.hi, nf), __fmaf_rn(ln2.hi, nf, -__fmul_rn(ln2.hi, nf)) +
-                                                           __fmul_rn(ln2.lo, nf));
-    ff r = a - ln2n;
-    r = ff(__fmul_rn(r.hi, 0.03125f), __fmul_rn(r.lo, 0.03125f));
-    // Horner: 1 + r (1 + r/2 (1 + r/3 (1 + r/4 (1 + r/5 (1 + r/6)))))
-    constexpr ff c6 = ff(1.0 / 720.0), c5 = ff(1.0 / 120.0), c4 = ff(1.0 / 24.0), c3 = ff(1.0 / 6.0);
-    ff p = c6;
-    p = p * r + c5;
-    p = p * r + c4;
-    p = p * r + c3;
-    p = p * r + ff(0.5f);
-    p = p * r + ff(1.0f);
-    p = p * r + ff(1.0f);
-#pragma unroll
-    for (int i = 0; i < 5; ++i) p = p * p;
+    constexpr ff ln2_32 = ff(0.02166084939249829);          // ln(2) / 32
+    const float nf = rintf(__fmul_rn(a.hi, 46.166241308446828f));
+    const ff p = ff_two_prod(ln2_32.hi, nf);
+    const ff t = ff_fast_two_sum(p.hi, __fmaf_rn(ln2_32.lo, nf, p.lo));
+    const ff r = a - t;
+    // r^2 / 2 (unnormalised pair) and the FP32 tail r^3 (1/6 + r/24 + r^2/120)
+    const ff q = ff_two_prod(r.hi, r.hi);
+    const ff h = ff(__fmul_rn(q.hi, 0.5f), __fmul_rn(__fmaf_rn(2.0f * r.hi, r.lo, q.lo), 0.5f));
+    const float poly = __fmaf_rn(r.hi, __fmaf_rn(r.hi, 1.0f / 60.0f, 1.0f / 12.0f), 1.0f / 3.0f);
+    const float tail = __fmul_rn(__fmul_rn(h.hi, r.hi), poly);
+    ff s = h + ff(tail);
+    s = r + s;
+    s = ff(1.0f) + s;
     const int n = (int)nf;
-    const float s = __int_as_float((n + 127) << 23);   // 2^n, n in [-126, 127]
-    return ff(__fmul_rn(p.hi, s), __fmul_rn(p.lo, s));
+    const ff m = s * kExp2Frac[n & 31];
+    const float sc = __int_as_float(((n >> 5) + 127) << 23);   // 2^k, k in [-126, 127]
+    return ff(__fmul_rn(m.hi, sc), __fmul_rn(m.lo, sc));
 }
 
 // A running product kept as mantissa * 2^e: the mantissa is brought back to

@@ -708,18 +708,23 @@ __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int s
 #pragma unroll 1
         for (int sh = S.sh_start[I]; sh < S.sh_start[I + 1]; ++sh) {
             const int p0 = S.sh_p0[sh], p1 = p0 + S.sh_np[sh];
+            const int s0 = S.sh_s0[sh], s1 = S.sh_s1[sh], pa = S.sh_p[sh];
+            // radial sums R0 = sum c e, R1 = sum c al e, R2 = sum c al^2 e of
+            // the shell's s0, s1 and p coefficient sets (warp-uniform skips
+            // of the sets a shell does not have)
             ff a0 = 0, a1 = 0, ap = 0, b0 = 0, b1 = 0, bp = 0, c0 = 0, c1 = 0, cpp = 0;
 #pragma unroll 1
             for (int p = p0; p < p1; ++p) {
                 const ff al = S.pexp[p];
                 const ff e = fexp(-al * r2);
-                const ff e0 = S.cs0[p] * e, e1 = S.cs1[p] * e, ep = S.cp[p] * e;
-                const ff a0e = al * e0, a1e = al * e1, ape = al * ep;
-                a0 += e0; a1 += e1; ap += ep;
-                b0 += a0e; b1 += a1e; bp += ape;
-                c0 += al * a0e; c1 += al * a1e; cpp += al * ape;
+                const ff ea = al * e, eaa = al * ea;
+                if (s0 >= 0) { ff_fma_lazy(a0, S.cs0[p], e); ff_fma_lazy(b0, S.cs0[p], ea); ff_fma_lazy(c0, S.cs0[p], eaa); }
+                if (s1 >= 0) { ff_fma_lazy(a1, S.cs1[p], e); ff_fma_lazy(b1, S.cs1[p], ea); ff_fma_lazy(c1, S.cs1[p], eaa); }
+                if (pa >= 0) { ff_fma_lazy(ap, S.cp[p], e); ff_fma_lazy(bp, S.cp[p], ea); ff_fma_lazy(cpp, S.cp[p], eaa); }
             }
-            const int s0 = S.sh_s0[sh], s1 = S.sh_s1[sh], pa = S.sh_p[sh];
+            a0 = ff_norm(a0); b0 = ff_norm(b0); c0 = ff_norm(c0);
+            a1 = ff_norm(a1); b1 = ff_norm(b1); c1 = ff_norm(c1);
+            ap = ff_norm(ap); bp = ff_norm(bp); cpp = ff_norm(cpp);
             const ff lp = ff(-10.0f) * bp + ff(4.0f) * r2 * cpp;
 #pragma unroll 1
             for (int m = 0; m < 5; ++m) {
@@ -746,10 +751,19 @@ __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int s
 #pragma unroll
                 for (int k = 0; k < NM; ++k) {
                     const ff c = S.C[sig][a][k];
-                    v[k] += c * chi; gx[k] += c * ax; gy[k] += c * ay; gz[k] += c * az; l[k] += c * la;
+                    ff_fma_lazy(v[k], c, chi);
+                    ff_fma_lazy(gx[k], c, ax);
+                    ff_fma_lazy(gy[k], c, ay);
+                    ff_fma_lazy(gz[k], c, az);
+                    ff_fma_lazy(l[k], c, la);
                 }
             }
         }
+    }
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        v[k] = ff_norm(v[k]); gx[k] = ff_norm(gx[k]); gy[k] = ff_norm(gy[k]); gz[k] = ff_norm(gz[k]);
+        l[k] = ff_norm(l[k]);
     }
 }
 

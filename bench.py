@@ -12,8 +12,9 @@ the plain FP64 form runs the same schedule with FP64 walkers.
 value  = walker-moves/s with walker state resident in HBM, timed by CUDA
          events around each step (L2 flushed between steps, outside timing)
 e2e    = same metric through the C ABI with host buffers: every step uploads
-         the walkers' positions from pinned host memory and reads back the
-         E_L of every walker.
+         the walkers' positions from pinned host memory, rebuilds their
+         inverse Slater matrices (qmc_walkers_rebuild_inverse), sweeps, and
+         reads back the refreshed E_L of every walker.
 --impl reference times the oracle's restatement of the reference algorithm
 (full re-evaluation of psi per proposal) on the host cores.
 """
@@ -292,7 +293,7 @@ def main():
         ctx.synchronize()
         t0 = time.perf_counter()
         wk_e2e.set_positions_ptr(pin_pos.ptr)          # H2D of the step's configurations
-        wk_e2e.refresh_async()                          # FP64 inverse for the uploaded walkers
+        wk_e2e.rebuild_inverse()                        # FP64 inverse and log|psi| of the uploaded walkers
         wk_e2e.sweep(L.QMC_MOVE_ONE_GAUSS, SW, 10 ** 6 + i * SW, seed, step=args.step_size, count=False)
         L.check(ctx.lib.qmc_walkers_refresh(wk_e2e.h, el_ptr, None), "qmc_walkers_refresh")  # D2H E_L
         t1 = time.perf_counter()

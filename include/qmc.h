@@ -229,6 +229,11 @@ int qmc_walkers_get_positions(qmc_walkers_t wk, double* pos);
  * positions, plus the FP64 local energy.  e_local [W] may be NULL (kept on
  * the device); e_sum receives the FP64 compensated sum (may be NULL). */
 int qmc_walkers_refresh(qmc_walkers_t wk, double* e_local, double* e_sum);
+/* FP64 rebuild of the inverse Slater matrices, sign and log|psi| only: the
+ * state a sweep needs after qmc_walkers_set_positions (the reference's
+ * DDWalkerState::refresh, src/sampling/vmc.rs:243-276, without the drift).  The
+ * stored E_L values are unspecified until the next qmc_walkers_refresh. */
+int qmc_walkers_rebuild_inverse(qmc_walkers_t wk);
 /* n_sweeps Monte Carlo steps for all walkers (one launch):
  * src/sampling/vmc.rs:95-119 (all-electron), :339-394 (single-electron).
  * Sweep indices step0 .. step0+n_sweeps-1 key the random stream.

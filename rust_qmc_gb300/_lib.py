@@ -96,6 +96,7 @@ PROTOTYPES = {
     "qmc_walkers_set_positions": [_vp, _dp],
     "qmc_walkers_get_positions": [_vp, _dp],
     "qmc_walkers_refresh": [_vp, _dp, _dp],
+    "qmc_walkers_rebuild_inverse": [_vp],
     "qmc_walkers_sweep": [_vp, C.c_int, C.c_int, _u64, C.c_double, C.c_double, C.c_double, _u64,
                           C.POINTER(C.c_longlong)],
     "qmc_walkers_get_state": [_vp, _dp, _ip, _dp],

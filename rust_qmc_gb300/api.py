@@ -287,6 +287,11 @@ class Walkers:
     def refresh_async(self):
         L.check(self.lib.qmc_walkers_refresh(self.h, None, None), "qmc_walkers_refresh")
 
+    def rebuild_inverse(self):
+        """Inverse Slater matrices, sign and log|psi| from the current
+        positions, without E_L (asynchronous on the context stream)."""
+        L.check(self.lib.qmc_walkers_rebuild_inverse(self.h), "qmc_walkers_rebuild_inverse")
+
     def sweep(self, move_kind, n_sweeps, step0, seed, step=0.3, tau=0.01, max_drift=1.0, count=True):
         acc = C.c_longlong()
         L.check(self.lib.qmc_walkers_sweep(self.h, move_kind, n_sweeps, step0, step, tau, max_drift, seed,

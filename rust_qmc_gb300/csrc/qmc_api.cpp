@@ -848,6 +848,15 @@ int qmc_walkers_refresh(qmc_walkers_t wk, double* e_local, double* e_sum) {
     return QMC_OK;
 }
 
+int qmc_walkers_rebuild_inverse(qmc_walkers_t wk) {
+    if (!wk) return QMC_ERR_ARG;
+    cudaSetDevice(wk->sys->ctx->device);
+    MeasureOut mo;
+    mo.inverse_only = true;
+    CK(launch_measure(wk->sys->hs, wk->dw, 0, true, mo, wk->sys->ctx->stream));
+    return QMC_OK;
+}
+
 int qmc_walkers_sweep(qmc_walkers_t wk, int move_kind, int n_sweeps, uint64_t step0, double step, double tau,
                       double max_drift, uint64_t seed, long long* accepted) {
     if (!wk || n_sweeps < 0 || move_kind < 0 || move_kind > 3) return QMC_ERR_ARG;

@@ -95,6 +95,8 @@ struct MeasureOut {
     double* O = nullptr;                 // [W][P]
     double* fhf = nullptr;               // [W][n_nuc][3]
     double* omega = nullptr;             // [W][n_nuc][3]
+    // only the inverse, sign and log|psi| are wanted (E_L may be skipped)
+    bool inverse_only = false;
 };
 
 int nmax_of_shape(int shape);

@@ -694,7 +694,7 @@ struct RowLayout {
 // primitives and AOs: a single copy of the AO -> MO contraction, so that the
 // instruction stream of the float-float refresh stays cache-resident.  The
 // AO formulas are MOEval's (src/systems/methane.rs:498-590).
-template <class SH>
+template <class SH, int MODE>
 __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int sig, ff x, ff y, ff z,
                                                     ff (&v)[SH::NMAX], ff (&gx)[SH::NMAX], ff (&gy)[SH::NMAX],
                                                     ff (&gz)[SH::NMAX], ff (&l)[SH::NMAX]) {
@@ -717,10 +717,15 @@ __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int s
             for (int p = p0; p < p1; ++p) {
                 const ff al = S.pexp[p];
                 const ff e = fexp(-al * r2);
-                const ff ea = al * e, eaa = al * ea;
-                if (s0 >= 0) { ff_fma_lazy(a0, S.cs0[p], e); ff_fma_lazy(b0, S.cs0[p], ea); ff_fma_lazy(c0, S.cs0[p], eaa); }
-                if (s1 >= 0) { ff_fma_lazy(a1, S.cs1[p], e); ff_fma_lazy(b1, S.cs1[p], ea); ff_fma_lazy(c1, S.cs1[p], eaa); }
-                if (pa >= 0) { ff_fma_lazy(ap, S.cp[p], e); ff_fma_lazy(bp, S.cp[p], ea); ff_fma_lazy(cpp, S.cp[p], eaa); }
+                if (s0 >= 0) ff_fma_lazy(a0, S.cs0[p], e);
+                if (s1 >= 0) ff_fma_lazy(a1, S.cs1[p], e);
+                if (pa >= 0) ff_fma_lazy(ap, S.cp[p], e);
+                if (MODE >= 2) {
+                    const ff ea = al * e, eaa = al * ea;
+                    if (s0 >= 0) { ff_fma_lazy(b0, S.cs0[p], ea); ff_fma_lazy(c0, S.cs0[p], eaa); }
+                    if (s1 >= 0) { ff_fma_lazy(b1, S.cs1[p], ea); ff_fma_lazy(c1, S.cs1[p], eaa); }
+                    if (pa >= 0) { ff_fma_lazy(bp, S.cp[p], ea); ff_fma_lazy(cpp, S.cp[p], eaa); }
+                }
             }
             a0 = ff_norm(a0); b0 = ff_norm(b0); c0 = ff_norm(c0);
             a1 = ff_norm(a1); b1 = ff_norm(b1); c1 = ff_norm(c1);
@@ -752,10 +757,12 @@ __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int s
                 for (int k = 0; k < NM; ++k) {
                     const ff c = S.C[sig][a][k];
                     ff_fma_lazy(v[k], c, chi);
-                    ff_fma_lazy(gx[k], c, ax);
-                    ff_fma_lazy(gy[k], c, ay);
-                    ff_fma_lazy(gz[k], c, az);
-                    ff_fma_lazy(l[k], c, la);
+                    if (MODE >= 2) {
+                        ff_fma_lazy(gx[k], c, ax);
+                        ff_fma_lazy(gy[k], c, ay);
+                        ff_fma_lazy(gz[k], c, az);
+                        ff_fma_lazy(l[k], c, la);
+                    }
                 }
             }
         }
@@ -767,20 +774,22 @@ __device__ __forceinline__ void orbitals_gto_rolled(const SysT<SH, ff>& S, int s
     }
 }
 
-template <class SH, class TS, int SIG>
-__device__ __forceinline__ void rows_orbitals(const SysT<SH, ff>& S, int sig, ff x, ff y, ff z, ff (&v)[SH::NMAX],
+template <class SH, int SIG, int MODE>
+__device__ __forceinline__ void rows_orbitals(const SysT<SH, ff>& S, ff x, ff y, ff z, ff (&v)[SH::NMAX],
                                               ff (&gx)[SH::NMAX], ff (&gy)[SH::NMAX], ff (&gz)[SH::NMAX],
                                               ff (&l)[SH::NMAX]) {
-    MOEval<SH, ff, SIG, 2, 0> m;
+    MOEval<SH, ff, SIG, MODE, 0> m;
     m.run(S, x, y, z);
 #pragma unroll
     for (int k = 0; k < SH::NMAX; ++k) { v[k] = m.v[k]; gx[k] = m.gx[k]; gy[k] = m.gy[k]; gz[k] = m.gz[k]; l[k] = m.l[k]; }
 }
 
-// Pass 1 for electron e (sector sig) of walker w.
-template <class SH, class TS>
+// Pass 1 for electron e (sector sig) of walker w.  VALUES: only the orbital
+// values and the Jastrow u (what the inverse and log|psi| need).
+template <class SH, class TS, bool VALUES>
 __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* __restrict__ pos,
                                              float2* __restrict__ rows, int e, int w, int Wcap) {
+    constexpr int MODE = VALUES ? 0 : 2;
     using RL = RowLayout<SH>;
     constexpr int NM = RL::NM;
     const size_t st = (size_t)Wcap;
@@ -791,14 +800,15 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
     {
         ff v[NM], ogx[NM], ogy[NM], ogz[NM], ol[NM];
         if constexpr (SH::BASIS == BASIS_GTO) {
-            orbitals_gto_rolled<SH>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
+            orbitals_gto_rolled<SH, MODE>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
         } else {
-            if (sig == 0) rows_orbitals<SH, TS, 0>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
-            else rows_orbitals<SH, TS, 1>(S, sig, x, y, z, v, ogx, ogy, ogz, ol);
+            if (sig == 0) rows_orbitals<SH, 0, MODE>(S, x, y, z, v, ogx, ogy, ogz, ol);
+            else rows_orbitals<SH, 1, MODE>(S, x, y, z, v, ogx, ogy, ogz, ol);
         }
 #pragma unroll
         for (int k = 0; k < NM; ++k) {
             ff_store(out + (0 * NM + k) * st, v[k]);
+            if (VALUES) continue;
             ff_store(out + (1 * NM + k) * st, ogx[k]);
             ff_store(out + (2 * NM + k) * st, ogy[k]);
             ff_store(out + (3 * NM + k) * st, ogz[k]);
@@ -824,7 +834,7 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
         }
         u += ff(0.5f) * uu;
         const bool skip = (SH::JAS == JAS_PADE_EEN) ? (d < ff(1e-10)) : (d == ff(0));
-        if (!skip) {
+        if (!VALUES && !skip) {
             gx += upr * dx; gy += upr * dy; gz += upr * dz;
             lu += lt;
             const ff up = upr * d;
@@ -841,10 +851,14 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
         ff uu, upr, lt;
         pade_ab(S.enA[I], S.enB[I], d, ri, uu, upr, lt);
         u -= uu;
-        if (!(d < ff(1e-10))) {
+        if (!VALUES && !(d < ff(1e-10))) {
             gx -= upr * dx; gy -= upr * dy; gz -= upr * dz;
             lu -= lt;
         }
+    }
+    if (VALUES) {
+        ff_store(out + (RL::J0 + 5) * st, u);
+        return;
     }
     ff_store(out + (RL::J0 + 0) * st, gx);
     ff_store(out + (RL::J0 + 1) * st, gy);
@@ -856,7 +870,7 @@ __device__ __forceinline__ void rows_electron(const SysT<SH, ff>& S, const TS* _
 }
 
 // One spin sector (NS electrons, runtime sector index sig) of pass 2.
-template <class SH, class TS, int NS>
+template <class SH, class TS, int NS, bool VALUES>
 __device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const float2* __restrict__ rows,
                                                 TS* __restrict__ dinv, int SIG, int w, int wr, bool act, int Wcap,
                                                 int write_state, ff& pm, int& pe, int& sg, bool& ok, ff& kin,
@@ -879,6 +893,11 @@ __device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const flo
         for (int k = 0; k < NS; ++k)
 #pragma unroll
             for (int j = 0; j < NS; ++j) dinv[((size_t)(SIG * NM * NM + k * NM + j)) * Wcap + w] = (TS)Di[k][j];
+    }
+    if (VALUES) {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) ut += ff_load(rows + ((size_t)(SIG * SH::NUP + q) * RL::QN + RL::J0 + 5) * st + wr);
+        return;
     }
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
@@ -904,7 +923,7 @@ __device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const flo
 }
 
 // Pass 2 for walker w (inactive lanes read walker 0's rows and store nothing).
-template <class SH, class TS>
+template <class SH, class TS, bool VALUES>
 __device__ __forceinline__ double assemble_walker(const SysT<SH, ff>& S, const float2* __restrict__ rows,
                                                   TS* __restrict__ dinv, double* __restrict__ logabs,
                                                   int* __restrict__ sign, double* __restrict__ el, int w, bool act,
@@ -918,41 +937,48 @@ __device__ __forceinline__ double assemble_walker(const SysT<SH, ff>& S, const f
         // instruction stream keeps the FP32 pipe fed from the cache)
 #pragma unroll 1
         for (int sig = 0; sig < 2; ++sig)
-            assemble_sector<SH, TS, SH::NUP>(S, rows, dinv, sig, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin,
-                                             ut, vt);
+            assemble_sector<SH, TS, SH::NUP, VALUES>(S, rows, dinv, sig, w, wr, act, Wcap, write_state, pm, pe, sg,
+                                                     ok, kin, ut, vt);
     } else {
-        assemble_sector<SH, TS, SH::NUP>(S, rows, dinv, 0, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
-        assemble_sector<SH, TS, SH::NDN>(S, rows, dinv, 1, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin, ut, vt);
+        assemble_sector<SH, TS, SH::NUP, VALUES>(S, rows, dinv, 0, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin,
+                                                 ut, vt);
+        assemble_sector<SH, TS, SH::NDN, VALUES>(S, rows, dinv, 1, w, wr, act, Wcap, write_state, pm, pe, sg, ok, kin,
+                                                 ut, vt);
     }
     const double logdet = log((double)pm) + (double)pe * 0.6931471805599453;
-    const double e_l = (double)(ff(-0.5f) * kin + vt + S.v_nn);
+    const double e_l = VALUES ? 0.0 : (double)(ff(-0.5f) * kin + vt + S.v_nn);
     if (!act) return 0.0;
     int fl = 0;
     if (!ok) fl |= FLAG_SINGULAR;
-    if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
+    if (!isfinite(e_l) || !isfinite(logdet)) fl |= FLAG_NONFINITE;
     if (fl) atomicOr(flags, fl);
-    if (write_state) { logabs[w] = logdet + (double)ut; sign[w] = sg; el[w] = e_l; }
+    if (write_state) {
+        logabs[w] = logdet + (double)ut;
+        sign[w] = sg;
+        if (!VALUES) el[w] = e_l;
+    }
     return e_l;
 }
 
-template <class SH, class TS>
+template <class SH, class TS, bool VALUES>
 __global__ void __launch_bounds__(128) k_rows(const __grid_constant__ SysT<SH, ff> S, const TS* __restrict__ pos,
                                               float2* __restrict__ rows, int W, int Wcap) {
     const int w = blockIdx.x * 128 + threadIdx.x;
     const int e = blockIdx.y;
     if (w >= W) return;
-    rows_electron<SH, TS>(S, pos, rows, e, w, Wcap);
+    rows_electron<SH, TS, VALUES>(S, pos, rows, e, w, Wcap);
 }
 
-template <class SH, class TS, int TPB>
+template <class SH, class TS, int TPB, bool VALUES>
 __global__ void __launch_bounds__(TPB) k_assemble(const __grid_constant__ SysT<SH, ff> S,
                                                   const float2* __restrict__ rows, TS* __restrict__ dinv,
                                                   double* __restrict__ logabs, int* __restrict__ sign,
                                                   double* __restrict__ el, int W, int Wcap, int write_state,
                                                   double* partial, int* flags) {
     const int w = blockIdx.x * TPB + threadIdx.x;
-    const double e_l = assemble_walker<SH, TS>(S, rows, dinv, logabs, sign, el, w, w < W, Wcap, write_state, flags);
-    if (partial) block_partial<TPB>(e_l, partial, blockIdx.x);
+    const double e_l = assemble_walker<SH, TS, VALUES>(S, rows, dinv, logabs, sign, el, w, w < W, Wcap, write_state,
+                                                       flags);
+    if (!VALUES && partial) block_partial<TPB>(e_l, partial, blockIdx.x);
 }
 
 // Batched forms.  Pass 1 runs over (tile, electron) items in tile-major
@@ -976,7 +1002,7 @@ __global__ void __launch_bounds__(TPB) kb_rows(const BatchTile* __restrict__ til
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + (int)threadIdx.x;
-        if (w < R.W) rows_electron<SH, TS>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
+        if (w < R.W) rows_electron<SH, TS, false>(S, (const TS*)R.pos, R.rows, e, w, R.Wcap);
     }
 }
 
@@ -997,8 +1023,8 @@ __global__ void __launch_bounds__(TPB) kb_assemble(const BatchTile* __restrict__
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + (int)threadIdx.x;
-        const double e_l = assemble_walker<SH, TS>(S, R.rows, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W,
-                                                   R.Wcap, 1, R.flags);
+        const double e_l = assemble_walker<SH, TS, false>(S, R.rows, (TS*)R.dinv, R.logabs, R.sign, R.el, w,
+                                                          w < R.W, R.Wcap, 1, R.flags);
         block_partial<TPB>(e_l, tile_partial, ti);
     }
 }
@@ -1337,12 +1363,13 @@ struct ShapeOps {
         return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
     }
 
+    template <bool VALUES>
     static int measure_split(const HostSys& hs, DevWalkers& dw, bool write_state, cudaStream_t st) {
         SysT<SH, ff> S;
         if (!fill_sys(hs, S)) return 7;
         if (dw.W == 0) return 0;
         dim3 g1((dw.W + 127) / 128, SH::NE);
-        k_rows<SH, float><<<g1, 128, 0, st>>>(S, (const float*)dw.pos, dw.rows, dw.W, dw.Wcap);
+        k_rows<SH, float, VALUES><<<g1, 128, 0, st>>>(S, (const float*)dw.pos, dw.rows, dw.W, dw.Wcap);
         ++g_launch_count;
         int rc = cuda_status(cudaGetLastError());
         if (rc) return rc;
@@ -1350,8 +1377,9 @@ struct ShapeOps {
         const int nb = (dw.W + TPB - 1) / TPB;
         double* partial = nullptr;
         if (write_state && dw.partial && dw.partial_cap >= 2 * nb + 1) partial = dw.partial;
-        k_assemble<SH, float, TPB><<<nb, TPB, 0, st>>>(S, dw.rows, (float*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W,
-                                                       dw.Wcap, write_state ? 1 : 0, partial, dw.flags);
+        if (VALUES) partial = nullptr;
+        k_assemble<SH, float, TPB, VALUES><<<nb, TPB, 0, st>>>(S, dw.rows, (float*)dw.dinv, dw.logabs, dw.sign, dw.el,
+                                                               dw.W, dw.Wcap, write_state ? 1 : 0, partial, dw.flags);
         ++g_launch_count;
         rc = cuda_status(cudaGetLastError());
         if (rc || !partial) return rc;
@@ -1367,7 +1395,8 @@ struct ShapeOps {
             if (dw.prec == 0) return measure2<double, double, 0>(hs, dw, ws, out, st);
             // FP64-class refresh on the FP32 pipe: the two-pass form when only
             // the walker state is wanted, else the single-kernel form
-            if (dw.rows && !out.grad && !out.lap && !out.fhf && !out.omega) return measure_split(hs, dw, ws, st);
+            if (dw.rows && !out.grad && !out.lap && !out.fhf && !out.omega)
+                return out.inverse_only ? measure_split<true>(hs, dw, ws, st) : measure_split<false>(hs, dw, ws, st);
             return measure2<ff, float, 0>(hs, dw, ws, out, st);
         }
         if (dw.prec == 1) return measure2<float, float, 0>(hs, dw, ws, out, st);

@@ -494,3 +494,35 @@ def test_benzene_refresh_block_shapes_agree(ctx, prec):
     assert np.array_equal(el1, el2) and np.array_equal(la1, la2) and np.array_equal(sg1, sg2)
     assert abs(e1 - e2) <= 1e-12 * abs(el1).sum()
     assert abs(e2 - el2.sum()) <= 1e-12 * abs(el2).sum()
+
+
+@pytest.mark.parametrize("name", ["h2", "li_ref", "ch4_min", "ch4_gto", "c6h6", "heg"])
+@pytest.mark.parametrize("prec", [L.QMC_FP32_REFINE, L.QMC_FP64])
+def test_rebuild_inverse_matches_refresh(ctx, name, prec):
+    """qmc_walkers_rebuild_inverse leaves the walker state a full refresh
+    leaves (log|psi| and sign bit for bit), and a Gaussian sweep after it
+    follows the same trajectory as a sweep after the full refresh."""
+    builders = dict(BUILDERS, c6h6=lambda: Q.benzene_minimal(), heg=lambda: Q.electron_gas())
+    sysh = Q.System(ctx, builders[name]())
+    W = 256
+    src = Q.Walkers(sysh, W, prec)
+    src.init(seed=41)
+    pos = src.get_positions()
+    src.close()
+    out = []
+    for rebuild in (False, True):
+        wk = Q.Walkers(sysh, W, prec)
+        wk.set_positions(pos)
+        if rebuild:
+            wk.rebuild_inverse()
+        else:
+            wk.refresh()
+        la, sg, _ = wk.state()
+        wk.sweep(L.QMC_MOVE_ONE_GAUSS, 4, 7, seed=5, step=0.3, count=False)
+        out.append((la, sg, wk.get_positions(), wk.status()))
+        wk.close()
+    (la0, sg0, p0, f0), (la1, sg1, p1, f1) = out
+    assert np.all(np.isfinite(la0))
+    assert np.array_equal(la0, la1) and np.array_equal(sg0, sg1)
+    assert np.array_equal(p0, p1)
+    assert f0 == 0 and f1 == 0

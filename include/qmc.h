@@ -283,6 +283,21 @@ int qmc_vmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed,
  * E_L in FP64 every refresh_every steps. */
 int qmc_dmc_run(qmc_sys_t sys, const qmc_run_params* params, uint64_t seed, qmc_run_result* result,
                 double* energies);
+/* ImportanceSampledDMC::run with its force estimators (src/sampling/is_dmc.rs:
+ * 303-380, 479-485, 520-534), [n_nuc x 3] each, in the reference's
+ * hellmann_feynman_force convention (src/systems/methane.rs:1241-1272):
+ * forces_vmc   = <F_HF> of a separate VMC run: min(n_walkers, 50) walkers,
+ *                all-electron Gaussian moves of width 0.5 (single-electron
+ *                sweeps of that width for benzene), n_vmc_equilibrate steps,
+ *                then max(1, n_vmc_force_samples / walkers) rounds of five
+ *                steps, each recording every walker;
+ * forces_mixed = <F_HF> over every walker of every production step of the
+ *                DMC run (the run of qmc_dmc_run with the same seed);
+ * forces_extrapolated = 2 forces_mixed - forces_vmc.
+ * The electron sums run on the device (FP64, compensated, per step). */
+int qmc_dmc_run_forces(qmc_sys_t sys, const qmc_run_params* params, int n_vmc_equilibrate,
+                       int n_vmc_force_samples, uint64_t seed, qmc_run_result* result, double* energies,
+                       double* forces_mixed, double* forces_vmc, double* forces_extrapolated);
 
 /* ---- single-electron ratio (MultiWfn evaluate twice, src/sampling/vmc.rs:356-370) ---- */
 /* ratio[w] = psi(R_w with electron e at r_new[w]) / psi(R_w) for W

@@ -103,6 +103,8 @@ PROTOTYPES = {
     "qmc_walkers_status": [_vp, _ip],
     "qmc_vmc_run": [_vp, C.POINTER(RunParams), _u64, C.POINTER(RunResult), _dp],
     "qmc_dmc_run": [_vp, C.POINTER(RunParams), _u64, C.POINTER(RunResult), _dp],
+    "qmc_dmc_run_forces": [_vp, C.POINTER(RunParams), C.c_int, C.c_int, _u64, C.POINTER(RunResult), _dp, _dp, _dp,
+                           _dp],
     "qmc_walkers_create_dmc": [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)],
     "qmc_walkers_count": [_vp, _ip],
     "qmc_walkers_dmc_step": [_vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _u64, _u64, C.c_int, _ip,

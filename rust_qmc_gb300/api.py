@@ -420,18 +420,49 @@ def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_
                 status_flags=res.status_flags, energies=energies[:res.n_samples])
 
 
-def dmc_run(system, *, n_walkers, n_steps, n_burnin=0, tau=0.005, max_drift=1.0, precision=L.QMC_FP64,
-            refresh_every=1, e_ref_damping=0.5, fixed_node=True, reference_diffusion=False, seed=1):
-    """ImportanceSampledDMC::run (energy part) on the device."""
+def _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping, fixed_node,
+                reference_diffusion):
     p = L.RunParams()
     p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = n_walkers, n_steps, n_burnin, L.QMC_MOVE_ONE_DRIFT
     p.tau, p.max_drift, p.precision, p.refresh_every = tau, max_drift, precision, refresh_every
     p.e_ref_damping, p.fixed_node = e_ref_damping, int(bool(fixed_node))
     p.reference_diffusion = int(bool(reference_diffusion))
-    res = L.RunResult()
-    energies = np.zeros(n_steps)
-    L.check(system.lib.qmc_dmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_dmc_run")
+    return p
+
+
+def _run_dict(res, energies):
     return dict(energy=res.energy, error=res.error, autocorrelation_time=res.autocorrelation_time,
                 acceptance_rate=res.acceptance_rate, variance=res.variance, n_samples=res.n_samples,
                 status_flags=res.status_flags, avg_population=res.avg_population,
                 energies=energies[:res.n_samples])
+
+
+def dmc_run(system, *, n_walkers, n_steps, n_burnin=0, tau=0.005, max_drift=1.0, precision=L.QMC_FP64,
+            refresh_every=1, e_ref_damping=0.5, fixed_node=True, reference_diffusion=False, seed=1):
+    """ImportanceSampledDMC::run (energy part) on the device."""
+    p = _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping,
+                    fixed_node, reference_diffusion)
+    res = L.RunResult()
+    energies = np.zeros(n_steps)
+    L.check(system.lib.qmc_dmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_dmc_run")
+    return _run_dict(res, energies)
+
+
+def dmc_run_forces(system, *, n_walkers, n_steps, n_burnin=0, tau=0.005, max_drift=1.0, precision=L.QMC_FP64,
+                   refresh_every=1, e_ref_damping=0.5, fixed_node=True, reference_diffusion=False,
+                   n_vmc_equilibrate=500, n_vmc_force_samples=2000, seed=1):
+    """ImportanceSampledDMC::run with the mixed, VMC and extrapolated
+    Hellmann-Feynman force estimators (qmc_dmc_run_forces); the energy part is
+    dmc_run's with the same arguments."""
+    p = _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping,
+                    fixed_node, reference_diffusion)
+    res = L.RunResult()
+    energies = np.zeros(n_steps)
+    n = system.num_nuclei()
+    fm, fv, fe = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+    L.check(system.lib.qmc_dmc_run_forces(system.h, C.byref(p), n_vmc_equilibrate, n_vmc_force_samples, seed,
+                                          C.byref(res), _d(energies), _d(fm), _d(fv), _d(fe)),
+            "qmc_dmc_run_forces")
+    out = _run_dict(res, energies)
+    out.update(forces_mixed=fm, forces_vmc=fv, forces_extrapolated=fe)
+    return out

@@ -979,7 +979,114 @@ int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     return QMC_OK;
 }
 
-int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies) {
+// Device buffers of the Hellmann-Feynman force estimators: nuclei [n_nuc][4],
+// block-partial scratch, and one FP64 force sum [3 n_nuc] per recorded step.
+struct ForceAcc {
+    int n_nuc = 0, n_rows = 0, recorded = 0;
+    double* d_nuc = nullptr;
+    double* d_partial = nullptr;
+    double* d_series = nullptr;
+    size_t partial_cap = 0;
+    double walkers = 0.0;                  // walker samples summed so far
+    ~ForceAcc() { cudaFree(d_nuc); cudaFree(d_partial); cudaFree(d_series); }
+    int init(const HostSys& hs, int w_cap, int rows, cudaStream_t st) {
+        n_nuc = hs.n_nuc;
+        n_rows = rows;
+        if (n_nuc == 0) return QMC_OK;
+        std::vector<double> nuc(4 * (size_t)n_nuc);
+        for (int I = 0; I < n_nuc; ++I) {
+            for (int c = 0; c < 3; ++c) nuc[4 * I + c] = hs.R[3 * I + c];
+            nuc[4 * I + 3] = hs.Z[I];
+        }
+        partial_cap = hf_force_scratch_doubles(w_cap, n_nuc);
+        CU(cudaMalloc((void**)&d_nuc, 8 * nuc.size()));
+        CU(cudaMalloc((void**)&d_partial, 8 * partial_cap));
+        CU(cudaMalloc((void**)&d_series, 8 * 3 * (size_t)n_nuc * (rows > 0 ? rows : 1)));
+        CU(cudaMemcpyAsync(d_nuc, nuc.data(), 8 * nuc.size(), cudaMemcpyHostToDevice, st));
+        return QMC_OK;
+    }
+    // sum of the electron-nucleus forces of the walker set, one row per call
+    int record(const HostSys& hs, const DevWalkers& dw, cudaStream_t st) {
+        if (n_nuc == 0) return QMC_OK;
+        if (recorded >= n_rows) return QMC_ERR_ARG;
+        if (launch_hf_force_sum(dw, hs.N, n_nuc, d_nuc, d_partial, partial_cap, d_series + 3 * (size_t)n_nuc * recorded,
+                                st))
+            return QMC_ERR_CUDA;
+        ++recorded;
+        walkers += dw.W;
+        return QMC_OK;
+    }
+    // mean force per walker sample plus the nuclear term of the reference's
+    // hellmann_feynman_force (F_I -= sum_J Z_I Z_J (R_I - R_J) / |R_I - R_J|^3)
+    int mean(const HostSys& hs, cudaStream_t st, double* out) {
+        if (n_nuc == 0) return QMC_OK;
+        std::vector<double> rows(3 * (size_t)n_nuc * recorded);
+        if (recorded) {
+            CU(cudaMemcpyAsync(rows.data(), d_series, 8 * rows.size(), cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+        }
+        for (int k = 0; k < 3 * n_nuc; ++k) {
+            double sum = 0.0, comp = 0.0;               // Neumaier over the recorded steps
+            for (int r = 0; r < recorded; ++r) {
+                const double v = rows[3 * (size_t)n_nuc * r + k], t = sum + v;
+                comp += std::fabs(sum) >= std::fabs(v) ? (sum - t) + v : (v - t) + sum;
+                sum = t;
+            }
+            out[k] = walkers > 0 ? (sum + comp) / walkers : 0.0;
+        }
+        for (int I = 0; I < n_nuc; ++I)
+            for (int J = 0; J < n_nuc; ++J) {
+                if (I == J) continue;
+                double d[3], r2 = 0.0;
+                for (int c = 0; c < 3; ++c) { d[c] = hs.R[3 * I + c] - hs.R[3 * J + c]; r2 += d[c] * d[c]; }
+                const double r = std::sqrt(r2);
+                if (r > 1e-10)
+                    for (int c = 0; c < 3; ++c) out[3 * I + c] -= hs.Z[I] * hs.Z[J] * d[c] / (r2 * r);
+            }
+        return QMC_OK;
+    }
+};
+
+// ImportanceSampledDMC::vmc_forces (src/sampling/is_dmc.rs:303-380): min(n_walkers, 50)
+// walkers, all-electron Gaussian proposals of width 0.5 (single-electron
+// Gaussian sweeps of that width for shapes without an all-electron sampler),
+// n_equil steps, then rounds of five steps recording every walker's force
+// until n_samples / walkers rounds.
+static int vmc_forces(qmc_sys_t s, int n_walkers, int precision, int n_equil, int n_samples, uint64_t seed,
+                      double* out) {
+    const HostSys& hs = s->hs;
+    cudaStream_t st = s->ctx->stream;
+    const int W = std::min(n_walkers, 50);
+    const int rounds = std::max(1, n_samples / W);
+    qmc_walkers_s* wk = nullptr;
+    CK(alloc_walkers(s, W, precision, &wk));
+    struct Guard { qmc_walkers_s* w; ~Guard() { if (w) { cudaStreamSynchronize(w->sys->ctx->stream); free_walkers(w); } } } guard{wk};
+    ForceAcc fa;
+    CK(fa.init(hs, W, rounds, st));
+    CK(launch_init(hs, wk->dw, seed, st));
+    MeasureOut none;
+    CK(launch_measure(hs, wk->dw, 0, true, none, st));
+    const bool all = hs.shape != SHAPE_C6H6 && hs.shape != SHAPE_HEG54;
+    const int mk = all ? QMC_MOVE_ALL_GAUSS : QMC_MOVE_ONE_GAUSS;
+    uint64_t step = 0;
+    auto advance = [&](int n) -> int {
+        if (n <= 0) return QMC_OK;
+        CK(launch_sweep(hs, wk->dw, mk, n, step, 0.5, 0.0, 0.0, seed, st));
+        step += (uint64_t)n;
+        // single-electron sweeps carry FP32 inverses: rebuild them each round
+        if (!all) CK(launch_measure(hs, wk->dw, 0, true, none, st));
+        return QMC_OK;
+    };
+    CK(advance(n_equil));
+    for (int r = 0; r < rounds; ++r) {
+        CK(advance(5));
+        CK(fa.record(hs, wk->dw, st));
+    }
+    return fa.mean(hs, st, out);
+}
+
+static int dmc_run_impl(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies,
+                        double* forces_mixed) {
     if (!s || !p || !res) return QMC_ERR_ARG;
     if (p->n_walkers <= 0 || p->n_steps <= 0 || p->n_burnin < 0 || !(p->tau > 0) || !(p->max_drift > 0)) return QMC_ERR_ARG;
     std::memset(res, 0, sizeof(*res));
@@ -1006,6 +1113,8 @@ int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     double e_ref = 0.0;
     CK(reinit(seed, e_ref));
     CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+    ForceAcc fa;
+    if (forces_mixed) CK(fa.init(hs, 4 * target, p->n_steps, st));
     std::vector<double> series;
     double pop_sum = 0.0;
     long long moves = 0;
@@ -1036,6 +1145,7 @@ int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
         if (t >= p->n_burnin) {
             series.push_back(em);
             pop_sum += n_new;
+            if (forces_mixed) CK(fa.record(hs, wk->dw, st));   // <F_HF> over the population, is_dmc.rs:479-485
         }
         e_ref = em - kappa * std::log((double)n_new / (double)target) / p->tau;   // is_dmc.rs:489-490
     }
@@ -1059,6 +1169,26 @@ int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     res->avg_population = p->n_steps ? pop_sum / (double)p->n_steps : 0.0;
     if (energies) for (size_t i = 0; i < series.size(); ++i) energies[i] = series[i];
     (void)acc_burn;
+    if (forces_mixed) CK(fa.mean(hs, st, forces_mixed));
+    return QMC_OK;
+}
+
+int qmc_dmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies) {
+    return dmc_run_impl(s, p, seed, res, energies, nullptr);
+}
+
+int qmc_dmc_run_forces(qmc_sys_t s, const qmc_run_params* p, int n_vmc_equilibrate, int n_vmc_force_samples,
+                       uint64_t seed, qmc_run_result* res, double* energies, double* forces_mixed,
+                       double* forces_vmc, double* forces_extrapolated) {
+    if (!s || !p || !res || !forces_mixed || !forces_vmc || !forces_extrapolated) return QMC_ERR_ARG;
+    if (n_vmc_equilibrate < 0 || n_vmc_force_samples < 0 || p->n_walkers <= 0) return QMC_ERR_ARG;
+    cudaSetDevice(s->ctx->device);
+    const int n3 = 3 * s->hs.n_nuc;
+    // Phase 1 of ImportanceSampledDMC::run (is_dmc.rs:388-389), on its own key
+    CK(vmc_forces(s, p->n_walkers, p->precision, n_vmc_equilibrate, n_vmc_force_samples,
+                  seed ^ 0xD1B54A32D192ED03ull, forces_vmc));
+    CK(dmc_run_impl(s, p, seed, res, energies, forces_mixed));
+    for (int k = 0; k < n3; ++k) forces_extrapolated[k] = 2.0 * forces_mixed[k] - forces_vmc[k];   // is_dmc.rs:525-530
     return QMC_OK;
 }
 

@@ -445,6 +445,28 @@ __device__ __forceinline__ Comp comp_add(Comp a, Comp b) {
     return {s, a.c + b.c + e};
 }
 
+// Compensated sum of v over the block's TPB threads into partial[2 slot],
+// partial[2 slot + 1] (a fixed-order tree; every thread must call it).
+template <int TPB>
+__device__ __forceinline__ void block_partial(double v, double* partial, int slot) {
+    __shared__ double ss[TPB], sc[TPB];
+    ss[threadIdx.x] = v;
+    sc[threadIdx.x] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int o = TPB / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            Comp a{ss[threadIdx.x], sc[threadIdx.x]}, b{ss[threadIdx.x + o], sc[threadIdx.x + o]};
+            Comp c = comp_add(a, b);
+            ss[threadIdx.x] = c.s;
+            sc[threadIdx.x] = c.c;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { partial[2 * slot] = ss[0]; partial[2 * slot + 1] = sc[0]; }
+    __syncthreads();
+}
+
 // Persistent batched launches: block b owns the contiguous run of tiles
 // [t0, t1) of the class's tile list, so consecutive tiles mostly share a
 // system and its table is staged once per run.

@@ -122,6 +122,13 @@ int launch_walker_sum(const double* X, int W, int ncol, double* d_out, double* d
 int launch_sr_sums(const double* E, const double* O, int W, int P, double* d_out,
                    double* d_scratch, int scratch_cap, cudaStream_t st);
 int launch_flush(void* buf, size_t bytes, cudaStream_t st);
+// Sum over the W walkers of the Hellmann-Feynman electron-nucleus forces into
+// d_out[3 n_nuc] (FP64, compensated); d_nuc = [n_nuc][4] (x, y, z, Z); the
+// scratch holds hf_force_scratch_doubles(W, n_nuc) doubles.
+size_t hf_force_scratch_doubles(int W, int n_nuc);
+int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+int launch_hf_force_sum(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_partial,
+                        size_t partial_cap, double* d_out, cudaStream_t st);
 // DMC branching (src/sampling/is_dmc.rs:278-302): copies per walker from the
 // FP64 log-weight, exclusive scan, order-stable gather into `dst`.
 // stats[0] = new population, stats[1] = sum of copies x E_L, stats[2] = flags.

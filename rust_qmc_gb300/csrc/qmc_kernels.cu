@@ -218,6 +218,59 @@ int launch_walker_sum(const double* X, int W, int ncol, double* d_out, double* d
     return launch_sr_sums(X, X, W, 0, d_out, d_scratch, scratch_cap, st);
 }
 
+// Hellmann-Feynman electron-nucleus forces summed over walkers
+// (src/systems/methane.rs:1247-1256, hydrogen.rs:233-243, benzene.rs:834-844):
+// walker w contributes f_I = Z_I sum_i (r_i - R_I) / |r_i - R_I|^3, pairs
+// closer than 1e-10 skipped.  One compensated partial per block and force
+// component, partial[3 I + c][block]; nuc = [n_nuc][4] (x, y, z, Z).
+template <class TS, int TPB>
+__global__ void __launch_bounds__(TPB) k_hf_force_partials(const TS* __restrict__ pos, int W, int Wcap, int N,
+                                                           int n_nuc, const double* __restrict__ nuc,
+                                                           double* __restrict__ partial, int nblk) {
+    const int w = blockIdx.x * TPB + threadIdx.x;
+    const bool act = w < W;
+    for (int I = 0; I < n_nuc; ++I) {
+        const double X = nuc[4 * I], Y = nuc[4 * I + 1], Zc = nuc[4 * I + 2], Q = nuc[4 * I + 3];
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        if (act) {
+            for (int i = 0; i < N; ++i) {
+                const double dx = (double)pos[(size_t)(3 * i) * Wcap + w] - X;
+                const double dy = (double)pos[(size_t)(3 * i + 1) * Wcap + w] - Y;
+                const double dz = (double)pos[(size_t)(3 * i + 2) * Wcap + w] - Zc;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                const double d = sqrt(d2);
+                if (d > 1e-10) {
+                    const double f = Q / (d2 * d);
+                    fx += f * dx; fy += f * dy; fz += f * dz;
+                }
+            }
+        }
+        block_partial<TPB>(fx, partial + (size_t)(3 * I + 0) * 2 * nblk, blockIdx.x);
+        block_partial<TPB>(fy, partial + (size_t)(3 * I + 1) * 2 * nblk, blockIdx.x);
+        block_partial<TPB>(fz, partial + (size_t)(3 * I + 2) * 2 * nblk, blockIdx.x);
+    }
+}
+
+size_t hf_force_scratch_doubles(int W, int n_nuc) { return (size_t)2 * ((W + 127) / 128) * 3 * n_nuc; }
+
+int launch_hf_force_sum(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_partial,
+                        size_t partial_cap, double* d_out, cudaStream_t st) {
+    constexpr int TPB = 128;
+    if (n_nuc <= 0 || dw.W <= 0) return 0;
+    const int nblk = (dw.W + TPB - 1) / TPB;
+    if (hf_force_scratch_doubles(dw.W, n_nuc) > partial_cap) return 1;
+    if (dw.prec == 0)
+        k_hf_force_partials<double, TPB><<<nblk, TPB, 0, st>>>((const double*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc,
+                                                               d_partial, nblk);
+    else
+        k_hf_force_partials<float, TPB><<<nblk, TPB, 0, st>>>((const float*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc,
+                                                              d_partial, nblk);
+    ++g_launch_count;
+    int rc = cuda_status(cudaGetLastError());
+    if (rc) return rc;
+    return launch_sum_partials(d_partial, nblk, 3 * n_nuc, d_out, st);
+}
+
 int launch_flush(void* buf, size_t bytes, cudaStream_t st) {
     size_t n = bytes / sizeof(uint4);
     k_flush<<<152 * 8, 256, 0, st>>>((uint4*)buf, n, (unsigned)(g_launch_count & 0xffff));

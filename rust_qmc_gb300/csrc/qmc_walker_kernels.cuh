@@ -543,26 +543,6 @@ __global__ void k_init(const __grid_constant__ SysT<SH, double> S, TS* __restric
     }
 }
 
-template <int TPB>
-__device__ __forceinline__ void block_partial(double v, double* partial, int slot) {
-    __shared__ double ss[TPB], sc[TPB];
-    ss[threadIdx.x] = v;
-    sc[threadIdx.x] = 0.0;
-    __syncthreads();
-#pragma unroll
-    for (int o = TPB / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            Comp a{ss[threadIdx.x], sc[threadIdx.x]}, b{ss[threadIdx.x + o], sc[threadIdx.x + o]};
-            Comp c = comp_add(a, b);
-            ss[threadIdx.x] = c.s;
-            sc[threadIdx.x] = c.c;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) { partial[2 * slot] = ss[0]; partial[2 * slot + 1] = sc[0]; }
-    __syncthreads();
-}
-
 // Full evaluation of walker w (refresh of the inverse, log|psi|, E_L and the
 // requested extras); returns E_L (0 for an inactive lane, which still runs the
 // arithmetic on a dummy configuration so that the block stays converged).

@@ -374,25 +374,37 @@ def benzene_minimal(seed=SEED_BASE + 4, b_ee=1.5, b_en=2.0, cc=2.64, ch=2.05):
         jas=jastrow3_params(b_ee, b_en), init_nuc=init, init_sigma=0.5)
 
 
-def heg_k_vectors(n, L):
-    """The n lowest plane waves of a cubic box (src/systems/heg.rs:198-235):
-    integer vectors in [-m, m]^3 generated in nx, ny, nz order and stably
-    sorted by |k|^2, m = ceil(2 n^(1/3)) + 2."""
+def monkhorst_pack_grid(n):
+    """Twists of an n x n x n Monkhorst-Pack grid in reduced coordinates
+    (src/systems/heg.rs:176-190): theta_s = (2 s - n - 1) / (2 n), s = 1..n,
+    generated in i, j, k order."""
+    th = [(2.0 * (i + 1.0) - n - 1.0) / (2.0 * n) for i in range(n)]
+    return np.array([[tx, ty, tz] for tx in th for ty in th for tz in th]).reshape(-1, 3)
+
+
+def heg_k_vectors(n, L, twist=None):
+    """The n lowest plane waves k + theta (2 pi / L) of a cubic box
+    (src/systems/heg.rs:194-232): integer vectors in [-m, m]^3 generated in
+    nx, ny, nz order, shifted by the twist and stably sorted by |k + theta|^2,
+    m = ceil(2 n^(1/3)) + 2."""
     m = int(math.ceil(n ** (1.0 / 3.0) * 2.0)) + 2
     dk = 2.0 * math.pi / L
+    tw = (0.0, 0.0, 0.0) if twist is None else tuple(float(t) for t in twist)
+    kt = (tw[0] * dk, tw[1] * dk, tw[2] * dk)
     cand = []
     for nx in range(-m, m + 1):
         for ny in range(-m, m + 1):
             for nz in range(-m, m + 1):
-                cand.append(((nx * dk) ** 2 + (ny * dk) ** 2 + (nz * dk) ** 2, nx, ny, nz))
+                kx, ky, kz = nx * dk + kt[0], ny * dk + kt[1], nz * dk + kt[2]
+                cand.append((kx * kx + ky * ky + kz * kz, kx, ky, kz))
     cand.sort(key=lambda t: t[0])        # Python's sort is stable, like Rust's sort_by
-    return np.array([[c[1] * dk, c[2] * dk, c[3] * dk] for c in cand[:n]])
+    return np.array([[c[1], c[2], c[3]] for c in cand[:n]])
 
 
 HEG_FORMS = {"pade": 0, "rpa": 1, "yukawa": 2}
 
 
-def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, alpha_L=4.0, kmax=6):
+def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, alpha_L=4.0, kmax=6, twist=None):
     """Homogeneous electron gas (src/systems/heg.rs:119-170): box
     L = (4 pi N / 3)^(1/3) r_s, closed-shell plane-wave determinants (N/2 per
     spin, same k set), Jastrow u = A r/(1 + r/F + 0.2 r^2/F^2) (RPA form) with
@@ -401,10 +413,13 @@ def electron_gas(n_elec=54, rs=4.0, F=7.0, form="rpa", reference_quirks=False, a
     the reference's; otherwise the one-component-plasma Ewald sum with
     alpha = alpha_L / L (alpha_L >= 3.74: real-space images within 5.6/alpha
     < 1.5 L) and |n| <= kmax reciprocal vectors.  The default (4, 6) keeps the
-    Ewald energy within 1e-10 Ha of the converged value with 462 vectors."""
+    Ewald energy within 1e-10 Ha of the converged value with 462 vectors.
+    ``twist`` (reduced coordinates, heg.rs:116-131) shifts every orbital wave
+    vector by theta 2 pi / L; |psi|^2, the drift and E_L are periodic for any
+    twist, so the same kernels run twisted boundary conditions."""
     box = (4.0 * math.pi / 3.0 * n_elec) ** (1.0 / 3.0) * rs
     nup = n_elec // 2
-    k = heg_k_vectors(nup, box)
+    k = heg_k_vectors(nup, box, twist)
     jas = np.zeros(8)
     jas[0] = HEG_FORMS[form]
     jas[2], jas[3] = 0.25, 0.5          # antiparallel, parallel (heg.rs:146-147)

@@ -374,7 +374,10 @@ def test_benzene_fp64_dmc_matches_oracle(ctx, oracle):
 # ---------------------------------------------------------------------------
 # Periodic electron gas (complex plane-wave determinants, Ewald)
 # ---------------------------------------------------------------------------
-HEG_BUILDERS = {"heg": lambda: Q.electron_gas(), "heg_ref": lambda: Q.electron_gas(reference_quirks=True)}
+HEG_BUILDERS = {"heg": lambda: Q.electron_gas(), "heg_ref": lambda: Q.electron_gas(reference_quirks=True),
+                "heg_twist": lambda: Q.electron_gas(twist=(0.25, -0.25, 0.25)),
+                "heg_pade_twist": lambda: Q.electron_gas(form="pade", twist=(1.0 / 3.0, 0.0, -1.0 / 3.0)),
+                "heg_yukawa": lambda: Q.electron_gas(form="yukawa")}
 
 
 @pytest.mark.parametrize("name", list(HEG_BUILDERS))

@@ -113,14 +113,11 @@ __host__ __device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
         if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-#ifdef __CUDA_ARCH__
-        uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-        uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-#else
+        // one 32 x 32 -> 64-bit product per multiplier (a single wide
+        // multiply on the device)
         uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
         uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
         uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
-#endif
         U4 n;
         n.x = hi1 ^ c.y ^ k0;
         n.y = lo1;

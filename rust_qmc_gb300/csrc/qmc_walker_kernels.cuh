@@ -1009,8 +1009,36 @@ __global__ void __launch_bounds__(TPB) kb_assemble(const BatchTile* __restrict__
     }
 }
 
+template <class T> struct Vec2T;
+template <> struct Vec2T<float> { using type = float2; };
+template <> struct Vec2T<double> { using type = double2; };
+
+// Walker positions in shared memory: (x, y) pairs [NE][TPB] (one 64-bit
+// access per electron, 128-bit for FP64) followed by z [NE][TPB].
+template <class T, int TPB, int NE>
+struct PosCols {
+    using V2 = typename Vec2T<T>::type;
+    V2* xy;
+    T* zz;
+    int t;
+    __device__ __forceinline__ PosCols(T* base, int t_)
+        : xy(reinterpret_cast<V2*>(base)), zz(base + 2 * NE * TPB), t(t_) {}
+    __device__ __forceinline__ T operator()(int j, int c) const {
+        if (c == 2) return zz[j * TPB + t];
+        const V2 v = xy[j * TPB + t];
+        return c == 0 ? v.x : v.y;
+    }
+    __device__ __forceinline__ void set(int j, T x, T y, T z) const {
+        V2 v;
+        v.x = x;
+        v.y = y;
+        xy[j * TPB + t] = v;
+        zz[j * TPB + t] = z;
+    }
+};
+
 // Single-electron sweeps.  Shared memory holds the block's walkers as
-// structure-of-arrays columns: positions [3 NE][TPB], inverse Slater
+// structure-of-arrays columns: positions (PosCols, 3 NE words), inverse Slater
 // matrices [2][NMAX^2][TPB]; each thread only touches its own column, so no
 // barrier is needed.
 template <class SH, class T, int SIG, int MOVE, int TPB>
@@ -1020,7 +1048,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
     constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
     constexpr int NM = SH::NMAX;
     constexpr bool PAIRS = sweep_pairs<SH, MOVE>() > 0;
-    auto P = [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; };
+    const PosCols<T, TPB, SH::NE> P(sp, t);
 #define DI(k, j) sd[((SIG * NM * NM) + (k) * NM + (j)) * TPB + t]
     for (int q = 0; q < NS; ++q) {
         const int e = SIG * SH::NUP + q;
@@ -1082,9 +1110,7 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
         if (prob != prob) flg |= FLAG_NONFINITE;
         // fixed-node rejection: a proposal that changes the sign of psi is refused
         if (md.uacc < prob && R != T(0) && !(fixed_node && R < T(0))) {
-            sp[(3 * e + 0) * TPB + t] = nx;
-            sp[(3 * e + 1) * TPB + t] = ny;
-            sp[(3 * e + 2) * TPB + t] = nz;
+            P.set(e, nx, ny, nz);
             T iR = T(1) / R;
             T cq[NM];
 #pragma unroll
@@ -1119,8 +1145,11 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
                                              unsigned long long* acc_out, int* flags, int fixed_node) {
     constexpr int NM = SH::NMAX;
     const int t = threadIdx.x;
+    const PosCols<T, TPB, SH::NE> P(sp, t);
 #pragma unroll
-    for (int i = 0; i < 3 * SH::NE; ++i) sp[i * TPB + t] = gpos[(size_t)i * Wcap + w];
+    for (int e = 0; e < SH::NE; ++e)
+        P.set(e, gpos[(size_t)(3 * e) * Wcap + w], gpos[(size_t)(3 * e + 1) * Wcap + w],
+              gpos[(size_t)(3 * e + 2) * Wcap + w]);
 #pragma unroll
     for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = gdinv[(size_t)i * Wcap + w];
     T* pc = sd + 2 * NM * NM * TPB + t;
@@ -1128,11 +1157,11 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
     // shared-memory budget of a walker)
     T u1c[SH::NE];
     if constexpr (sweep_pairs<SH, MOVE>() > 0) {
-        pair_cache_fill<SH, T, TPB>(S, [&](int j, int c) -> T { return sp[(3 * j + c) * TPB + t]; }, pc);
+        pair_cache_fill<SH, T, TPB>(S, P, pc);
         if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll 1
             for (int e = 0; e < SH::NE; ++e)
-                u1c[e] = one_body_u(S, sp[(3 * e) * TPB + t], sp[(3 * e + 1) * TPB + t], sp[(3 * e + 2) * TPB + t]);
+                u1c[e] = one_body_u(S, P(e, 0), P(e, 1), P(e, 2));
         }
     }
     int sgn = gsign[w];
@@ -1146,7 +1175,9 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
                                           sgn, acc, flg);
     }
 #pragma unroll
-    for (int i = 0; i < 3 * SH::NE; ++i) gpos[(size_t)i * Wcap + w] = sp[i * TPB + t];
+    for (int e = 0; e < SH::NE; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gpos[(size_t)(3 * e + c) * Wcap + w] = P(e, c);
 #pragma unroll
     for (int i = 0; i < 2 * NM * NM; ++i) gdinv[(size_t)i * Wcap + w] = sd[i * TPB + t];
     gsign[w] = sgn;

@@ -177,6 +177,26 @@ __device__ __forceinline__ MoveDraw<T> move_draw(uint64_t seed, uint32_t walker,
     return d;
 }
 
+// Warp-per-walker sweeps: lane i draws the proposal of electron e0 + i of
+// the sector (i < ns <= 32) once per sweep, and proposal q reads draw q with
+// a shuffle -- the same counters, so the same stream as one draw per move.
+template <class T>
+__device__ __forceinline__ MoveDraw<T> sector_draws(uint64_t seed, uint32_t walker, uint64_t step, int e0, int ns,
+                                                    int lane) {
+    MoveDraw<T> d{T(0), T(0), T(0), T(0)};
+    if (lane < ns) d = move_draw<T>(seed, walker, step, (uint32_t)(e0 + lane));
+    return d;
+}
+template <class T>
+__device__ __forceinline__ MoveDraw<T> draw_of(const MoveDraw<T>& d, int q) {
+    MoveDraw<T> r;
+    r.n0 = __shfl_sync(0xffffffffu, d.n0, q);
+    r.n1 = __shfl_sync(0xffffffffu, d.n1, q);
+    r.n2 = __shfl_sync(0xffffffffu, d.n2, q);
+    r.uacc = __shfl_sync(0xffffffffu, d.uacc, q);
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Orbital evaluation: phi_k(r) = sum_a C[sig][a][k] chi_a(r) for the NS
 // columns of sector SIG, optionally with gradients (MODE >= 1) and

@@ -312,11 +312,13 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
             T (&Di)[NM] = sig == 0 ? Di0 : Di1;
             const int NS = sig == 0 ? NUP : NDN;
             const T kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
+            static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
+            const MoveDraw<T> draws = sector_draws<T>(seed, (uint32_t)w, st, sig * NUP, NS, lane);
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
                 P.get(e, rx, ry, rz);
-                MoveDraw<T> md = move_draw<T>(seed, (uint32_t)w, st, (uint32_t)e);
+                const MoveDraw<T> md = draw_of(draws, q);
                 T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
                 if (MOVE == MOVE_ONE_DRIFT) {
                     // Re(grad ln D) at the current position: lane l sums (i k_j phi_j) Dinv[j][l]

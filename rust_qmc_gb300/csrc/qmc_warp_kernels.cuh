@@ -318,11 +318,13 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
         for (int sig = 0; sig < 2; ++sig) {
             T (&D)[NM] = sig == 0 ? D0 : D1;
             const int NS = sig == 0 ? NUP : NDN;
+            static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
+            const MoveDraw<T> draws = sector_draws<T>(seed, (uint32_t)w, st, sig * NUP, NS, lane);
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
                 P.get(e, rx, ry, rz);
-                MoveDraw<T> md = move_draw<T>(seed, (uint32_t)w, st, (uint32_t)e);
+                const MoveDraw<T> md = draw_of(draws, q);
                 T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
                 T gq[3];
                 if (MOVE == MOVE_ONE_DRIFT) {

@@ -3,6 +3,7 @@
     python -m rust_qmc_gb300.workloads refresh --system ch4_min --walkers 65536
     python -m rust_qmc_gb300.workloads sweeps  --system heg --walkers 16384 --sweeps 8
     python -m rust_qmc_gb300.workloads batch   --systems 512 --sweeps 8
+    python -m rust_qmc_gb300.workloads dmc     --system c6h6 --walkers 16384 --sweeps 4
 
 Each run creates one walker set of the chosen system and precision, seeds it,
 refreshes it once (inverse, log|psi| and E_L from the positions), then times
@@ -10,7 +11,9 @@ the requested operation with CUDA events on the context stream and prints one
 line per repetition.  The first kernel launches of a run are the initial
 refresh, which is what a profiler capture with a launch-count limit sees first.
 ``batch`` instead binds the uneven mix of ``batch_mix`` (one walker set per
-system) into one batch and times graph-captured steps of qmc_batch_run_steps.
+system) into one batch and times graph-captured steps of qmc_batch_run_steps;
+``dmc`` times ``--sweeps`` IS-DMC steps (drift-diffusion sweep, E_L,
+branching and compaction) of a population of ``--walkers`` per repetition.
 """
 import argparse
 import sys
@@ -29,7 +32,7 @@ SYSTEMS = {
     "c6h6": lambda: S.benzene_minimal(),
     "heg": lambda: S.electron_gas(),
 }
-MOVES = {"gauss": L.QMC_MOVE_ONE_GAUSS, "drift": L.QMC_MOVE_ONE_DRIFT}
+MOVES = {"gauss": L.QMC_MOVE_ONE_GAUSS, "drift": L.QMC_MOVE_ONE_DRIFT, "all": L.QMC_MOVE_ALL_GAUSS}
 BATCH_KINDS = ("h2", "li", "ch4_min", "c6h6", "heg")
 
 
@@ -41,6 +44,29 @@ def batch_mix(n, seed=5):
     kinds = [BATCH_KINDS[i % len(BATCH_KINDS)] for i in range(n)]
     walkers = [int(w) for w in rng.integers(256, 4097, size=n)]
     return kinds, walkers
+
+
+def run_dmc(a, ctx, sysh, prec):
+    W = a.walkers
+    wk = Walkers(sysh, W, prec, capacity=4 * W)
+    wk.init(seed=3)
+    e_ref = wk.refresh() / W
+    t = 0
+    for i in range(a.repeat):
+        ctx.synchronize()
+        ctx.record(0)
+        n_moves = 0
+        for _ in range(a.sweeps):
+            n_before = wk.W
+            n, em = wk.dmc_step(0.005, e_ref, seed=1, step=t, fp64_measure=True)
+            t += 1
+            n_moves += n_before * sysh.N
+            e_ref = em - 0.5 * np.log(n / W) / 0.005
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        print("dmc %s W=%d %s: %.3f ms for %d steps  %.3e moves/s  population %d"
+              % (a.system, W, a.precision, ms, a.sweeps, n_moves / ms * 1e3, wk.W), flush=True)
+    wk.close()
 
 
 def run_batch(a, ctx, prec):
@@ -75,7 +101,7 @@ def run_batch(a, ctx, prec):
 
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    p.add_argument("what", choices=["refresh", "sweeps", "batch"])
+    p.add_argument("what", choices=["refresh", "sweeps", "batch", "dmc"])
     p.add_argument("--system", choices=sorted(SYSTEMS), default="ch4_min")
     p.add_argument("--walkers", type=int, default=65536)
     p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
@@ -92,6 +118,11 @@ def main(argv=None):
         return 0
     spec = SYSTEMS[a.system]()
     sysh = System(ctx, spec)
+    if a.what == "dmc":
+        run_dmc(a, ctx, sysh, prec)
+        sysh.close()
+        ctx.close()
+        return 0
     wk = Walkers(sysh, a.walkers, prec)
     wk.init(seed=3)
     wk.refresh()

@@ -7,6 +7,7 @@
 #pragma once
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 #include <cuda_runtime.h>
 #include "qmc_ff.cuh"
 
@@ -78,6 +79,14 @@ struct SysT {
     int init_nuc[SH::NE];           // internal electron order
     int perm[SH::NE];               // internal -> caller electron index
 };
+
+template <int J>
+struct IntC { static constexpr int value = J; };
+template <int N, class F, int... Is>
+__device__ __forceinline__ void unroll_impl(F&& f, std::integer_sequence<int, Is...>) { (f(IntC<Is>{}), ...); }
+// f(IntC<0>{}), ..., f(IntC<N-1>{}) with compile-time indices.
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) { unroll_impl<N>(f, std::make_integer_sequence<int, N>{}); }
 
 // ---------------------------------------------------------------------------
 // Math helpers (float paths use the hardware approximations).

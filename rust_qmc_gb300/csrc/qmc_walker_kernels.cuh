@@ -276,14 +276,6 @@ __device__ __forceinline__ T* pair_slot(T* pa, T* pb, int e) {
     return J < e ? pa + J * TPB : pb + (J * (J - 1) / 2) * TPB;
 }
 
-template <int J>
-struct IntC { static constexpr int value = J; };
-template <int N, class F, int... Is>
-__device__ __forceinline__ void unroll_impl(F&& f, std::integer_sequence<int, Is...>) { (f(IntC<Is>{}), ...); }
-// f(IntC<0>{}), ..., f(IntC<N-1>{}) with compile-time indices.
-template <int N, class F>
-__device__ __forceinline__ void static_for(F&& f) { unroll_impl<N>(f, std::make_integer_sequence<int, N>{}); }
-
 // One-body (electron-nucleus) part of u at one position, summed over nuclei.
 template <class SH, class T>
 __device__ __forceinline__ T one_body_u(const SysT<SH, T>& S, T x, T y, T z) {

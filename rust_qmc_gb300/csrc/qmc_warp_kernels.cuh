@@ -182,7 +182,7 @@ __device__ __forceinline__ void mo_lane(const SysW<T>& S, int sig, int lane, con
         const int cnt = min(32, S.n_ao - base);
         for (int t = 0; t < cnt; ++t) {
             T c = S.C[sig][base + t][lane];
-            v += c * wshfl(ao.v[r], t);
+            if (MODE != 3) v += c * wshfl(ao.v[r], t);
             if (MODE >= 1) {
                 gx += c * wshfl(ao.gx[r], t);
                 gy += c * wshfl(ao.gy[r], t);
@@ -461,7 +461,8 @@ __global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restric
 }
 
 // Full evaluation from positions (refresh + E_L), one warp per walker.
-// Per-warp shared scratch holds the sector's D, grad D and lap D rows.
+// Per-warp shared scratch holds the sector's D rows, then the rows of its
+// inverse; orbital derivatives are evaluated in a second pass.
 template <int NE, int NUP, int NNUC, class TC, class TS>
 __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow, const TS* __restrict__ gpos,
                                                     TS* __restrict__ gdinv, double* __restrict__ glog,
@@ -493,50 +494,49 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             const int NS = sig == 0 ? NUP : NDN;
+            // pass 1: orbital values, row q = electron q, column = lane (MO)
             for (int q = 0; q < NS; ++q) {
-                const int e = sig * NUP + q;
                 TC rx, ry, rz;
-                P.get(e, rx, ry, rz);
-                AOLane<TC, 2> ao;
-                ao_lane<TC, 2>(S, rx, ry, rz, lane, ao);
+                P.get(sig * NUP + q, rx, ry, rz);
+                AOLane<TC, 0> ao;
+                ao_lane<TC, 0>(S, rx, ry, rz, lane, ao);
                 TC v, gx, gy, gz, l;
-                mo_lane<TC, 2>(S, sig, lane, ao, v, gx, gy, gz, l);
-                Mrow[(0 * NM + q) * 32 + lane] = v;
-                Mrow[(1 * NM + q) * 32 + lane] = gx;
-                Mrow[(2 * NM + q) * 32 + lane] = gy;
-                Mrow[(3 * NM + q) * 32 + lane] = gz;
-                Mrow[(4 * NM + q) * 32 + lane] = l;
+                mo_lane<TC, 0>(S, sig, lane, ao, v, gx, gy, gz, l);
+                Mrow[q * 32 + lane] = v;
             }
             __syncwarp();
-            // Gauss-Jordan with partial pivoting: lane j carries column j of [D | I]
-            TC Dc[NM], Ic[NM];
+            // Gauss-Jordan in place with partial pivoting: lane j carries
+            // column j of D and ends with column j of the inverse of the
+            // row-permuted matrix.  Step k: rows k and p = argmax |D[i][k]|
+            // interchanged; row k divided by a = D[k][k], column k becomes
+            // -D[i][k]/a (1/a on the diagonal), the rest loses D[i][k] x row k
+            // -- lane k's update takes the same form with t = 1 + 1/a.  The row
+            // interchanges are undone as column interchanges: lane j gathers
+            // column src(j), src = tau_{n-1}( ... tau_0(j)).
+            TC A[NM];
 #pragma unroll
-            for (int i = 0; i < NM; ++i) {
-                Dc[i] = (i < NS && lane < NS) ? Mrow[(0 * NM + i) * 32 + lane] : TC(i == lane ? 1 : 0);
-                Ic[i] = (i == lane) ? TC(1) : TC(0);
-            }
-#pragma unroll
-            for (int k = 0; k < NM; ++k) {
-                if (k >= NS) break;
-                // pivot search in column k (lane k)
+            for (int i = 0; i < NM; ++i) A[i] = (i < NS && lane < NS) ? Mrow[i * 32 + lane] : TC(i == lane ? 1 : 0);
+            int src = lane;
+            static_for<NM>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                if (k >= NS) return;
                 int p = k;
-                TC best = fabs(Dc[k]);
+                TC best = fabs(A[k]);
 #pragma unroll
                 for (int i = k + 1; i < NM; ++i) {
-                    TC a = fabs(Dc[i]);
+                    TC a = fabs(A[i]);
                     if (i < NS && a > best) { best = a; p = i; }
                 }
                 p = wshfl(p, k);
 #pragma unroll
                 for (int i = k + 1; i < NM; ++i) {
                     bool sw = (i == p);
-                    TC a = Dc[k], b = Dc[i];
-                    Dc[k] = sw ? b : a; Dc[i] = sw ? a : b;
-                    TC c = Ic[k], d = Ic[i];
-                    Ic[k] = sw ? d : c; Ic[i] = sw ? c : d;
+                    TC a = A[k], b = A[i];
+                    A[k] = sw ? b : a; A[i] = sw ? a : b;
                 }
                 if (p != k) sg = -sg;
-                TC piv = wshfl(Dc[k], k);
+                src = (src == k) ? p : ((src == p) ? k : src);
+                TC piv = wshfl(A[k], k);
                 if (!(piv != TC(0))) { ok = false; piv = TC(1); }
                 if (piv < 0) sg = -sg;
                 if constexpr (std::is_same<TC, ff>::value) {
@@ -545,36 +545,45 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
                 } else {
                     logdet += log(fabs((double)piv));
                 }
-                TC ip = TC(1) / piv;
-                Dc[k] *= ip;
-                Ic[k] *= ip;
+                const TC ip = TC(1) / piv;
+                const TC t = (lane == k) ? TC(1) + ip : A[k] * ip;
+                A[k] = (lane == k) ? ip : t;
 #pragma unroll
                 for (int i = 0; i < NM; ++i) {
                     if (i == k || i >= NS) continue;
-                    TC f = wshfl(Dc[i], k);
-                    Dc[i] -= f * Dc[k];
-                    Ic[i] -= f * Ic[k];
+                    const TC f = wshfl(A[i], k);
+                    A[i] -= f * t;
                 }
+            });
+            // unscramble: lane j takes column src(j); then A[k] = D^-1[k][lane]
+#pragma unroll
+            for (int i = 0; i < NM; ++i) {
+                if (i >= NS) break;
+                A[i] = wshfl(A[i], src);
             }
-            // lane j now holds column j of D^-1
             if (write_state && lane < NS) {
 #pragma unroll
                 for (int k = 0; k < NM; ++k)
-                    if (k < NS) gdinv[((size_t)(sig * NM * NM + k * NM + lane)) * Wcap + w] = (TS)Ic[k];
+                    if (k < NS) gdinv[((size_t)(sig * NM * NM + k * NM + lane)) * Wcap + w] = (TS)A[k];
             }
-            // row-wise products for this lane's electron q = lane
-            if (lane < NS) {
-                TC ax = 0, ay = 0, az = 0, al = 0;
+            __syncwarp();
 #pragma unroll
-                for (int k = 0; k < NM; ++k) {
-                    if (k >= NS) break;
-                    TC dk = Ic[k];
-                    ax += Mrow[(1 * NM + lane) * 32 + k] * dk;
-                    ay += Mrow[(2 * NM + lane) * 32 + k] * dk;
-                    az += Mrow[(3 * NM + lane) * 32 + k] * dk;
-                    al += Mrow[(4 * NM + lane) * 32 + k] * dk;
-                }
-                gdx[sig] = ax; gdy[sig] = ay; gdz[sig] = az; ld[sig] = al;
+            for (int k = 0; k < NM; ++k)
+                if (k < NS) Mrow[k * 32 + lane] = A[k];    // row k of D^-1
+            __syncwarp();
+            // pass 2: for electron q, lane k evaluates grad and lap of phi_k(r_q)
+            // and weights them by D^-1[k][q]; warp sums give this sector's
+            // grad ln D and lap D / D of electron q, kept by lane q
+            for (int q = 0; q < NS; ++q) {
+                TC rx, ry, rz;
+                P.get(sig * NUP + q, rx, ry, rz);
+                AOLane<TC, 3> ao;
+                ao_lane<TC, 3>(S, rx, ry, rz, lane, ao);
+                TC v, gx, gy, gz, l;
+                mo_lane<TC, 3>(S, sig, lane, ao, v, gx, gy, gz, l);
+                const TC d = lane < NS ? Mrow[lane * 32 + q] : TC(0);
+                const TC ax = wsum(gx * d), ay = wsum(gy * d), az = wsum(gz * d), al = wsum(l * d);
+                if (lane == q) { gdx[sig] = ax; gdy[sig] = ay; gdz[sig] = az; ld[sig] = al; }
             }
             __syncwarp();
         }
@@ -680,7 +689,7 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
     load_sysw(&S, Sg);
     const int wib = threadIdx.x >> 5;
     const int w = blockIdx.x * WPB + wib;
-    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;   // [5][NM rows][32 lanes]
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * 32;   // [NM rows][32 lanes]
     double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, gpos, gdinv, glog, gsign, gel, w, w < W, Wcap,
                                                           write_state, out_grad, out_lap, flags);
     if (partial) warp_block_partial<WPB>(e_l, partial, blockIdx.x);
@@ -694,7 +703,7 @@ __global__ void __launch_bounds__(32 * WPB) kwb_measure(const BatchTile* __restr
     __shared__ SysW<TC> S;
     extern __shared__ __align__(16) unsigned char wsm[];
     const int wib = threadIdx.x >> 5;
-    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * 5 * NM * 32;
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * 32;
     int t0, t1;
     batch_tile_range(ntiles, t0, t1);
     int cur = -1;
@@ -758,7 +767,7 @@ struct WarpShapeOps {
         int rc = table<TC>(hs, &S);
         if (rc) return rc;
         int nb = (dw.W + WB - 1) / WB;
-        size_t smem = sizeof(TC) * WB * 5 * NM * 32;
+        size_t smem = sizeof(TC) * WB * NM * 32;
         auto kern = kw_measure<NE, NUP, NNUC, TC, TS, WB>;
         static bool attr = false;
         if (!attr) {
@@ -775,14 +784,15 @@ struct WarpShapeOps {
         return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
     }
 
-    // Walkers per block of the standalone refresh, 4 or 7, chosen by timing.
-    // The row scratch is per warp and the system table per block, so 7
-    // walkers per block keep 7 warps per SM resident where 4 keep 4; which is
-    // faster depends on the arithmetic type.  A refresh recomputes the same
-    // state whatever the block shape, so the first refresh of at least 1024
-    // walkers per arithmetic type (outside stream capture) runs both shapes,
-    // times each once after a warm-up launch, and keeps the faster.
-    static constexpr int WB_A = 4, WB_B = 7;
+    // Walkers per block of the standalone refresh, 4 or 8, chosen by timing.
+    // The system table is per block and the row scratch per warp, so the two
+    // shapes trade the table's fixed shared-memory cost against registers
+    // per block; which keeps more warps resident and issues faster depends
+    // on the arithmetic type.  A refresh recomputes the same state whatever
+    // the block shape, so the first refresh of at least 1024 walkers per
+    // arithmetic type (outside stream capture) runs both shapes, times each
+    // once after a warm-up launch, and keeps the faster.
+    static constexpr int WB_A = 4, WB_B = 8;
 
     template <class TC, class TS>
     static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
@@ -884,7 +894,7 @@ struct WarpShapeOps {
 
     template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = sizeof(TC) * WPB * 5 * NM * 32;
+        const size_t smem = sizeof(TC) * WPB * NM * 32;
         auto kern = kwb_measure<NE, NUP, NNUC, TC, TS, WPB>;
         static bool attr = false;
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }

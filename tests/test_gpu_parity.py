@@ -484,7 +484,7 @@ def test_refresh_energy_sum_matches_walker_energies(ctx, name):
 
 @pytest.mark.parametrize("prec", [L.QMC_FP32_REFINE, L.QMC_FP64])
 def test_benzene_refresh_block_shapes_agree(ctx, prec):
-    """The benzene refresh picks 4 or 7 walkers per block by timing both on
+    """The benzene refresh picks 4 or 8 walkers per block by timing both on
     its first call of 1024+ walkers; both shapes compute each walker alike,
     so the walker state after the tuning call equals the state after a later
     call with the chosen shape, bit for bit."""

@@ -12,8 +12,9 @@ line per repetition.  The first kernel launches of a run are the initial
 refresh, which is what a profiler capture with a launch-count limit sees first.
 ``batch`` instead binds the uneven mix of ``batch_mix`` (one walker set per
 system) into one batch and times graph-captured steps of qmc_batch_run_steps;
-``dmc`` times ``--sweeps`` IS-DMC steps (drift-diffusion sweep, E_L,
-branching and compaction) of a population of ``--walkers`` per repetition.
+``dmc`` equilibrates ``--walkers`` with 128 Gaussian sweeps, then times
+``--sweeps`` IS-DMC steps (drift-diffusion sweep, E_L, branching and
+compaction) per repetition.
 """
 import argparse
 import sys
@@ -50,6 +51,12 @@ def run_dmc(a, ctx, sysh, prec):
     W = a.walkers
     wk = Walkers(sysh, W, prec, capacity=4 * W)
     wk.init(seed=3)
+    wk.refresh()
+    # VMC equilibration first (the initial Gaussian clouds give E_L spread so
+    # wide that branching would empty most of the population)
+    for k in range(4):
+        wk.sweep(L.QMC_MOVE_ONE_GAUSS, 32, 32 * k, seed=2, step=0.3, count=False)
+        wk.refresh()
     e_ref = wk.refresh() / W
     t = 0
     for i in range(a.repeat):

@@ -276,10 +276,18 @@ __global__ void khw_init(const SysH<double>* __restrict__ S, TS* __restrict__ po
 }
 
 // Single-electron sweeps, one warp per walker.
+template <class T> struct HComplex;
+template <> struct HComplex<float> { using type = float2; };
+template <> struct HComplex<double> { using type = double2; };
+// Shared bytes per warp of the sweep's inverse columns (both sectors).
+template <int NM, class T>
+__host__ __device__ constexpr size_t hsweep_warp_bytes() { return sizeof(T) * 2 * 2 * NM * 32; }
+
 template <int NE, int NUP, class T, int MOVE>
 __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict__ gpos, T* __restrict__ gdinv,
-                                                 int w, int Wcap, int n_sweeps, uint64_t step0, T step, T tau,
-                                                 T maxd, uint64_t seed, unsigned long long* acc_out, int* flags) {
+                                                 typename HComplex<T>::type* Dsh, int w, int Wcap, int n_sweeps,
+                                                 uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+                                                 unsigned long long* acc_out, int* flags) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
     const int lane = threadIdx.x & 31;
@@ -292,15 +300,20 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
         P.y[r] = ok ? gpos[(3 * j + 1) * (size_t)Wcap + w] : T(0);
         P.z[r] = ok ? gpos[(3 * j + 2) * (size_t)Wcap + w] : T(0);
     }
-    // complex inverse columns: [sector][k] (re, im); storage [2][NM*NM][2][Wcap]
-    T Dr0[NM], Di0[NM], Dr1[NM], Di1[NM];
+    // complex inverse columns in the warp's shared rows: Dsh[(sig NM + k) 32 + lane]
+    // = D^-1[k][lane] (re, im) of sector sig; each lane touches only its own
+    // column (HBM storage [2][NM*NM][2][Wcap])
+    using C2 = typename HComplex<T>::type;
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
         size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
-        Dr0[k] = lane < NUP ? gdinv[b0 + w] : T(0);
-        Di0[k] = lane < NUP ? gdinv[b0 + Wcap + w] : T(0);
-        Dr1[k] = lane < NDN ? gdinv[b1 + w] : T(0);
-        Di1[k] = lane < NDN ? gdinv[b1 + Wcap + w] : T(0);
+        C2 d0, d1;
+        d0.x = lane < NUP ? gdinv[b0 + w] : T(0);
+        d0.y = lane < NUP ? gdinv[b0 + Wcap + w] : T(0);
+        d1.x = lane < NDN ? gdinv[b1 + w] : T(0);
+        d1.y = lane < NDN ? gdinv[b1 + Wcap + w] : T(0);
+        Dsh[(0 * NM + k) * 32 + lane] = d0;
+        Dsh[(1 * NM + k) * 32 + lane] = d1;
     }
     unsigned acc = 0;
     int flg = 0;
@@ -308,8 +321,7 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
         const uint64_t st = step0 + (uint64_t)it;
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
-            T (&Dr)[NM] = sig == 0 ? Dr0 : Dr1;
-            T (&Di)[NM] = sig == 0 ? Di0 : Di1;
+            C2* Dc = Dsh + sig * NM * 32 + lane;      // Dc[k * 32] = D^-1[k][lane]
             const int NS = sig == 0 ? NUP : NDN;
             const T kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
             static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
@@ -325,12 +337,13 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                     T s, c;
                     fsincos(kx * rx + ky * ry + kz * rz, &s, &c);
                     T ax = 0, ay = 0, az = 0;
-#pragma unroll
+#pragma unroll 9
                     for (int j = 0; j < NM; ++j) {
                         T pr = __shfl_sync(0xffffffffu, c, j), pi = __shfl_sync(0xffffffffu, s, j);
                         T kjx = S.kvec[sig][j][0], kjy = S.kvec[sig][j][1], kjz = S.kvec[sig][j][2];
                         // Re(i k phi D) = -k Im(phi D)
-                        T im = pr * Di[j] + pi * Dr[j];
+                        const C2 d = Dc[j * 32];
+                        T im = pr * d.y + pi * d.x;
                         ax -= kjx * im; ay -= kjy * im; az -= kjz * im;
                     }
                     ax = __shfl_sync(0xffffffffu, ax, q); ay = __shfl_sync(0xffffffffu, ay, q); az = __shfl_sync(0xffffffffu, az, q);
@@ -348,11 +361,12 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                 fsincos(kx * nx + ky * ny + kz * nz, &ps, &pc);
                 // t_l = sum_j phi_j Dinv[j][l]; R = t_q
                 T tr = 0, ti = 0;
-#pragma unroll
+#pragma unroll 9
                 for (int j = 0; j < NM; ++j) {
                     T pr = __shfl_sync(0xffffffffu, pc, j), pi = __shfl_sync(0xffffffffu, ps, j);
-                    tr += pr * Dr[j] - pi * Di[j];
-                    ti += pr * Di[j] + pi * Dr[j];
+                    const C2 d = Dc[j * 32];
+                    tr += pr * d.x - pi * d.y;
+                    ti += pr * d.y + pi * d.x;
                 }
                 const T Rr = __shfl_sync(0xffffffffu, tr, q), Ri = __shfl_sync(0xffffffffu, ti, q);
                 const T R2 = Rr * Rr + Ri * Ri;
@@ -361,10 +375,11 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                 if (MOVE == MOVE_ONE_DRIFT) {
                     // Re(grad ln D') = Re(G / R) with G = sum_j i k_j phi_j(r') Dinv[j][q]
                     T Gx_r = 0, Gy_r = 0, Gz_r = 0, Gx_i = 0, Gy_i = 0, Gz_i = 0;
-#pragma unroll
+#pragma unroll 9
                     for (int j = 0; j < NM; ++j) {
                         T pr = __shfl_sync(0xffffffffu, pc, j), pi = __shfl_sync(0xffffffffu, ps, j);
-                        T re = pr * Dr[j] - pi * Di[j], im = pr * Di[j] + pi * Dr[j];
+                        const C2 d = Dc[j * 32];
+                        T re = pr * d.x - pi * d.y, im = pr * d.y + pi * d.x;
                         T kjx = S.kvec[sig][j][0], kjy = S.kvec[sig][j][1], kjz = S.kvec[sig][j][2];
                         Gx_r -= kjx * im; Gy_r -= kjy * im; Gz_r -= kjz * im;
                         Gx_i += kjx * re; Gy_i += kjy * re; Gz_i += kjz * re;
@@ -397,13 +412,14 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                     const T iR2 = T(1) / R2;
                     const T iRr = Rr * iR2, iRi = -Ri * iR2;              // 1/R
                     const T fr = tr * iRr - ti * iRi, fi = tr * iRi + ti * iRr;   // t_l / R
-#pragma unroll
+#pragma unroll 9
                     for (int k = 0; k < NM; ++k) {
-                        T qr = __shfl_sync(0xffffffffu, Dr[k], q), qi = __shfl_sync(0xffffffffu, Di[k], q);
-                        T nr, ni;
-                        if (lane == q) { nr = qr * iRr - qi * iRi; ni = qr * iRi + qi * iRr; }
-                        else { nr = Dr[k] - (qr * fr - qi * fi); ni = Di[k] - (qr * fi + qi * fr); }
-                        Dr[k] = nr; Di[k] = ni;
+                        const C2 d = Dc[k * 32];
+                        T qr = __shfl_sync(0xffffffffu, d.x, q), qi = __shfl_sync(0xffffffffu, d.y, q);
+                        C2 n;
+                        if (lane == q) { n.x = qr * iRr - qi * iRi; n.y = qr * iRi + qi * iRr; }
+                        else { n.x = d.x - (qr * fr - qi * fi); n.y = d.y - (qr * fi + qi * fr); }
+                        Dc[k * 32] = n;
                     }
                     ++acc;
                 }
@@ -422,8 +438,9 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
         size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
-        if (lane < NUP) { gdinv[b0 + w] = Dr0[k]; gdinv[b0 + Wcap + w] = Di0[k]; }
-        if (lane < NDN) { gdinv[b1 + w] = Dr1[k]; gdinv[b1 + Wcap + w] = Di1[k]; }
+        const C2 d0 = Dsh[(0 * NM + k) * 32 + lane], d1 = Dsh[(1 * NM + k) * 32 + lane];
+        if (lane < NUP) { gdinv[b0 + w] = d0.x; gdinv[b0 + Wcap + w] = d0.y; }
+        if (lane < NDN) { gdinv[b1 + w] = d1.x; gdinv[b1 + Wcap + w] = d1.y; }
     }
     if (lane == 0) {
         if (acc) atomicAdd(acc_out, (unsigned long long)acc);
@@ -432,24 +449,32 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
 }
 
 template <int NE, int NUP, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
+// 16 warps per SM for FP32 walkers (four blocks of four: 56 KB of shared
+// memory each, at most 128 registers), 8 for FP64 walkers.
+__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
                                                       T* __restrict__ gdinv, int W, int Wcap, int n_sweeps,
                                                       uint64_t step0, T step, T tau, T maxd, uint64_t seed,
                                                       unsigned long long* acc_out, int* flags) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     __shared__ SysH<T> S;
+    extern __shared__ __align__(16) unsigned char hsm[];
     load_sysh(&S, Sg, (int)sizeof(SysH<T>));
     const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
     if (w >= W) return;
-    khw_sweep_walker<NE, NUP, T, MOVE>(S, gpos, gdinv, w, Wcap, n_sweeps, step0, step, tau, maxd, seed, acc_out,
-                                       flags);
+    auto* Dsh = reinterpret_cast<typename HComplex<T>::type*>(hsm) + (size_t)(threadIdx.x >> 5) * 2 * NM * 32;
+    khw_sweep_walker<NE, NUP, T, MOVE>(S, gpos, gdinv, Dsh, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
+                                       acc_out, flags);
 }
 
 // Batched form: persistent blocks over (system, WPB-walker tile) pairs.
 template <int NE, int NUP, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                        const BatchRec* __restrict__ recs,
                                                        const BatchCtl* __restrict__ ctl) {
+    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     __shared__ SysH<T> S;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    auto* Dsh = reinterpret_cast<typename HComplex<T>::type*>(hsm) + (size_t)(threadIdx.x >> 5) * 2 * NM * 32;
     const BatchCtl c = *ctl;
     int t0, t1;
     batch_tile_range(ntiles, t0, t1);
@@ -464,7 +489,7 @@ __global__ void __launch_bounds__(32 * WPB) khwb_sweep(const BatchTile* __restri
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + (int)(threadIdx.x >> 5);
         if (w < R.W)
-            khw_sweep_walker<NE, NUP, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, w, R.Wcap, c.n_sweeps, c.step,
+            khw_sweep_walker<NE, NUP, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, Dsh, w, R.Wcap, c.n_sweeps, c.step,
                                                (T)c.step_size, (T)c.tau, (T)c.max_drift,
                                                batch_system_seed(c.seed, R.index), R.acc, R.flags);
     }
@@ -917,10 +942,17 @@ struct HegShapeOps {
     template <class T, int MOVE>
     static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
         auto kern = khwb_sweep<NE, NUP, T, MOVE, WPB>;
-        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, 0) == cudaSuccess ? 0 : 2;
+        const size_t smem = WPB * hsweep_warp_bytes<NM, T>();
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
         const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
-        kern<<<grid, 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
@@ -1002,8 +1034,16 @@ struct HegShapeOps {
         int rc = table<T>(hs, &S);
         if (rc) return rc;
         int nb = (dw.W + WPB - 1) / WPB;
-        khw_sweep<NE, NUP, T, MOVE, WPB><<<nb, 32 * WPB, 0, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.W, dw.Wcap, n, s0,
-                                                                (T)step, (T)tau, (T)maxd, seed, dw.acc, dw.flags);
+        auto kern = khw_sweep<NE, NUP, T, MOVE, WPB>;
+        const size_t smem = WPB * hsweep_warp_bytes<NM, T>();
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
+        kern<<<nb, 32 * WPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.W, dw.Wcap, n, s0, (T)step, (T)tau, (T)maxd,
+                                         seed, dw.acc, dw.flags);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }

@@ -553,9 +553,9 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 Ai[i] = in ? Mi[i * 32 + lane] : TC(0);
             }
             int src = lane;
-#pragma unroll
-            for (int k = 0; k < NM; ++k) {
-                if (k >= NS) break;
+            static_for<NM>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                if (k >= NS) return;
                 int p = k;
                 TC best = Ar[k] * Ar[k] + Ai[k] * Ai[k];
 #pragma unroll
@@ -595,7 +595,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     TC fr = hshfl(Ar[i], k), fi = hshfl(Ai[i], k);
                     Ar[i] -= fr * tr - fi * ti; Ai[i] -= fr * ti + fi * tr;
                 }
-            }
+            });
             // unscramble: lane j takes column src(j)
 #pragma unroll
             for (int i = 0; i < NM; ++i) {

@@ -147,6 +147,60 @@ __device__ __forceinline__ void fsincos(ff x, ff* s, ff* c) {
     *c = ff(cd);
 }
 
+// erfc on [0, 6] in float-float arithmetic (0 beyond): the Chebyshev
+// interpolant erfc(x) = c_0 / 2 + sum_{k=1..42} c_k T_k(t), t = x / 3 - 1,
+// through 64 first-kind nodes (coefficients from gen_erfc_table.py, mpmath
+// at 40 digits; |c_k| < 2e-18 beyond k = 42), summed by Clenshaw's
+// recurrence: terms k >= 24 in FP32 (their partial sums stay below 1e-7),
+// the rest in float-float.  Absolute error below 2e-14 on [0, 6].
+static __constant__ const ff kErfcCheb[24] = {
+    ff(3.673991e-01f, -6.9200334e-09f),
+    ff(-3.3617035e-01f, 1.6510556e-09f),
+    ff(2.5549158e-01f, 9.960313e-09f),
+    ff(-1.5657288e-01f, 9.566121e-10f),
+    ff(7.125926e-02f, -5.790789e-10f),
+    ff(-1.7145663e-02f, 7.2621587e-10f),
+    ff(-5.9834975e-03f, -6.355615e-11f),
+    ff(9.309509e-03f, 1.6978224e-11f),
+    ff(-5.190865e-03f, 1.0619118e-10f),
+    ff(1.1763682e-03f, 4.8458522e-11f),
+    ff(5.319446e-04f, 3.415539e-13f),
+    ff(-6.203452e-04f, 1.8230945e-11f),
+    ff(2.4648002e-04f, 1.3352023e-11f),
+    ff(-4.3256662e-07f, -1.3714815e-14f),
+    ff(-5.34781e-05f, 3.0843093e-13f),
+    ff(2.795329e-05f, -6.6343177e-13f),
+    ff(-3.1002157e-06f, 4.7403328e-14f),
+    ff(-3.9868787e-06f, 1.6839862e-13f),
+    ff(2.4134415e-06f, 3.8801173e-14f),
+    ff(-3.3472375e-07f, 2.2182666e-15f),
+    ff(-2.8443293e-07f, 9.959113e-15f),
+    ff(1.730987e-07f, 5.6202656e-15f),
+    ff(-2.0892596e-08f, -6.1127414e-16f),
+    ff(-1.984897e-08f, -5.560824e-16f)};
+static __constant__ const float kErfcChebTail[19] = {1.05052615e-08f, -7.149105e-10f, -1.2955014e-09f, 5.301936e-10f, 9.567597e-12f, -7.440549e-11f, 2.116448e-11f, 3.314318e-12f, -3.5774686e-12f, 5.862873e-13f, 2.661633e-13f, -1.3746954e-13f, 4.9925553e-15f, 1.3928812e-14f, -3.9142388e-15f, -5.4379457e-16f, 5.295314e-16f, -6.445588e-17f, -3.8180913e-17f};
+__device__ __forceinline__ ff erfc_ff(ff x) {
+    if (!(x.hi < 6.0f)) return ff(0.0f);
+    const ff t = x * ff(1.0 / 3.0) - ff(1.0f);
+    const float th2 = 2.0f * t.hi;
+    float b1 = 0.0f, b2 = 0.0f;
+#pragma unroll
+    for (int k = 42; k >= 24; --k) {
+        const float b0 = __fmaf_rn(th2, b1, __fsub_rn(kErfcChebTail[k - 24], b2));
+        b2 = b1;
+        b1 = b0;
+    }
+    ff B1 = ff(b1), B2 = ff(b2);
+    const ff t2 = ff(2.0f * t.hi, 2.0f * t.lo);
+#pragma unroll
+    for (int k = 23; k >= 1; --k) {
+        const ff B0 = t2 * B1 + kErfcCheb[k] - B2;
+        B2 = B1;
+        B1 = B0;
+    }
+    return ff(0.5f * kErfcCheb[0].hi, 0.5f * kErfcCheb[0].lo) + t * B1 - B2;
+}
+
 // Nearest integer of a float-float value (ties resolved by the leading part).
 using ::rint;
 __device__ __forceinline__ ff rint(ff x) {
@@ -681,6 +735,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
         // image term is FP64; the other 26 images lie beyond L/2, where each
         // term is below erfc(alpha L/2)/(L/2), and are summed in FP32.
         double vreal = 0.0;
+        ff vreal_ff = ff(0.0f);
         {
             TC* ps = Mr;                                  // the rows buffer is free again
             __syncwarp();
@@ -705,8 +760,14 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                 if (j >= NE) j -= NE;
                 const TC dx = min_img(ps[3 * i] - ps[3 * j], S), dy = min_img(ps[3 * i + 1] - ps[3 * j + 1], S),
                          dz = min_img(ps[3 * i + 2] - ps[3 * j + 2], S);
-                const double r = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
-                if (r > 1e-10) vreal += erfc((double)S.alpha * r) / r;
+                if constexpr (std::is_same<TC, ff>::value) {
+                    // float-float minimum-image term: no FP64 in this phase
+                    const ff r = fsqrt(dx * dx + dy * dy + dz * dz);
+                    if (r.hi > 1e-10f) vreal_ff += erfc_ff(S.alpha * r) / r;
+                } else {
+                    const double r = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
+                    if (r > 1e-10) vreal += erfc((double)S.alpha * r) / r;
+                }
                 if (S.real_images) {
                     // box units: the image shift is an exact integer, alpha L is
                     // exact in FP32 for the usual splittings, and sqrt and the
@@ -727,7 +788,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                                     acc += __fdiv_rn(erfcf(__fmul_rn(aLf, d)), d);
                                 }
                             }
-                    vreal += (double)acc * (double)S.invL;
+                    if constexpr (std::is_same<TC, ff>::value) vreal_ff += ff(acc) * S.invL;
+                    else vreal += (double)acc * (double)S.invL;
                 }
             }
         }
@@ -813,7 +875,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
         }
         u = hsum(u);
         kin = hsum(kin);
-        vreal = hsum(vreal);
+        vreal = hsum(vreal + (double)vreal_ff);
         double V = vreal + vk + S.ksum_const + S.e_const;
         e_l = -0.5 * (double)kin + V;
         if (lane == 0) {

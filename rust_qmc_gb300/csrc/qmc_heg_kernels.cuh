@@ -139,12 +139,41 @@ __device__ __forceinline__ void load_sysh(SysH<T>* dst, const SysH<T>* __restric
 
 __device__ __forceinline__ void fsincos(double x, double* s, double* c) { sincos(x, s, c); }
 __device__ __forceinline__ void fsincos(float x, float* s, float* c) { __sincosf(x, s, c); }
-// float-float phases through one FP64 sincos
+// float-float sine and cosine without FP64: Cody-Waite reduction
+// r = x - n pi/2 with pi/2 in three FP32 parts (the leading difference is
+// exact by Sterbenz's lemma, the n multiples by TwoProd), then the Taylor
+// series on |r| <= pi/4 -- terms through r^7 (sine) and r^8 (cosine) in
+// float-float, the rest (below 3.1e-7) in FP32 -- and the quadrant n mod 4.
+// Absolute error below 1e-13 for |x| <= 60.
 __device__ __forceinline__ void fsincos(ff x, ff* s, ff* c) {
-    double sd, cd;
-    sincos((double)x, &sd, &cd);
-    *s = ff(sd);
-    *c = ff(cd);
+    const float n = rintf(__fmul_rn(x.hi, 0.63661975f));
+    const ff p = ff_two_prod(1.5707964f, n), q = ff_two_prod(-4.371139e-08f, n);
+    ff r = ff(__fsub_rn(x.hi, p.hi)) + ff(x.lo);
+    r = r + ff(-p.lo);
+    r = r - q;
+    r = r + ff(-__fmul_rn(-1.7151245e-15f, n));
+    const ff r2 = r * r;
+    const float h2 = r2.hi;
+    // sin r = r + r^3 (-1/3! + r^2 (1/5! + r^2 (-1/7! + r^2 (1/9! - r^2/11! + r^4/13!))))
+    const float qs = __fmul_rn(h2, __fmaf_rn(h2, __fmaf_rn(h2, 1.6059044e-10f, -2.5052108e-08f), 2.7557319e-06f));
+    ff cs = ff(-1.0 / 5040.0) + ff(qs);
+    cs = cs * r2 + ff(1.0 / 120.0);
+    cs = cs * r2 + ff(-1.0 / 6.0);
+    const ff sn = r + cs * r2 * r;
+    // cos r = 1 + r^2 (-1/2 + r^2 (1/4! + r^2 (-1/6! + r^2 (1/8! + r^2 (-1/10! + r^2/12! - ...)))))
+    const float qc = __fmaf_rn(h2, __fmaf_rn(h2, __fmaf_rn(h2, 4.7794773e-14f, -1.1470746e-11f), 2.0876757e-09f),
+                               -2.7557319e-07f);
+    ff cc = ff(1.0 / 40320.0) + ff(__fmul_rn(qc, h2));
+    cc = cc * r2 + ff(-1.0 / 720.0);
+    cc = cc * r2 + ff(1.0 / 24.0);
+    cc = cc * r2 + ff(-0.5);
+    const ff cn = ff(1.0f) + cc * r2;
+    switch ((int)n & 3) {
+        case 0: *s = sn; *c = cn; break;
+        case 1: *s = cn; *c = -sn; break;
+        case 2: *s = -sn; *c = -cn; break;
+        default: *s = -cn; *c = sn; break;
+    }
 }
 
 // erfc on [0, 6] in float-float arithmetic (0 beyond): the Chebyshev

@@ -18,7 +18,7 @@
 // reciprocal and square roots take one Newton correction from the FP32
 // hardware seed; exp is table-driven (Tang, ACM TOMS 15 (1989)): a
 // Cody-Waite reduction by ln2/32, a 32-entry table of 2^(j/32) and a short
-// polynomial, with relative error ~1e-13.  Every intrinsic below is
+// polynomial, with relative error below 5e-13.  Every intrinsic below is
 // an IEEE round-to-nearest FP32 operation (__fadd_rn etc.), which the
 // compiler neither contracts nor reassociates.
 #pragma once

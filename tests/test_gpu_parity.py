@@ -530,3 +530,24 @@ def test_rebuild_inverse_matches_refresh(ctx, name, prec):
     assert np.array_equal(la0, la1) and np.array_equal(sg0, sg1)
     assert np.array_equal(p0, p1)
     assert f0 == 0 and f1 == 0
+
+
+@pytest.mark.parametrize("name", ["h2", "li_ref", "ch4_min", "ch4_gto"])
+def test_fp64_gaussian_sweeps_ragged_walker_count(ctx, oracle, name):
+    """Gaussian single-electron sweeps of 97 walkers (a partial last block of
+    the 64-walker sweep blocks, with their shared-memory pair caches) follow
+    the oracle's chains like full blocks do."""
+    spec = BUILDERS[name]()
+    sysh = Q.System(ctx, spec)
+    W, n = 97, 3
+    wk = Q.Walkers(sysh, W, L.QMC_FP64)
+    wk.init(seed=57)
+    wk.refresh()
+    pos0 = wk.get_positions()
+    acc = wk.sweep(L.QMC_MOVE_ONE_GAUSS, n, 3, seed=777, step=0.3)
+    got = wk.get_positions()
+    want, acc_o, _ = oracle.sweeps(spec, pos0, n, 3, L.QMC_MOVE_ONE_GAUSS, 777, step=0.3, want_energy=False)
+    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
+    assert same.mean() >= 0.98, same.mean()
+    assert same[-33:].mean() >= 0.95            # the walkers of the partial block
+    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))

@@ -872,18 +872,50 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                             tr[r] = qr[r] * zmr[r] - qi[r] * zmi[r];
                             ti[r] = qr[r] * zmi[r] + qi[r] * zmr[r];
                         }
-                        for (int nz = -K; nz <= K; ++nz) {
-                            if (!(nx == 0 && ny == 0 && nz <= 0) && (S.kcube || nz * nz <= rest)) {
-                                TC rr = hsum(tr[0] + tr[1]), ri = hsum(ti[0] + ti[1]);
-                                vkt += kweight<TC>(KT, t) * (rr * rr + ri * ri);
-                                ++t;
-                            }
+                        // nz in chunks of four: the four lane partials of rho_k
+                        // are reduced together (butterfly reduce-scatter: two
+                        // exchanges at distance 16, one at 8, then a full
+                        // reduction over the low three lane bits), after which
+                        // lanes 0, 8, 16, 24 hold chunk values 0..3
+                        const int vi = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
+                        for (int nz0 = -K; nz0 <= K; nz0 += 4) {
+                            TC pr[4], pim[4];
+                            int tk[4];
+                            bool ok4[4];
 #pragma unroll
-                            for (int r = 0; r < 2; ++r) {
-                                TC x = tr[r] * ezr[r] - ti[r] * ezi[r];
-                                ti[r] = tr[r] * ezi[r] + ti[r] * ezr[r];
-                                tr[r] = x;
+                            for (int j = 0; j < 4; ++j) {
+                                const int nz = nz0 + j;
+                                ok4[j] = nz <= K && !(nx == 0 && ny == 0 && nz <= 0) && (S.kcube || nz * nz <= rest);
+                                tk[j] = t;
+                                t += ok4[j] ? 1 : 0;
+                                pr[j] = ok4[j] ? tr[0] + tr[1] : TC(0);
+                                pim[j] = ok4[j] ? ti[0] + ti[1] : TC(0);
+#pragma unroll
+                                for (int r = 0; r < 2; ++r) {
+                                    TC x = tr[r] * ezr[r] - ti[r] * ezi[r];
+                                    ti[r] = tr[r] * ezi[r] + ti[r] * ezr[r];
+                                    tr[r] = x;
+                                }
                             }
+                            const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+                            TC wr[2], wi[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {            // distance 16: keep v_h or v_{h+2}
+                                const TC sr = b4 ? pr[h] : pr[h + 2], si = b4 ? pim[h] : pim[h + 2];
+                                wr[h] = (b4 ? pr[h + 2] : pr[h]) + hshfl_xor(sr, 16);
+                                wi[h] = (b4 ? pim[h + 2] : pim[h]) + hshfl_xor(si, 16);
+                            }
+                            const TC sr = b3 ? wr[0] : wr[1], si = b3 ? wi[0] : wi[1];   // distance 8
+                            TC vr = (b3 ? wr[1] : wr[0]) + hshfl_xor(sr, 8);
+                            TC vim = (b3 ? wi[1] : wi[0]) + hshfl_xor(si, 8);
+#pragma unroll
+                            for (int m = 4; m > 0; m >>= 1) {
+                                vr += hshfl_xor(vr, m);
+                                vim += hshfl_xor(vim, m);
+                            }
+                            const bool okv = vi == 0 ? ok4[0] : (vi == 1 ? ok4[1] : (vi == 2 ? ok4[2] : ok4[3]));
+                            const int tv = vi == 0 ? tk[0] : (vi == 1 ? tk[1] : (vi == 2 ? tk[2] : tk[3]));
+                            if ((lane & 7) == 0 && okv) vkt += kweight<TC>(KT, tv) * (vr * vr + vim * vim);
                         }
                     }
 #pragma unroll
@@ -900,7 +932,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     pxr[r] = x;
                 }
             }
-            vk = (double)vkt;
+            vk = (double)hsum(vkt);
         }
         u = hsum(u);
         kin = hsum(kin);

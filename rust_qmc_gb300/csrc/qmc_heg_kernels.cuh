@@ -579,13 +579,21 @@ __global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw
 }
 
 // FP64 (or FP32) full evaluation: complex Gauss-Jordan, kinetic terms, Ewald.
-template <int NE, int NUP, class TC, class TS>
+// PART 0: the whole refresh.  The float-float refresh of FP32 walkers can
+// also run as two launches over per-walker scratch drows [7][NE][Wcap]:
+// PART 1, the determinant half (orbital matrix, inverse, log|D| into glog,
+// grad ln D and lap D / D per electron into drows), and PART 2, the energy
+// half (Jastrow, Ewald sums, E_L), which reads them back.  Each launch
+// carries half the code and PART 2 none of the inversion's registers.
+template <int NE, int NUP, class TC, class TS, int PART = 0>
 __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KTable* __restrict__ KT, TC* Mr,
                                                      const TS* __restrict__ gpos, TS* __restrict__ gdinv,
                                                      double* __restrict__ glog, int* __restrict__ gsign,
                                                      double* __restrict__ gel, int w, bool act, int Wcap,
                                                      int write_state, double* __restrict__ out_grad,
-                                                     double* __restrict__ out_lap, int* flags) {
+                                                     double* __restrict__ out_lap, int* flags,
+                                                     float2* __restrict__ drows = nullptr) {
+    static_assert(PART == 0 || std::is_same<TC, ff>::value, "the two-part refresh is float-float only");
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
     const int lane = threadIdx.x & 31;
@@ -607,6 +615,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
         bool ok = true;
         TC gdx[2] = {0, 0}, gdy[2] = {0, 0}, gdz[2] = {0, 0}, gqx[2] = {0, 0}, gqy[2] = {0, 0}, gqz[2] = {0, 0};
         TC ldet[2] = {0, 0};
+        if constexpr (PART != 2) {
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             const int NS = sig == 0 ? NUP : NDN;
@@ -718,6 +727,39 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
         }
         if constexpr (std::is_same<TC, ff>::value)
             logdet = 0.5 * (log((double)pmag) + (double)pexp * 0.6931471805599453);
+        }
+        if constexpr (PART == 1) {
+#pragma unroll
+            for (int sig = 0; sig < 2; ++sig) {
+                const int NS = sig == 0 ? NUP : NDN;
+                if (lane < NS) {
+                    const int i = sig * NUP + lane;
+                    const TC v[7] = {gdx[sig], gdy[sig], gdz[sig], gqx[sig], gqy[sig], gqz[sig], ldet[sig]};
+#pragma unroll
+                    for (int c = 0; c < 7; ++c) ff_store(drows + (size_t)(c * NE + i) * Wcap + w, v[c]);
+                }
+            }
+            if (lane == 0) {
+                if (!ok) atomicOr(flags, FLAG_SINGULAR);
+                glog[w] = logdet;
+            }
+            return 0.0;
+        }
+        if constexpr (PART == 2) {
+#pragma unroll
+            for (int sig = 0; sig < 2; ++sig) {
+                const int NS = sig == 0 ? NUP : NDN;
+                if (lane < NS) {
+                    const int i = sig * NUP + lane;
+                    TC v[7];
+#pragma unroll
+                    for (int c = 0; c < 7; ++c) v[c] = ff_load(drows + (size_t)(c * NE + i) * Wcap + w);
+                    gdx[sig] = v[0]; gdy[sig] = v[1]; gdz[sig] = v[2];
+                    gqx[sig] = v[3]; gqy[sig] = v[4]; gqz[sig] = v[5]; ldet[sig] = v[6];
+                }
+            }
+            logdet = glog[w];
+        }
         // Jastrow for this lane's electrons (pairs from both ends)
         TC u = 0, kin = 0;
 #pragma unroll
@@ -964,30 +1006,36 @@ __device__ __forceinline__ void hwarp_block_partial(double v, double* partial, i
     __syncthreads();
 }
 
-template <int NE, int NUP, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB, 2) khw_measure(const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT,
-                                                        const TS* __restrict__ gpos,
-                                                        TS* __restrict__ gdinv, double* __restrict__ glog,
-                                                        int* __restrict__ gsign, double* __restrict__ gel, int W,
-                                                        int Wcap, int write_state, double* __restrict__ out_grad,
-                                                        double* __restrict__ out_lap, double* partial, int* flags) {
-    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+// Shared words per warp of a refresh launch: the orbital matrix rows for the
+// determinant half, the positions for the energy half alone.
+template <int NE, int NUP, int PART>
+__host__ __device__ constexpr int hmeasure_warp_words() {
+    return PART == 2 ? 3 * NE : 2 * (NUP > NE - NUP ? NUP : NE - NUP) * 32;
+}
+
+template <int NE, int NUP, class TC, class TS, int WPB, int PART = 0>
+__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 3 : 2) khw_measure(
+    const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT, const TS* __restrict__ gpos,
+    TS* __restrict__ gdinv, double* __restrict__ glog, int* __restrict__ gsign, double* __restrict__ gel, int W,
+    int Wcap, int write_state, double* __restrict__ out_grad, double* __restrict__ out_lap, double* partial,
+    int* flags, float2* __restrict__ drows) {
     extern __shared__ __align__(16) unsigned char hsm[];
     SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
     TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
     load_sysh(&S, Sg, (int)sizeof(SysH<TC>));
     const int wib = threadIdx.x >> 5;
     const int w = blockIdx.x * WPB + wib;
-    double e_l = khw_measure_walker<NE, NUP, TC, TS>(S, KT, rows + (size_t)wib * 2 * NM * 32, gpos, gdinv, glog, gsign,
-                                                     gel, w, w < W, Wcap, write_state, out_grad, out_lap, flags);
-    if (partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
+    double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
+        S, KT, rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(), gpos, gdinv, glog, gsign, gel, w, w < W,
+        Wcap, write_state, out_grad, out_lap, flags, drows);
+    if (PART != 1 && partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
 // Batched form (compute type TC, state written, per-tile E_L partials).
-template <int NE, int NUP, class TC, class TS, int WPB>
-__global__ void __launch_bounds__(32 * WPB, 2) khwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
-                                                         const BatchRec* __restrict__ recs, double* tile_partial) {
-    constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
+template <int NE, int NUP, class TC, class TS, int WPB, int PART = 0>
+__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 3 : 2) khwb_measure(const BatchTile* __restrict__ tiles,
+                                                                         int ntiles, const BatchRec* __restrict__ recs,
+                                                                         double* tile_partial) {
     extern __shared__ __align__(16) unsigned char hsm[];
     SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
     TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
@@ -1003,11 +1051,11 @@ __global__ void __launch_bounds__(32 * WPB, 2) khwb_measure(const BatchTile* __r
         }
         const BatchRec& R = recs[tl.rec];
         const int w = tl.w0 + wib;
-        double e_l = khw_measure_walker<NE, NUP, TC, TS>(S, static_cast<const KTable*>(R.ktab),
-                                                             rows + (size_t)wib * 2 * NM * 32, (const TS*)R.pos,
-                                                             (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap,
-                                                             1, nullptr, nullptr, R.flags);
-        hwarp_block_partial<WPB>(e_l, tile_partial, ti);
+        double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
+            S, static_cast<const KTable*>(R.ktab), rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(),
+            (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr, nullptr, R.flags,
+            R.rows);
+        if (PART != 1) hwarp_block_partial<WPB>(e_l, tile_partial, ti);
     }
 }
 
@@ -1091,10 +1139,15 @@ struct HegShapeOps {
         return 7;
     }
 
-    template <class TC, class TS>
+    template <class TC, class TS, int PART>
+    static size_t measure_smem() {
+        return ((sizeof(SysH<TC>) + 15) / 16) * 16 + sizeof(TC) * WPB * hmeasure_warp_words<NE, NUP, PART>();
+    }
+
+    template <class TC, class TS, int PART>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = ((sizeof(SysH<TC>) + 15) / 16) * 16 + sizeof(TC) * WPB * 2 * NM * 32;
-        auto kern = khwb_measure<NE, NUP, TC, TS, WPB>;
+        const size_t smem = measure_smem<TC, TS, PART>();
+        auto kern = khwb_measure<NE, NUP, TC, TS, WPB, PART>;
         static bool attr = false;
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
@@ -1106,8 +1159,20 @@ struct HegShapeOps {
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
 
+    // FP32 walker sets (which carry the refresh scratch) refresh in two
+    // launches, FP64 ones in one; the occupancy reported for the persistent
+    // grid is the lower of the two halves'.
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
-        return bc.prec == 0 ? batch_measure_t<double, double>(bc, st, occ) : batch_measure_t<ff, float>(bc, st, occ);
+        if (bc.prec == 0) return batch_measure_t<double, double, 0>(bc, st, occ);
+        if (occ) {
+            int o1 = 0, o2 = 0;
+            int rc = batch_measure_t<ff, float, 1>(bc, st, &o1);
+            if (!rc) rc = batch_measure_t<ff, float, 2>(bc, st, &o2);
+            *occ = o1 < o2 ? o1 : o2;
+            return rc;
+        }
+        int rc = batch_measure_t<ff, float, 1>(bc, st, nullptr);
+        return rc ? rc : batch_measure_t<ff, float, 2>(bc, st, nullptr);
     }
 
     static int init(const HostSys& hs, DevWalkers& dw, uint64_t seed, cudaStream_t st) {
@@ -1121,6 +1186,19 @@ struct HegShapeOps {
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
 
+    template <class TC, class TS, int PART>
+    static int launch_measure_part(const SysH<TC>* S, const KTable* KT, DevWalkers& dw, bool ws, const MeasureOut& out,
+                                   double* partial, int nb, cudaStream_t st) {
+        const size_t smem = measure_smem<TC, TS, PART>();
+        auto kern = khw_measure<NE, NUP, TC, TS, WPB, PART>;
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
+        kern<<<nb, 32 * WPB, smem, st>>>(S, KT, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W,
+                                         dw.Wcap, ws ? 1 : 0, out.grad, out.lap, partial, dw.flags, dw.rows);
+        ++g_launch_count;
+        return cudaGetLastError() == cudaSuccess ? 0 : 2;
+    }
+
     template <class TC, class TS>
     static int measure2(const HostSys& hs, DevWalkers& dw, bool ws, const MeasureOut& out, cudaStream_t st) {
         const SysH<TC>* S;
@@ -1128,15 +1206,18 @@ struct HegShapeOps {
         int rc = table<TC>(hs, &S, &KT);
         if (rc) return rc;
         int nb = (dw.W + WPB - 1) / WPB;
-        size_t smem = ((sizeof(SysH<TC>) + 15) / 16) * 16 + sizeof(TC) * WPB * 2 * NM * 32;
-        auto kern = khw_measure<NE, NUP, TC, TS, WPB>;
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         double* partial = (ws && dw.partial && dw.partial_cap >= 2 * nb + 1) ? dw.partial : nullptr;
-        kern<<<nb, 32 * WPB, smem, st>>>(S, KT, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign, dw.el, dw.W,
-                                         dw.Wcap, ws ? 1 : 0, out.grad, out.lap, partial, dw.flags);
-        ++g_launch_count;
-        if (cudaGetLastError() != cudaSuccess) return 2;
+        bool two = false;
+        if constexpr (std::is_same<TC, ff>::value) two = ws && dw.rows && !out.grad && !out.lap;
+        if (two) {
+            if constexpr (std::is_same<TC, ff>::value) {
+                rc = launch_measure_part<TC, TS, 1>(S, KT, dw, ws, out, nullptr, nb, st);
+                if (!rc) rc = launch_measure_part<TC, TS, 2>(S, KT, dw, ws, out, partial, nb, st);
+            }
+        } else {
+            rc = launch_measure_part<TC, TS, 0>(S, KT, dw, ws, out, partial, nb, st);
+        }
+        if (rc) return rc;
         if (!partial) return 0;
         return launch_sum_partials(partial, nb, 1, dw.partial + dw.partial_cap - 1, st);
     }

@@ -53,6 +53,8 @@ size_t refresh_rows_bytes(int shape) {
         case SHAPE_LI: return b(ShapeLi::NE, ShapeLi::NMAX);
         case SHAPE_CH4: return b(ShapeCH4::NE, ShapeCH4::NMAX);
         case SHAPE_CH4MIN: return b(ShapeCH4Min::NE, ShapeCH4Min::NMAX);
+        // two-pass electron-gas refresh: 7 float-float terms per electron (54)
+        case SHAPE_HEG54: return (size_t)8 * 54 * 7;
     }
     return 0;
 }

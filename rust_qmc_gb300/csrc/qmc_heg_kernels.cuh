@@ -1014,7 +1014,7 @@ __host__ __device__ constexpr int hmeasure_warp_words() {
 }
 
 template <int NE, int NUP, class TC, class TS, int WPB, int PART = 0>
-__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 3 : 2) khw_measure(
+__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khw_measure(
     const SysH<TC>* __restrict__ Sg, const KTable* __restrict__ KT, const TS* __restrict__ gpos,
     TS* __restrict__ gdinv, double* __restrict__ glog, int* __restrict__ gsign, double* __restrict__ gel, int W,
     int Wcap, int write_state, double* __restrict__ out_grad, double* __restrict__ out_lap, double* partial,
@@ -1033,7 +1033,7 @@ __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 3 : 2) khw_measure(
 
 // Batched form (compute type TC, state written, per-tile E_L partials).
 template <int NE, int NUP, class TC, class TS, int WPB, int PART = 0>
-__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 3 : 2) khwb_measure(const BatchTile* __restrict__ tiles,
+__global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khwb_measure(const BatchTile* __restrict__ tiles,
                                                                          int ntiles, const BatchRec* __restrict__ recs,
                                                                          double* tile_partial) {
     extern __shared__ __align__(16) unsigned char hsm[];
@@ -1152,8 +1152,21 @@ struct HegShapeOps {
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        const int grid =
-            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
+        int grid_full = bc.grid_measure;
+        if (PART == 2) {
+            // the energy half keeps more blocks resident than the determinant
+            // half the class grid is sized for: its own resident-slot count
+            static int slots = 0;
+            if (!slots) {
+                int dev = 0, nsm = 0, o = 0;
+                if (cudaGetDevice(&dev) == cudaSuccess &&
+                    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 32 * WPB, smem) == cudaSuccess)
+                    slots = o * nsm;
+            }
+            if (slots > grid_full) grid_full = slots;
+        }
+        const int grid = grid_full > 0 ? (grid_full < bc.ntiles ? grid_full : bc.ntiles) : bc.ntiles;
         kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;

@@ -37,12 +37,12 @@ MOVES = {"gauss": L.QMC_MOVE_ONE_GAUSS, "drift": L.QMC_MOVE_ONE_DRIFT, "all": L.
 BATCH_KINDS = ("h2", "li", "ch4_min", "c6h6", "heg")
 
 
-def batch_mix(n, seed=5):
+def batch_mix(n, seed=5, kinds=BATCH_KINDS):
     """The uneven-batch workload: n systems cycling over H2, Li, CH4 (9 AO),
-    benzene and the 54-electron gas, walker counts drawn from U{256..4096}
-    by a seeded generator."""
+    benzene and the 54-electron gas (or the given subset), walker counts drawn
+    from U{256..4096} by a seeded generator."""
     rng = np.random.default_rng(seed)
-    kinds = [BATCH_KINDS[i % len(BATCH_KINDS)] for i in range(n)]
+    kinds = [kinds[i % len(kinds)] for i in range(n)]
     walkers = [int(w) for w in rng.integers(256, 4097, size=n)]
     return kinds, walkers
 
@@ -77,7 +77,7 @@ def run_dmc(a, ctx, sysh, prec):
 
 
 def run_batch(a, ctx, prec):
-    kinds, walkers = batch_mix(a.systems)
+    kinds, walkers = batch_mix(a.systems, kinds=tuple(a.kinds.split(",")) if a.kinds else BATCH_KINDS)
     specs = {k: SYSTEMS[k]() for k in set(kinds)}
     handles = {k: System(ctx, specs[k]) for k in specs}
     sets = []
@@ -116,6 +116,7 @@ def main(argv=None):
     p.add_argument("--move", choices=sorted(MOVES), default="gauss")
     p.add_argument("--repeat", type=int, default=3)
     p.add_argument("--systems", type=int, default=512, help="systems in the uneven batch (batch)")
+    p.add_argument("--kinds", default="", help="comma-separated subset of %s (batch)" % ",".join(BATCH_KINDS))
     a = p.parse_args(argv)
     prec = L.QMC_FP32_REFINE if a.precision == "fp32" else L.QMC_FP64
     ctx = Context(0)

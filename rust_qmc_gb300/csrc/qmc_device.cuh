@@ -493,6 +493,30 @@ __device__ __forceinline__ void block_partial(double v, double* partial, int slo
     __syncthreads();
 }
 
+// A warp-per-walker sweep's arrays and controls.  The standalone kernels fill
+// one from their parameters, which ptxas re-reads at each use rather than
+// holding registers across the sweep loop.  The batched kernels keep one per
+// block in shared memory and pass it as volatile, so that each use is a
+// shared load and, again, nothing is held in registers across the loop (a
+// copy loaded once from the batch record in global memory would be).
+template <class T>
+struct SweepArgs {
+    T* pos;
+    T* dinv;
+    int* sign;
+    unsigned long long* acc;
+    int* flags;
+    uint64_t step0, seed;
+    T step, tau, maxd;
+    int W, Wcap, n_sweeps, fixed_node;
+};
+
+template <class T>
+__device__ __forceinline__ SweepArgs<T> sweep_args(const BatchRec& R, const BatchCtl& c) {
+    return SweepArgs<T>{(T*)R.pos, (T*)R.dinv, R.sign, R.acc, R.flags, c.step, batch_system_seed(c.seed, R.index),
+                        (T)c.step_size, (T)c.tau, (T)c.max_drift, R.W, R.Wcap, c.n_sweeps, R.fixed_node};
+}
+
 // Persistent batched launches: block b owns the contiguous run of tiles
 // [t0, t1) of the class's tile list, so consecutive tiles mostly share a
 // system and its table is staged once per run.

@@ -366,11 +366,9 @@ template <> struct HComplex<double> { using type = double2; };
 template <int NM, class T>
 __host__ __device__ constexpr size_t hsweep_warp_bytes() { return sizeof(T) * 2 * 2 * NM * 32; }
 
-template <int NE, int NUP, class T, int MOVE>
-__device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict__ gpos, T* __restrict__ gdinv,
-                                                 typename HComplex<T>::type* Dsh, int w, int Wcap, int n_sweeps,
-                                                 uint64_t step0, T step, T tau, T maxd, uint64_t seed,
-                                                 unsigned long long* acc_out, int* flags) {
+// A is const volatile SweepArgs<T> (block-shared; see SweepArgs).
+template <int NE, int NUP, class T, int MOVE, class A>
+__device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, A& a, typename HComplex<T>::type* Dsh, int w) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
     const int lane = threadIdx.x & 31;
@@ -379,9 +377,9 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
     for (int r = 0; r < 2; ++r) {
         const int j = lane + 32 * r;
         const bool ok = j < NE;
-        P.x[r] = ok ? gpos[(3 * j + 0) * (size_t)Wcap + w] : T(0);
-        P.y[r] = ok ? gpos[(3 * j + 1) * (size_t)Wcap + w] : T(0);
-        P.z[r] = ok ? gpos[(3 * j + 2) * (size_t)Wcap + w] : T(0);
+        P.x[r] = ok ? a.pos[(3 * j + 0) * (size_t)a.Wcap + w] : T(0);
+        P.y[r] = ok ? a.pos[(3 * j + 1) * (size_t)a.Wcap + w] : T(0);
+        P.z[r] = ok ? a.pos[(3 * j + 2) * (size_t)a.Wcap + w] : T(0);
     }
     // complex inverse columns in the warp's shared rows: Dsh[(sig NM + k) 32 + lane]
     // = D^-1[k][lane] (re, im) of sector sig; each lane touches only its own
@@ -389,26 +387,26 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
     using C2 = typename HComplex<T>::type;
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
-        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
+        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * a.Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * a.Wcap;
         C2 d0, d1;
-        d0.x = lane < NUP ? gdinv[b0 + w] : T(0);
-        d0.y = lane < NUP ? gdinv[b0 + Wcap + w] : T(0);
-        d1.x = lane < NDN ? gdinv[b1 + w] : T(0);
-        d1.y = lane < NDN ? gdinv[b1 + Wcap + w] : T(0);
+        d0.x = lane < NUP ? a.dinv[b0 + w] : T(0);
+        d0.y = lane < NUP ? a.dinv[b0 + a.Wcap + w] : T(0);
+        d1.x = lane < NDN ? a.dinv[b1 + w] : T(0);
+        d1.y = lane < NDN ? a.dinv[b1 + a.Wcap + w] : T(0);
         Dsh[(0 * NM + k) * 32 + lane] = d0;
         Dsh[(1 * NM + k) * 32 + lane] = d1;
     }
     unsigned acc = 0;
     int flg = 0;
-    for (int it = 0; it < n_sweeps; ++it) {
-        const uint64_t st = step0 + (uint64_t)it;
+    for (int it = 0; it < a.n_sweeps; ++it) {
+        const uint64_t st = a.step0 + (uint64_t)it;
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             C2* Dc = Dsh + sig * NM * 32 + lane;      // Dc[k * 32] = D^-1[k][lane]
             const int NS = sig == 0 ? NUP : NDN;
             const T kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
             static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
-            const MoveDraw<T> draws = sector_draws<T>(seed, (uint32_t)w, st, sig * NUP, NS, lane);
+            const MoveDraw<T> draws = sector_draws<T>(a.seed, (uint32_t)w, st, sig * NUP, NS, lane);
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
@@ -432,12 +430,14 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                     ax = __shfl_sync(0xffffffffu, ax, q); ay = __shfl_sync(0xffffffffu, ay, q); az = __shfl_sync(0xffffffffu, az, q);
                     T g0[3], g1[3];
                     hjastrow_delta<NE, NUP, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
+                    const T tau = a.tau, maxd = a.maxd;
                     dlx = tau * 2 * (ax + g0[0]); dly = tau * 2 * (ay + g0[1]); dlz = tau * 2 * (az + g0[2]);
                     T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
                     if (m > maxd) { T sc = maxd / m; dlx *= sc; dly *= sc; dlz *= sc; }
                     T sd2 = fsqrt(2 * tau);
                     nx = rx + dlx + sd2 * md.n0; ny = ry + dly + sd2 * md.n1; nz = rz + dlz + sd2 * md.n2;
                 } else {
+                    const T step = a.step;
                     nx = rx + step * md.n0; ny = ry + step * md.n1; nz = rz + step * md.n2;
                 }
                 T ps, pc;
@@ -469,6 +469,7 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
                     }
                     Gx_r = __shfl_sync(0xffffffffu, Gx_r, q); Gy_r = __shfl_sync(0xffffffffu, Gy_r, q); Gz_r = __shfl_sync(0xffffffffu, Gz_r, q);
                     Gx_i = __shfl_sync(0xffffffffu, Gx_i, q); Gy_i = __shfl_sync(0xffffffffu, Gy_i, q); Gz_i = __shfl_sync(0xffffffffu, Gz_i, q);
+                    const T tau = a.tau, maxd = a.maxd;
                     T iR2 = R2 > 0 ? T(1) / R2 : T(0);
                     // Re(G / R) = (G_r R_r + G_i R_i) / |R|^2
                     T cx = (Gx_r * Rr + Gx_i * Ri) * iR2 + gn[0];
@@ -513,21 +514,21 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, T* __restrict
     for (int r = 0; r < 2; ++r) {
         const int j = lane + 32 * r;
         if (j < NE) {
-            gpos[(3 * j + 0) * (size_t)Wcap + w] = P.x[r];
-            gpos[(3 * j + 1) * (size_t)Wcap + w] = P.y[r];
-            gpos[(3 * j + 2) * (size_t)Wcap + w] = P.z[r];
+            a.pos[(3 * j + 0) * (size_t)a.Wcap + w] = P.x[r];
+            a.pos[(3 * j + 1) * (size_t)a.Wcap + w] = P.y[r];
+            a.pos[(3 * j + 2) * (size_t)a.Wcap + w] = P.z[r];
         }
     }
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
-        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * Wcap;
+        size_t b0 = ((size_t)(0 * NM * NM + k * NM + lane)) * 2 * a.Wcap, b1 = ((size_t)(1 * NM * NM + k * NM + lane)) * 2 * a.Wcap;
         const C2 d0 = Dsh[(0 * NM + k) * 32 + lane], d1 = Dsh[(1 * NM + k) * 32 + lane];
-        if (lane < NUP) { gdinv[b0 + w] = d0.x; gdinv[b0 + Wcap + w] = d0.y; }
-        if (lane < NDN) { gdinv[b1 + w] = d1.x; gdinv[b1 + Wcap + w] = d1.y; }
+        if (lane < NUP) { a.dinv[b0 + w] = d0.x; a.dinv[b0 + a.Wcap + w] = d0.y; }
+        if (lane < NDN) { a.dinv[b1 + w] = d1.x; a.dinv[b1 + a.Wcap + w] = d1.y; }
     }
     if (lane == 0) {
-        if (acc) atomicAdd(acc_out, (unsigned long long)acc);
-        if (flg) atomicOr(flags, flg);
+        if (acc) atomicAdd(a.acc, (unsigned long long)acc);
+        if (flg) atomicOr(a.flags, flg);
     }
 }
 
@@ -540,42 +541,37 @@ __global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw
                                                       unsigned long long* acc_out, int* flags) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     __shared__ SysH<T> S;
+    __shared__ SweepArgs<T> args;
     extern __shared__ __align__(16) unsigned char hsm[];
-    load_sysh(&S, Sg, (int)sizeof(SysH<T>));
+    if (threadIdx.x == 0)
+        args = SweepArgs<T>{gpos, gdinv, nullptr, acc_out, flags, step0, seed, step, tau, maxd, W, Wcap, n_sweeps, 0};
+    load_sysh(&S, Sg, (int)sizeof(SysH<T>));   // ends with a block barrier
     const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
     if (w >= W) return;
     auto* Dsh = reinterpret_cast<typename HComplex<T>::type*>(hsm) + (size_t)(threadIdx.x >> 5) * 2 * NM * 32;
-    khw_sweep_walker<NE, NUP, T, MOVE>(S, gpos, gdinv, Dsh, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
-                                       acc_out, flags);
+    const volatile SweepArgs<T>& a = args;
+    khw_sweep_walker<NE, NUP, T, MOVE>(S, a, Dsh, w);
 }
 
-// Batched form: persistent blocks over (system, WPB-walker tile) pairs.
+// Batched form: one block per (system, WPB-walker tile); the hardware block
+// scheduler balances uneven systems and classes that run side by side.
 template <int NE, int NUP, class T, int MOVE, int WPB>
 __global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                        const BatchRec* __restrict__ recs,
                                                        const BatchCtl* __restrict__ ctl) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     __shared__ SysH<T> S;
+    __shared__ SweepArgs<T> args;
     extern __shared__ __align__(16) unsigned char hsm[];
+    if ((int)blockIdx.x >= ntiles) return;
     auto* Dsh = reinterpret_cast<typename HComplex<T>::type*>(hsm) + (size_t)(threadIdx.x >> 5) * 2 * NM * 32;
-    const BatchCtl c = *ctl;
-    int t0, t1;
-    batch_tile_range(ntiles, t0, t1);
-    int cur = -1;
-    for (int ti = t0; ti < t1; ++ti) {
-        const BatchTile tl = tiles[ti];
-        if (tl.rec != cur) {
-            __syncthreads();
-            load_sysh(&S, static_cast<const SysH<T>*>(recs[tl.rec].tab_s), (int)sizeof(SysH<T>));
-            cur = tl.rec;
-        }
-        const BatchRec& R = recs[tl.rec];
-        const int w = tl.w0 + (int)(threadIdx.x >> 5);
-        if (w < R.W)
-            khw_sweep_walker<NE, NUP, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, Dsh, w, R.Wcap, c.n_sweeps, c.step,
-                                               (T)c.step_size, (T)c.tau, (T)c.max_drift,
-                                               batch_system_seed(c.seed, R.index), R.acc, R.flags);
-    }
+    const BatchTile tl = tiles[blockIdx.x];
+    if (threadIdx.x == 0) args = sweep_args<T>(recs[tl.rec], *ctl);
+    load_sysh(&S, static_cast<const SysH<T>*>(recs[tl.rec].tab_s), (int)sizeof(SysH<T>));   // ends with a barrier
+    const volatile SweepArgs<T>& a = args;
+    const int w = tl.w0 + (int)(threadIdx.x >> 5);
+    if (w >= a.W) return;
+    khw_sweep_walker<NE, NUP, T, MOVE>(S, a, Dsh, w);
 }
 
 // FP64 (or FP32) full evaluation: complex Gauss-Jordan, kinetic terms, Ewald.
@@ -1031,7 +1027,8 @@ __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khw_measure(
     if (PART != 1 && partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
-// Batched form (compute type TC, state written, per-tile E_L partials).
+// Batched form (compute type TC, state written, per-tile E_L partials), one
+// block per tile.
 template <int NE, int NUP, class TC, class TS, int WPB, int PART = 0>
 __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khwb_measure(const BatchTile* __restrict__ tiles,
                                                                          int ntiles, const BatchRec* __restrict__ recs,
@@ -1039,24 +1036,17 @@ __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khwb_measure(cons
     extern __shared__ __align__(16) unsigned char hsm[];
     SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
     TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
+    if ((int)blockIdx.x >= ntiles) return;
     const int wib = threadIdx.x >> 5;
-    int t0, t1;
-    batch_tile_range(ntiles, t0, t1);
-    int cur = -1;
-    for (int ti = t0; ti < t1; ++ti) {
-        const BatchTile tl = tiles[ti];
-        if (tl.rec != cur) {
-            load_sysh(&S, static_cast<const SysH<TC>*>(recs[tl.rec].tab_d), (int)sizeof(SysH<TC>));
-            cur = tl.rec;
-        }
-        const BatchRec& R = recs[tl.rec];
-        const int w = tl.w0 + wib;
-        double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
-            S, static_cast<const KTable*>(R.ktab), rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(),
-            (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr, nullptr, R.flags,
-            R.rows);
-        if (PART != 1) hwarp_block_partial<WPB>(e_l, tile_partial, ti);
-    }
+    const BatchTile tl = tiles[blockIdx.x];
+    const BatchRec& R = recs[tl.rec];
+    load_sysh(&S, static_cast<const SysH<TC>*>(R.tab_d), (int)sizeof(SysH<TC>));
+    const int w = tl.w0 + wib;
+    double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
+        S, static_cast<const KTable*>(R.ktab), rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(),
+        (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr, nullptr, R.flags,
+        R.rows);
+    if (PART != 1) hwarp_block_partial<WPB>(e_l, tile_partial, blockIdx.x);
 }
 
 int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
@@ -1122,8 +1112,7 @@ struct HegShapeOps {
         }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
-        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        kern<<<bc.ntiles, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
@@ -1152,29 +1141,14 @@ struct HegShapeOps {
         if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        int grid_full = bc.grid_measure;
-        if (PART == 2) {
-            // the energy half keeps more blocks resident than the determinant
-            // half the class grid is sized for: its own resident-slot count
-            static int slots = 0;
-            if (!slots) {
-                int dev = 0, nsm = 0, o = 0;
-                if (cudaGetDevice(&dev) == cudaSuccess &&
-                    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 32 * WPB, smem) == cudaSuccess)
-                    slots = o * nsm;
-            }
-            if (slots > grid_full) grid_full = slots;
-        }
-        const int grid = grid_full > 0 ? (grid_full < bc.ntiles ? grid_full : bc.ntiles) : bc.ntiles;
-        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        kern<<<bc.ntiles, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
 
     // FP32 walker sets (which carry the refresh scratch) refresh in two
-    // launches, FP64 ones in one; the occupancy reported for the persistent
-    // grid is the lower of the two halves'.
+    // launches, FP64 ones in one; the occupancy reported is the lower of the
+    // two halves'.
     static int batch_measure(const BatchClass& bc, cudaStream_t st, int* occ = nullptr) {
         if (bc.prec == 0) return batch_measure_t<double, double, 0>(bc, st, occ);
         if (occ) {

@@ -1,4 +1,4 @@
-// qmc_shape_c6h6_batch.cu -- batched persistent kernels for the c6h6 shape.
+// qmc_shape_c6h6_batch.cu -- batched kernels for the c6h6 shape.
 #include "qmc_warp_kernels.cuh"
 
 namespace qmc {
@@ -10,5 +10,5 @@ int shape_batch_measure_c6h6(const BatchClass& bc, cudaStream_t st, int* occ) {
     return Ops_c6h6::batch_measure(bc, st, occ);
 }
 int shape_batch_tables_c6h6(const HostSys& hs, int prec, BatchRec& r) { return Ops_c6h6::batch_tables(hs, prec, r); }
-int shape_batch_width_c6h6() { return Ops_c6h6::WPB; }
+int shape_batch_width_c6h6() { return Ops_c6h6::BTW; }
 }  // namespace qmc

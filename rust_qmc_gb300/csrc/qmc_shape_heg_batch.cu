@@ -1,4 +1,4 @@
-// qmc_shape_heg_batch.cu -- batched persistent kernels for the heg shape.
+// qmc_shape_heg_batch.cu -- batched kernels for the heg shape.
 #include "qmc_heg_kernels.cuh"
 
 namespace qmc {

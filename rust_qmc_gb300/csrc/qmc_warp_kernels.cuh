@@ -285,12 +285,10 @@ __device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, N
     return du;
 }
 
-// Single-electron sweeps, one warp per walker, WPB walkers per block.
-template <int NE, int NUP, int NNUC, class T, int MOVE>
-__device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict__ gpos, T* __restrict__ gdinv,
-                                                int* __restrict__ gsign, int w, int Wcap, int n_sweeps,
-                                                uint64_t step0, T step, T tau, T maxd, uint64_t seed,
-                                                unsigned long long* acc_out, int* flags, int fixed_node) {
+// Single-electron sweeps, one warp per walker, WPB walkers per block.  A is
+// const SweepArgs<T> or const volatile SweepArgs<T>.
+template <int NE, int NUP, int NNUC, class T, int MOVE, class A>
+__device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
     const int lane = threadIdx.x & 31;
@@ -299,27 +297,27 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
     for (int r = 0; r < 2; ++r) {
         const int j = lane + 32 * r;
         const bool ok = j < NE;
-        P.x[r] = ok ? gpos[(3 * j + 0) * (size_t)Wcap + w] : T(0);
-        P.y[r] = ok ? gpos[(3 * j + 1) * (size_t)Wcap + w] : T(0);
-        P.z[r] = ok ? gpos[(3 * j + 2) * (size_t)Wcap + w] : T(0);
+        P.x[r] = ok ? a.pos[(3 * j + 0) * (size_t)a.Wcap + w] : T(0);
+        P.y[r] = ok ? a.pos[(3 * j + 1) * (size_t)a.Wcap + w] : T(0);
+        P.z[r] = ok ? a.pos[(3 * j + 2) * (size_t)a.Wcap + w] : T(0);
     }
     T D0[NM], D1[NM];
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
-        D0[k] = lane < NUP ? gdinv[((size_t)(0 * NM * NM + k * NM + lane)) * Wcap + w] : T(0);
-        D1[k] = lane < NDN ? gdinv[((size_t)(1 * NM * NM + k * NM + lane)) * Wcap + w] : T(0);
+        D0[k] = lane < NUP ? a.dinv[((size_t)(0 * NM * NM + k * NM + lane)) * a.Wcap + w] : T(0);
+        D1[k] = lane < NDN ? a.dinv[((size_t)(1 * NM * NM + k * NM + lane)) * a.Wcap + w] : T(0);
     }
-    int sgn = gsign[w];
+    int sgn = a.sign[w];
     unsigned acc = 0;
     int flg = 0;
-    for (int it = 0; it < n_sweeps; ++it) {
-        const uint64_t st = step0 + (uint64_t)it;
+    for (int it = 0; it < a.n_sweeps; ++it) {
+        const uint64_t st = a.step0 + (uint64_t)it;
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             T (&D)[NM] = sig == 0 ? D0 : D1;
             const int NS = sig == 0 ? NUP : NDN;
             static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
-            const MoveDraw<T> draws = sector_draws<T>(seed, (uint32_t)w, st, sig * NUP, NS, lane);
+            const MoveDraw<T> draws = sector_draws<T>(a.seed, (uint32_t)w, st, sig * NUP, NS, lane);
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
@@ -341,12 +339,14 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
                     ax = wshfl(ax, q); ay = wshfl(ay, q); az = wshfl(az, q);
                     T g0[3], g1[3];
                     wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
+                    const T tau = a.tau, maxd = a.maxd;
                     dlx = tau * 2 * (ax + g0[0]); dly = tau * 2 * (ay + g0[1]); dlz = tau * 2 * (az + g0[2]);
                     T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
                     if (m > maxd) { T s = maxd / m; dlx *= s; dly *= s; dlz *= s; }
                     T sd2 = fsqrt(2 * tau);
                     nx = rx + dlx + sd2 * md.n0; ny = ry + dly + sd2 * md.n1; nz = rz + dlz + sd2 * md.n2;
                 } else {
+                    const T step = a.step;
                     nx = rx + step * md.n0; ny = ry + step * md.n1; nz = rz + step * md.n2;
                 }
                 AOLane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0> ao;
@@ -367,6 +367,7 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
                                                                                g0, gn);
                 if (MOVE == MOVE_ONE_DRIFT) {
                     bx = wshfl(bx, q); by = wshfl(by, q); bz = wshfl(bz, q);
+                    const T tau = a.tau, maxd = a.maxd;
                     T iR = R != T(0) ? T(1) / R : T(0);
                     T cx = tau * 2 * (bx * iR + gn[0]), cy = tau * 2 * (by * iR + gn[1]), cz = tau * 2 * (bz * iR + gn[2]);
                     T m = fsqrt(cx * cx + cy * cy + cz * cz);
@@ -380,7 +381,7 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
                 T prob = ratio * ratio;
                 if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);
                 if (prob != prob) flg |= FLAG_NONFINITE;
-                if (md.uacc < prob && R != T(0) && !(fixed_node && R < T(0))) {
+                if (md.uacc < prob && R != T(0) && !(a.fixed_node && R < T(0))) {
                     // positions: the owner lane of e stores the new coordinates
                     if ((e & 31) == lane) {
                         if (e < 32) { P.x[0] = nx; P.y[0] = ny; P.z[0] = nz; }
@@ -403,20 +404,20 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, T* __restrict_
     for (int r = 0; r < 2; ++r) {
         const int j = lane + 32 * r;
         if (j < NE) {
-            gpos[(3 * j + 0) * (size_t)Wcap + w] = P.x[r];
-            gpos[(3 * j + 1) * (size_t)Wcap + w] = P.y[r];
-            gpos[(3 * j + 2) * (size_t)Wcap + w] = P.z[r];
+            a.pos[(3 * j + 0) * (size_t)a.Wcap + w] = P.x[r];
+            a.pos[(3 * j + 1) * (size_t)a.Wcap + w] = P.y[r];
+            a.pos[(3 * j + 2) * (size_t)a.Wcap + w] = P.z[r];
         }
     }
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
-        if (lane < NUP) gdinv[((size_t)(0 * NM * NM + k * NM + lane)) * Wcap + w] = D0[k];
-        if (lane < NDN) gdinv[((size_t)(1 * NM * NM + k * NM + lane)) * Wcap + w] = D1[k];
+        if (lane < NUP) a.dinv[((size_t)(0 * NM * NM + k * NM + lane)) * a.Wcap + w] = D0[k];
+        if (lane < NDN) a.dinv[((size_t)(1 * NM * NM + k * NM + lane)) * a.Wcap + w] = D1[k];
     }
     if (lane == 0) {
-        gsign[w] = sgn;
-        if (acc) atomicAdd(acc_out, (unsigned long long)acc);
-        if (flg) atomicOr(flags, flg);
+        a.sign[w] = sgn;
+        if (acc) atomicAdd(a.acc, (unsigned long long)acc);
+        if (flg) atomicOr(a.flags, flg);
     }
 }
 
@@ -427,37 +428,37 @@ __global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__
                                                      uint64_t seed, unsigned long long* acc_out, int* flags,
                                                      int fixed_node) {
     __shared__ SysW<T> S;
-    load_sysw(&S, Sg);
+    __shared__ SweepArgs<T> args;
+    if (threadIdx.x == 0)
+        args = SweepArgs<T>{gpos, gdinv, gsign, acc_out, flags, step0, seed, step, tau, maxd, W, Wcap, n_sweeps,
+                            fixed_node};
+    load_sysw(&S, Sg);                         // ends with a block barrier
     const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
     if (w >= W) return;                        // whole warps only; no block barrier below
-    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, gpos, gdinv, gsign, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
-                                            acc_out, flags, fixed_node);
+    const volatile SweepArgs<T>& a = args;
+    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w);
 }
 
-// Batched form: persistent blocks over (system, WPB-walker tile) pairs.
-template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+// Batched form: TW / WPB blocks per (system, TW-walker tile), each sweeping
+// WPB walkers of it.  The hardware block scheduler balances uneven systems
+// and classes that run side by side, and the kernel carries no tile-loop
+// state into the walker's registers.
+template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB, int TW>
+__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 4) / WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                       const BatchRec* __restrict__ recs,
                                                       const BatchCtl* __restrict__ ctl) {
+    static_assert(TW % WPB == 0, "a tile splits into whole blocks");
+    constexpr int BPT = TW / WPB;
     __shared__ SysW<T> S;
-    const BatchCtl c = *ctl;
-    int t0, t1;
-    batch_tile_range(ntiles, t0, t1);
-    int cur = -1;
-    for (int ti = t0; ti < t1; ++ti) {
-        const BatchTile tl = tiles[ti];
-        if (tl.rec != cur) {
-            __syncthreads();
-            load_sysw(&S, static_cast<const SysW<T>*>(recs[tl.rec].tab_s));
-            cur = tl.rec;
-        }
-        const BatchRec& R = recs[tl.rec];
-        const int w = tl.w0 + (int)(threadIdx.x >> 5);
-        if (w < R.W)
-            kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, (T*)R.pos, (T*)R.dinv, R.sign, w, R.Wcap, c.n_sweeps, c.step,
-                                                    (T)c.step_size, (T)c.tau, (T)c.max_drift,
-                                                    batch_system_seed(c.seed, R.index), R.acc, R.flags, R.fixed_node);
-    }
+    __shared__ SweepArgs<T> args;
+    if ((int)blockIdx.x >= ntiles * BPT) return;
+    const BatchTile tl = tiles[blockIdx.x / BPT];
+    if (threadIdx.x == 0) args = sweep_args<T>(recs[tl.rec], *ctl);
+    load_sysw(&S, static_cast<const SysW<T>*>(recs[tl.rec].tab_s));   // ends with a block barrier
+    const volatile SweepArgs<T>& a = args;
+    const int w = tl.w0 + (int)(blockIdx.x % BPT) * WPB + (int)(threadIdx.x >> 5);
+    if (w >= a.W) return;                      // whole warps only; no block barrier below
+    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w);
 }
 
 // Full evaluation from positions (refresh + E_L), one warp per walker.
@@ -695,31 +696,24 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
     if (partial) warp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
-// Batched form (compute type TC, state written, per-tile E_L partials).
+// Batched form (compute type TC, state written, per-tile E_L partials), one
+// block of WPB warps per WPB-walker tile.
 template <int NE, int NUP, int NNUC, class TC, class TS, int WPB>
 __global__ void __launch_bounds__(32 * WPB) kwb_measure(const BatchTile* __restrict__ tiles, int ntiles,
                                                         const BatchRec* __restrict__ recs, double* tile_partial) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     __shared__ SysW<TC> S;
     extern __shared__ __align__(16) unsigned char wsm[];
+    if ((int)blockIdx.x >= ntiles) return;
     const int wib = threadIdx.x >> 5;
     TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * 32;
-    int t0, t1;
-    batch_tile_range(ntiles, t0, t1);
-    int cur = -1;
-    for (int ti = t0; ti < t1; ++ti) {
-        const BatchTile tl = tiles[ti];
-        if (tl.rec != cur) {
-            load_sysw(&S, static_cast<const SysW<TC>*>(recs[tl.rec].tab_d));
-            cur = tl.rec;
-        }
-        const BatchRec& R = recs[tl.rec];
-        const int w = tl.w0 + wib;
-        double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, (const TS*)R.pos, (TS*)R.dinv, R.logabs,
-                                                                  R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr,
-                                                                  nullptr, R.flags);
-        warp_block_partial<WPB>(e_l, tile_partial, ti);
-    }
+    const BatchTile tl = tiles[blockIdx.x];
+    const BatchRec& R = recs[tl.rec];
+    load_sysw(&S, static_cast<const SysW<TC>*>(R.tab_d));
+    const int w = tl.w0 + wib;
+    double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign,
+                                                          R.el, w, w < R.W, R.Wcap, 1, nullptr, nullptr, R.flags);
+    warp_block_partial<WPB>(e_l, tile_partial, blockIdx.x);
 }
 
 int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
@@ -729,6 +723,10 @@ template <int NE, int NUP, int NNUC>
 struct WarpShapeOps {
     static constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
     static constexpr int WPB = 4;
+    // Batch tiles hold BTW walkers: BTW / WPB sweep blocks each, and one
+    // refresh block of BTW warps (the wider refresh block shares the large
+    // shared-memory table among more warps).
+    static constexpr int BTW = 8;
 
     template <class T>
     static int table(const HostSys& hs, const SysW<T>** out) {
@@ -873,11 +871,10 @@ struct WarpShapeOps {
 
     template <class T, int MOVE>
     static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
-        auto kern = kwb_sweep<NE, NUP, NNUC, T, MOVE, WPB>;
+        auto kern = kwb_sweep<NE, NUP, NNUC, T, MOVE, WPB, BTW>;
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, 0) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
-        kern<<<grid, 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        kern<<<bc.ntiles * (BTW / WPB), 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
@@ -894,15 +891,17 @@ struct WarpShapeOps {
 
     template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = sizeof(TC) * WPB * NM * 32;
-        auto kern = kwb_measure<NE, NUP, NNUC, TC, TS, WPB>;
+        const size_t smem = sizeof(TC) * BTW * NM * 32;
+        auto kern = kwb_measure<NE, NUP, NNUC, TC, TS, BTW>;
         static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); attr = true; }
-        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * BTW, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        const int grid =
-            bc.grid_measure > 0 ? (bc.grid_measure < bc.ntiles ? bc.grid_measure : bc.ntiles) : bc.ntiles;
-        kern<<<grid, 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
+        kern<<<bc.ntiles, 32 * BTW, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, bc.tile_partial);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }

@@ -511,6 +511,29 @@ struct SweepArgs {
     int W, Wcap, n_sweeps, fixed_node;
 };
 
+// A warp-per-walker refresh's arrays, block-shared for the same reason as
+// SweepArgs (the kernels write the walker state at the end of a long walk).
+template <class TS>
+struct MeasureArgs {
+    const TS* pos;
+    TS* dinv;
+    double* log;
+    int* sign;
+    double* el;
+    double* grad;                  // optional per-electron outputs (null: not written)
+    double* lap;
+    int* flags;
+    float2* rows;                  // two-launch refresh scratch (electron gas)
+    const void* kt;                // reciprocal-space table (electron gas)
+    int W, Wcap, write_state;
+};
+
+template <class TS>
+__device__ __forceinline__ MeasureArgs<TS> measure_args(const BatchRec& R) {
+    return MeasureArgs<TS>{(const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, nullptr, nullptr, R.flags,
+                           R.rows, R.ktab, R.W, R.Wcap, 1};
+}
+
 template <class T>
 __device__ __forceinline__ SweepArgs<T> sweep_args(const BatchRec& R, const BatchCtl& c) {
     return SweepArgs<T>{(T*)R.pos, (T*)R.dinv, R.sign, R.acc, R.flags, c.step, batch_system_seed(c.seed, R.index),

@@ -581,14 +581,8 @@ __global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw
 // grad ln D and lap D / D per electron into drows), and PART 2, the energy
 // half (Jastrow, Ewald sums, E_L), which reads them back.  Each launch
 // carries half the code and PART 2 none of the inversion's registers.
-template <int NE, int NUP, class TC, class TS, int PART = 0>
-__device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KTable* __restrict__ KT, TC* Mr,
-                                                     const TS* __restrict__ gpos, TS* __restrict__ gdinv,
-                                                     double* __restrict__ glog, int* __restrict__ gsign,
-                                                     double* __restrict__ gel, int w, bool act, int Wcap,
-                                                     int write_state, double* __restrict__ out_grad,
-                                                     double* __restrict__ out_lap, int* flags,
-                                                     float2* __restrict__ drows = nullptr) {
+template <int NE, int NUP, class TC, class TS, int PART, class A>
+__device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, A& a, TC* Mr, int w, bool act) {
     static_assert(PART == 0 || std::is_same<TC, ff>::value, "the two-part refresh is float-float only");
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
@@ -601,9 +595,9 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
         for (int r = 0; r < 2; ++r) {
             const int j = lane + 32 * r;
             const bool ok = j < NE;
-            P.x[r] = ok ? (TC)gpos[(3 * j + 0) * (size_t)Wcap + w] : TC(0);
-            P.y[r] = ok ? (TC)gpos[(3 * j + 1) * (size_t)Wcap + w] : TC(0);
-            P.z[r] = ok ? (TC)gpos[(3 * j + 2) * (size_t)Wcap + w] : TC(0);
+            P.x[r] = ok ? (TC)a.pos[(3 * j + 0) * (size_t)a.Wcap + w] : TC(0);
+            P.y[r] = ok ? (TC)a.pos[(3 * j + 1) * (size_t)a.Wcap + w] : TC(0);
+            P.z[r] = ok ? (TC)a.pos[(3 * j + 2) * (size_t)a.Wcap + w] : TC(0);
         }
         double logdet = 0.0;
         ff pmag = ff(1.0f);                       // float-float form: |det|^2 = pmag 2^pexp
@@ -693,13 +687,13 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             }
             TC (&Ir)[NM] = Ar;
             TC (&Ii)[NM] = Ai;
-            if (write_state && lane < NS) {
+            if (a.write_state && lane < NS) {
 #pragma unroll
                 for (int k = 0; k < NM; ++k) {
                     if (k >= NS) break;
-                    size_t b = ((size_t)(sig * NM * NM + k * NM + lane)) * 2 * Wcap;
-                    gdinv[b + w] = (TS)Ir[k];
-                    gdinv[b + Wcap + w] = (TS)Ii[k];
+                    size_t b = ((size_t)(sig * NM * NM + k * NM + lane)) * 2 * a.Wcap;
+                    a.dinv[b + w] = (TS)Ir[k];
+                    a.dinv[b + a.Wcap + w] = (TS)Ii[k];
                 }
             }
             // lane = electron row q: grad ln D = sum_j Dinv[j][q] i k_j phi_j(r_q); lap D / D = -sum_j Dinv phi k^2
@@ -732,12 +726,12 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     const int i = sig * NUP + lane;
                     const TC v[7] = {gdx[sig], gdy[sig], gdz[sig], gqx[sig], gqy[sig], gqz[sig], ldet[sig]};
 #pragma unroll
-                    for (int c = 0; c < 7; ++c) ff_store(drows + (size_t)(c * NE + i) * Wcap + w, v[c]);
+                    for (int c = 0; c < 7; ++c) ff_store(a.rows + (size_t)(c * NE + i) * a.Wcap + w, v[c]);
                 }
             }
             if (lane == 0) {
-                if (!ok) atomicOr(flags, FLAG_SINGULAR);
-                glog[w] = logdet;
+                if (!ok) atomicOr(a.flags, FLAG_SINGULAR);
+                a.log[w] = logdet;
             }
             return 0.0;
         }
@@ -749,12 +743,12 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                     const int i = sig * NUP + lane;
                     TC v[7];
 #pragma unroll
-                    for (int c = 0; c < 7; ++c) v[c] = ff_load(drows + (size_t)(c * NE + i) * Wcap + w);
+                    for (int c = 0; c < 7; ++c) v[c] = ff_load(a.rows + (size_t)(c * NE + i) * a.Wcap + w);
                     gdx[sig] = v[0]; gdy[sig] = v[1]; gdz[sig] = v[2];
                     gqx[sig] = v[3]; gqy[sig] = v[4]; gqz[sig] = v[5]; ldet[sig] = v[6];
                 }
             }
-            logdet = glog[w];
+            logdet = a.log[w];
         }
         // Jastrow for this lane's electrons (pairs from both ends)
         TC u = 0, kin = 0;
@@ -787,12 +781,12 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                    cz = S.quirk_cross ? gqz[sig] : gdz[sig];
                 TC lp = ldet[sig] + lu + gx * gx + gy * gy + gz * gz + 2 * (cx * gx + cy * gy + cz * gz);
                 kin += lp;
-                if (out_grad) {
-                    out_grad[((size_t)w * NE + i) * 3 + 0] = (double)(gdx[sig] + gx);
-                    out_grad[((size_t)w * NE + i) * 3 + 1] = (double)(gdy[sig] + gy);
-                    out_grad[((size_t)w * NE + i) * 3 + 2] = (double)(gdz[sig] + gz);
+                if (a.grad) {
+                    a.grad[((size_t)w * NE + i) * 3 + 0] = (double)(gdx[sig] + gx);
+                    a.grad[((size_t)w * NE + i) * 3 + 1] = (double)(gdy[sig] + gy);
+                    a.grad[((size_t)w * NE + i) * 3 + 2] = (double)(gdz[sig] + gz);
                 }
-                if (out_lap) out_lap[(size_t)w * NE + i] = (double)lp;
+                if (a.lap) a.lap[(size_t)w * NE + i] = (double)lp;
             }
         }
         // Real-space Ewald, each unordered pair once, spread evenly over the
@@ -953,7 +947,7 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
                             }
                             const bool okv = vi == 0 ? ok4[0] : (vi == 1 ? ok4[1] : (vi == 2 ? ok4[2] : ok4[3]));
                             const int tv = vi == 0 ? tk[0] : (vi == 1 ? tk[1] : (vi == 2 ? tk[2] : tk[3]));
-                            if ((lane & 7) == 0 && okv) vkt += kweight<TC>(KT, tv) * (vr * vr + vim * vim);
+                            if ((lane & 7) == 0 && okv) vkt += kweight<TC>(static_cast<const KTable*>(a.kt), tv) * (vr * vr + vim * vim);
                         }
                     }
 #pragma unroll
@@ -981,8 +975,8 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, const KT
             int fl = 0;
             if (!ok) fl |= FLAG_SINGULAR;
             if (!isfinite(e_l)) fl |= FLAG_NONFINITE;
-            if (fl) atomicOr(flags, fl);
-            if (write_state) { glog[w] = logdet + (double)u; gsign[w] = 1; gel[w] = e_l; }
+            if (fl) atomicOr(a.flags, fl);
+            if (a.write_state) { a.log[w] = logdet + (double)u; a.sign[w] = 1; a.el[w] = e_l; }
         }
     }
     return act ? e_l : 0.0;
@@ -1016,14 +1010,18 @@ __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khw_measure(
     int Wcap, int write_state, double* __restrict__ out_grad, double* __restrict__ out_lap, double* partial,
     int* flags, float2* __restrict__ drows) {
     extern __shared__ __align__(16) unsigned char hsm[];
+    __shared__ MeasureArgs<TS> args;
     SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
     TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
-    load_sysh(&S, Sg, (int)sizeof(SysH<TC>));
+    if (threadIdx.x == 0)
+        args = MeasureArgs<TS>{gpos, gdinv, glog, gsign, gel, out_grad, out_lap, flags, drows, KT, W, Wcap,
+                               write_state};
+    load_sysh(&S, Sg, (int)sizeof(SysH<TC>));   // ends with a block barrier
+    const volatile MeasureArgs<TS>& a = args;
     const int wib = threadIdx.x >> 5;
     const int w = blockIdx.x * WPB + wib;
     double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
-        S, KT, rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(), gpos, gdinv, glog, gsign, gel, w, w < W,
-        Wcap, write_state, out_grad, out_lap, flags, drows);
+        S, a, rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(), w, w < W);
     if (PART != 1 && partial) hwarp_block_partial<WPB>(e_l, partial, blockIdx.x);
 }
 
@@ -1034,18 +1032,18 @@ __global__ void __launch_bounds__(32 * WPB, PART == 2 ? 4 : 2) khwb_measure(cons
                                                                          int ntiles, const BatchRec* __restrict__ recs,
                                                                          double* tile_partial) {
     extern __shared__ __align__(16) unsigned char hsm[];
+    __shared__ MeasureArgs<TS> args;
     SysH<TC>& S = *reinterpret_cast<SysH<TC>*>(hsm);
     TC* rows = reinterpret_cast<TC*>(hsm + ((sizeof(SysH<TC>) + 15) / 16) * 16);
     if ((int)blockIdx.x >= ntiles) return;
     const int wib = threadIdx.x >> 5;
     const BatchTile tl = tiles[blockIdx.x];
-    const BatchRec& R = recs[tl.rec];
-    load_sysh(&S, static_cast<const SysH<TC>*>(R.tab_d), (int)sizeof(SysH<TC>));
+    if (threadIdx.x == 0) args = measure_args<TS>(recs[tl.rec]);
+    load_sysh(&S, static_cast<const SysH<TC>*>(recs[tl.rec].tab_d), (int)sizeof(SysH<TC>));   // ends with a barrier
+    const volatile MeasureArgs<TS>& a = args;
     const int w = tl.w0 + wib;
     double e_l = khw_measure_walker<NE, NUP, TC, TS, PART>(
-        S, static_cast<const KTable*>(R.ktab), rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(),
-        (const TS*)R.pos, (TS*)R.dinv, R.logabs, R.sign, R.el, w, w < R.W, R.Wcap, 1, nullptr, nullptr, R.flags,
-        R.rows);
+        S, a, rows + (size_t)wib * hmeasure_warp_words<NE, NUP, PART>(), w, w < a.W);
     if (PART != 1) hwarp_block_partial<WPB>(e_l, tile_partial, blockIdx.x);
 }
 

@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__
 // and classes that run side by side, and the kernel carries no tile-loop
 // state into the walker's registers.
 template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB, int TW>
-__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 4) / WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+__global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                       const BatchRec* __restrict__ recs,
                                                       const BatchCtl* __restrict__ ctl) {
     static_assert(TW % WPB == 0, "a tile splits into whole blocks");

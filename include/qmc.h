@@ -323,9 +323,10 @@ int qmc_roofline_model(const qmc_system_desc* desc, int precision, double accept
 /* ---- uneven batches (no reference counterpart: rust_qmc runs one system
  * per process, src/main.rs) ---------------------------------------------------
  * A batch binds walker sets of one context -- any mix of systems, shapes,
- * precisions and sizes -- and advances them together: one persistent launch
- * per (shape, precision) class over (system, walker tile) pairs, the class
- * launches running concurrently inside one CUDA graph per step.
+ * precisions and sizes -- and advances them together: one sweep launch and
+ * one refresh (one or two launches) per (shape, precision) class over
+ * (system, walker tile) pairs, the class launches running concurrently inside
+ * one CUDA graph per step.
  * Walker set i of a batch driven with `seed` draws from the Philox key
  * qmc_batch_system_seed(seed, i) (SplitMix64 of seed + (i+1) * 0x9E3779B97F4A7C15),
  * so a batched sweep of set i equals qmc_walkers_sweep of that set with that

@@ -327,8 +327,8 @@ class Walkers:
 
 
 class Batch:
-    """Walker sets of one context advanced together (qmc_batch_*): one
-    persistent launch per shape class, one CUDA graph per step."""
+    """Walker sets of one context advanced together (qmc_batch_*): one sweep
+    and one refresh per shape class, one CUDA graph per step."""
 
     def __init__(self, ctx, walkers):
         self.ctx, self.lib, self.walkers = ctx, ctx.lib, list(walkers)

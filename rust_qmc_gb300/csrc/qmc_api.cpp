@@ -1253,9 +1253,11 @@ int qmc_host_free(void* p) {
 
 // ---------------------------------------------------------------------------
 // Uneven batches: many systems advanced together.  Walker sets are grouped
-// into classes by (shape, precision); each class is one persistent launch over
-// its (system, walker tile) list.  A step (sweeps + FP64 refresh + per-system
-// mean E_L + step-counter advance) is captured once into a CUDA graph whose
+// into classes by (shape, precision); each class launches its sweep and its
+// refresh over its (system, walker tile) list: sweeps one block per tile,
+// the thread-per-walker refresh as a persistent grid over the tiles.  A step
+// (sweeps + FP64 refresh + per-system mean E_L + step-counter advance) is
+// captured once into a CUDA graph whose
 // class branches run concurrently; the per-call scalars live in a device
 // control block, so the same graph replays for every step and every call.
 // ---------------------------------------------------------------------------
@@ -1268,7 +1270,6 @@ struct qmc_batch_s {
         BatchRec* d_recs = nullptr;
         int* d_tile_begin = nullptr;
         double* d_partial = nullptr;
-        int grid_sweep[2] = {0, 0};        // per single-electron move kind
         int grid_measure = 0;
         cudaStream_t stream = nullptr;
         cudaEvent_t done = nullptr;
@@ -1396,12 +1397,14 @@ int batch_build(qmc_ctx_s* ctx, const std::vector<qmc_walkers_s*>& wk, bool owns
         c.bc.recs = c.d_recs;
         c.bc.tile_begin = c.d_tile_begin;
         c.bc.tile_partial = c.d_partial;
-        // persistent grids: every resident block slot of the GPU (occupancy x SMs)
+        // sweeps run one block per tile; the occupancy queries set the kernels'
+        // shared-memory attributes before any stream capture
         for (int m = 0; m < 2; ++m) {
             int occ = batch_occupancy(c.bc.shape, c.bc.prec, QMC_MOVE_ONE_GAUSS + m, false);
             if (occ < 0) return -occ;
-            c.grid_sweep[m] = std::max(1, occ) * nsm;
         }
+        // persistent refresh grids of the thread-per-walker shapes: every
+        // resident block slot of the GPU (occupancy x SMs)
         int occ = batch_occupancy(c.bc.shape, c.bc.prec, 0, true);
         if (occ < 0) return -occ;
         c.grid_measure = std::max(1, occ) * nsm;
@@ -1437,7 +1440,6 @@ int batch_upload_ctl(qmc_batch_s* b, const BatchCtl& h) {
 // One step on the context stream, class after class (eager form).
 int batch_sweep_eager(qmc_batch_s* b, int mk) {
     for (auto& c : b->cls) {
-        c.bc.grid_sweep = c.grid_sweep[mk - QMC_MOVE_ONE_GAUSS];
         CK(launch_batch_sweep(c.bc, mk, b->d_ctl, b->ctx->stream));
     }
     return QMC_OK;
@@ -1460,7 +1462,6 @@ int batch_capture(qmc_batch_s* b, int mk, cudaGraphExec_t* out) {
     for (auto& c : b->cls) {
         if (rc) break;
         rc = cuda_rc(cudaStreamWaitEvent(c.stream, b->fork, 0));
-        c.bc.grid_sweep = c.grid_sweep[mk - QMC_MOVE_ONE_GAUSS];
         if (!rc) rc = launch_batch_sweep(c.bc, mk, b->d_ctl, c.stream);
         if (!rc) rc = launch_batch_measure(c.bc, c.stream);
         if (!rc) rc = launch_batch_energy(c.bc, b->d_ctl, b->d_series, (int)b->wk.size(), c.stream);

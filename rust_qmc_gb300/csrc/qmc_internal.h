@@ -136,8 +136,8 @@ int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, i
                   double tau, uint64_t seed, uint64_t step, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
-// Uneven batches: many systems, each with its own walker set, advanced by one
-// persistent launch per shape class over a list of (system, walker tile).
+// Uneven batches: many systems, each with its own walker set, advanced by a
+// few launches per shape class over a list of (system, walker tile).
 // ---------------------------------------------------------------------------
 #if defined(__CUDACC__)
 #define QMC_HD __host__ __device__
@@ -200,12 +200,13 @@ struct BatchClass {
     int nrec = 0;
     const int* tile_begin = nullptr;     // device [nrec + 1]
     double* tile_partial = nullptr;      // device [ntiles][2]
-    int grid_sweep = 0, grid_measure = 0;   // persistent grid sizes (0: one block per tile)
+    int grid_measure = 0;                // persistent refresh grid of the thread-per-walker shapes
+                                         // (0: one block per tile); other launches: one block per tile
 };
 
 // Walkers per tile for a shape (threads per walker block or walkers per warp block).
 int batch_tile_width(int shape);
-// Persistent launches for one class; `ctl` is device-resident.
+// The launches of one class; `ctl` is device-resident.
 int launch_batch_sweep(const BatchClass& bc, int move_kind, const BatchCtl* ctl, cudaStream_t st);
 int launch_batch_measure(const BatchClass& bc, cudaStream_t st);
 // Resident blocks per SM of the class's batch kernels (occupancy query).

@@ -1,4 +1,4 @@
-// qmc_shape_ch4_batch.cu -- batched persistent kernels for the ShapeCH4 system shape.
+// qmc_shape_ch4_batch.cu -- batched kernels for the ShapeCH4 system shape.
 #include "qmc_walker_kernels.cuh"
 
 namespace qmc {

@@ -1,4 +1,4 @@
-// qmc_shape_ch4min_batch.cu -- batched persistent kernels for the ShapeCH4Min system shape.
+// qmc_shape_ch4min_batch.cu -- batched kernels for the ShapeCH4Min system shape.
 #include "qmc_walker_kernels.cuh"
 
 namespace qmc {

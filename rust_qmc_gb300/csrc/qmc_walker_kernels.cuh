@@ -1130,20 +1130,19 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
 
 // n_sweeps single-electron sweeps of walker w, staged through the calling
 // thread's shared-memory columns sp / sd.
-template <class SH, class T, int MOVE, int TPB>
-__device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, T* __restrict__ gpos,
-                                             T* __restrict__ gdinv, int* __restrict__ gsign, int w, int Wcap,
-                                             int n_sweeps, uint64_t step0, T step, T tau, T maxd, uint64_t seed,
-                                             unsigned long long* acc_out, int* flags, int fixed_node) {
+// a: the walker arrays, c: the sweep controls; both the same const SweepArgs<T>
+// of kernel parameters, or the same block-shared const volatile one.
+template <class SH, class T, int MOVE, int TPB, class A, class C>
+__device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, A& a, C& c, int w) {
     constexpr int NM = SH::NMAX;
     const int t = threadIdx.x;
     const PosCols<T, TPB, SH::NE> P(sp, t);
 #pragma unroll
     for (int e = 0; e < SH::NE; ++e)
-        P.set(e, gpos[(size_t)(3 * e) * Wcap + w], gpos[(size_t)(3 * e + 1) * Wcap + w],
-              gpos[(size_t)(3 * e + 2) * Wcap + w]);
+        P.set(e, a.pos[(size_t)(3 * e) * a.Wcap + w], a.pos[(size_t)(3 * e + 1) * a.Wcap + w],
+              a.pos[(size_t)(3 * e + 2) * a.Wcap + w]);
 #pragma unroll
-    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = gdinv[(size_t)i * Wcap + w];
+    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = a.dinv[(size_t)i * a.Wcap + w];
     T* pc = sd + 2 * NM * NM * TPB + t;
     // one-body terms of the electrons (thread-local; the pair cache fills the
     // shared-memory budget of a walker)
@@ -1156,25 +1155,25 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
                 u1c[e] = one_body_u(S, P(e, 0), P(e, 1), P(e, 2));
         }
     }
-    int sgn = gsign[w];
+    int sgn = a.sign[w];
     unsigned acc = 0;
     int flg = 0;
-    for (int it = 0; it < n_sweeps; ++it) {
-        uint64_t st = step0 + (uint64_t)it;
-        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node,
-                                          sgn, acc, flg);
-        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, seed, step, tau, maxd, fixed_node,
-                                          sgn, acc, flg);
+    for (int it = 0; it < c.n_sweeps; ++it) {
+        uint64_t st = c.step0 + (uint64_t)it;
+        sweep_sector<SH, T, 0, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, c.seed, c.step, c.tau, c.maxd,
+                                          c.fixed_node, sgn, acc, flg);
+        sweep_sector<SH, T, 1, MOVE, TPB>(S, sp, sd, pc, u1c, t, (uint32_t)w, st, c.seed, c.step, c.tau, c.maxd,
+                                          c.fixed_node, sgn, acc, flg);
     }
 #pragma unroll
     for (int e = 0; e < SH::NE; ++e)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) gpos[(size_t)(3 * e + c) * Wcap + w] = P(e, c);
+        for (int c = 0; c < 3; ++c) a.pos[(size_t)(3 * e + c) * a.Wcap + w] = P(e, c);
 #pragma unroll
-    for (int i = 0; i < 2 * NM * NM; ++i) gdinv[(size_t)i * Wcap + w] = sd[i * TPB + t];
-    gsign[w] = sgn;
-    if (acc) atomicAdd(acc_out, (unsigned long long)acc);
-    if (flg) atomicOr(flags, flg);
+    for (int i = 0; i < 2 * NM * NM; ++i) a.dinv[(size_t)i * a.Wcap + w] = sd[i * TPB + t];
+    a.sign[w] = sgn;
+    if (acc) atomicAdd(a.acc, (unsigned long long)acc);
+    if (flg) atomicOr(a.flags, flg);
 }
 
 // Occupancy target: all walkers of the 65 536-walker workload resident in
@@ -1190,40 +1189,32 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
     T* sd = sp + 3 * SH::NE * TPB;
     const int w = blockIdx.x * TPB + threadIdx.x;
     if (w >= W) return;
-    sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, gpos, gdinv, gsign, w, Wcap, n_sweeps, step0, step, tau, maxd, seed,
-                                   acc_out, flags, fixed_node);
+    // kernel parameters: the measured-fastest form of this kernel (block-shared
+    // volatile arguments use fewer registers here but issue slower)
+    const SweepArgs<T> a{gpos, gdinv, gsign, acc_out, flags, step0, seed, step, tau, maxd, W, Wcap, n_sweeps,
+                         fixed_node};
+    sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w);
 }
 
-// Batched form: persistent blocks over (system, TPB-walker tile) pairs; the
-// system table is staged into shared memory ahead of the walker columns.
-
+// Batched form: one block per (system, TPB-walker tile); the system table is
+// staged into shared memory ahead of the walker columns.
 template <class SH, class T, int MOVE, int TPB>
 __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) kb_sweep_one(
     const BatchTile* __restrict__ tiles, int ntiles, const BatchRec* __restrict__ recs,
     const BatchCtl* __restrict__ ctl) {
     extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ SweepArgs<T> args;
     SysT<SH, T>& S = *reinterpret_cast<SysT<SH, T>*>(smraw);
     T* sp = reinterpret_cast<T*>(smraw + batch_table_bytes<SH, T>());
     T* sd = sp + 3 * SH::NE * TPB;
-    const BatchCtl c = *ctl;
-    int t0, t1;
-    batch_tile_range(ntiles, t0, t1);
-    int cur = -1;
-    for (int ti = t0; ti < t1; ++ti) {
-        const BatchTile tl = tiles[ti];
-        if (tl.rec != cur) {
-            __syncthreads();
-            stage_table(&S, recs[tl.rec].tab_s);
-            __syncthreads();
-            cur = tl.rec;
-        }
-        const BatchRec& R = recs[tl.rec];
-        const int w = tl.w0 + (int)threadIdx.x;
-        if (w < R.W)
-            sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, (T*)R.pos, (T*)R.dinv, R.sign, w, R.Wcap, c.n_sweeps, c.step,
-                                           (T)c.step_size, (T)c.tau, (T)c.max_drift,
-                                           batch_system_seed(c.seed, R.index), R.acc, R.flags, R.fixed_node);
-    }
+    if ((int)blockIdx.x >= ntiles) return;
+    const BatchTile tl = tiles[blockIdx.x];
+    if (threadIdx.x == 0) args = sweep_args<T>(recs[tl.rec], *ctl);
+    stage_table(&S, recs[tl.rec].tab_s);
+    __syncthreads();
+    const volatile SweepArgs<T>& a = args;
+    const int w = tl.w0 + (int)threadIdx.x;
+    if (w < a.W) sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w);
 }
 
 // Batched refresh + E_L (compute type TC) with one compensated partial per tile.
@@ -1496,8 +1487,7 @@ struct ShapeOps {
         }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, BTPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        const int grid = bc.grid_sweep > 0 ? (bc.grid_sweep < bc.ntiles ? bc.grid_sweep : bc.ntiles) : bc.ntiles;
-        kern<<<grid, BTPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        kern<<<bc.ntiles, BTPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
         ++g_launch_count;
         return cuda_status(cudaGetLastError());
     }

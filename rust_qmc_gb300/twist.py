@@ -4,7 +4,7 @@ examples/heg_vmc.rs:114-187 over HomogeneousElectronGas::new_with_twist_and_form
 
 Every Monkhorst-Pack twist is its own system (its orbital wave vectors shifted
 by theta 2 pi / L); all of them run as one uneven batch (qmc_batch_run: one
-persistent launch per step over every twist's walker tiles), so a 3x3x3 grid
+sweep and one refresh per step over every twist's walker tiles), so a 3x3x3 grid
 costs one set of launches, not 27 runs.  The reference runs each twist with
 its all-electron MCMCSimulation; the electron gas kernels here move one
 electron at a time, with Gaussian proposals of width ``step``.

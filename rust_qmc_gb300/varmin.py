@@ -9,7 +9,7 @@ each record every walker's E_L; population variance), keeps the first point
 of least variance and samples it once more.
 
 Here the points of a phase are the walker sets of one batch (qmc_batch_*):
-one persistent launch per step advances all of them, the FP64 refresh that
+one sweep and one refresh per step advance all of them, the FP64 refresh that
 ends each step gives every walker's E_L, and each point's mean, variance and
 error over its recorded samples are reduced on the host.  The batch moves
 electrons one at a time (Gaussian proposals of width ``step``) where the

@@ -247,6 +247,11 @@ __device__ __forceinline__ T min_img(T d, const SysH<T>& S) { return d - S.L * r
 __device__ __forceinline__ float hshfl(float v, int s) { return __shfl_sync(0xffffffffu, v, s); }
 __device__ __forceinline__ double hshfl(double v, int s) { return __shfl_sync(0xffffffffu, v, s); }
 __device__ __forceinline__ ff hshfl(ff v, int s) { return wshfl(v, s); }
+
+// |z|^2 of a pivot candidate on the leading parts (pivot choice only).
+__device__ __forceinline__ float pivot_mag(float r, float i) { return r * r + i * i; }
+__device__ __forceinline__ float pivot_mag(double r, double i) { return (float)(r * r + i * i); }
+__device__ __forceinline__ float pivot_mag(ff r, ff i) { return r.hi * r.hi + i.hi * i.hi; }
 __device__ __forceinline__ float hshfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
 __device__ __forceinline__ double hshfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
 __device__ __forceinline__ ff hshfl_xor(ff v, int m) { return shfl_xor(v, m); }
@@ -627,6 +632,13 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, A& a, TC
             // t = 1 + 1/a.  The row interchanges are undone at the end as column
             // interchanges in reverse order: lane j gathers column src(j),
             // src = tau_{n-1}( ... tau_0(j)), tau_k the swap of k and p_k.
+            // The pivot loop is rolled (one copy of the step's code, which an
+            // unrolled loop would repeat NS times): the registers hold the rows
+            // rotated so that row k sits in register 0 at step k -- the rows not
+            // yet pivoted in registers 0..NS-1-k, in the unrolled form's order,
+            // the pivoted ones after them -- and each step ends by moving
+            // register 0 to the back.  After NS steps the order is row k in
+            // register k again.
             TC Ar[NM], Ai[NM];
 #pragma unroll
             for (int i = 0; i < NM; ++i) {
@@ -635,25 +647,27 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, A& a, TC
                 Ai[i] = in ? Mi[i * 32 + lane] : TC(0);
             }
             int src = lane;
-            static_for<NM>([&](auto kc) {
-                constexpr int k = decltype(kc)::value;
-                if (k >= NS) return;
-                int p = k;
-                TC best = Ar[k] * Ar[k] + Ai[k] * Ai[k];
+#pragma unroll 1
+            for (int k = 0; k < NS; ++k) {
+                // pivot: the largest |D[i][k]| over the rows not yet pivoted
+                // (leading parts; the first of equal ones)
+                int p = 0;
+                float best = pivot_mag(Ar[0], Ai[0]);
 #pragma unroll
-                for (int i = k + 1; i < NM; ++i) {
-                    TC a = Ar[i] * Ar[i] + Ai[i] * Ai[i];
-                    if (i < NS && a > best) { best = a; p = i; }
+                for (int r = 1; r < NM; ++r) {
+                    const float m = pivot_mag(Ar[r], Ai[r]);
+                    if (r < NS - k && m > best) { best = m; p = r; }
                 }
                 p = __shfl_sync(0xffffffffu, p, k);
 #pragma unroll
-                for (int i = k + 1; i < NM; ++i) {
-                    bool sw = (i == p);
-                    TC a = Ar[k], b = Ar[i]; Ar[k] = sw ? b : a; Ar[i] = sw ? a : b;
-                    a = Ai[k]; b = Ai[i]; Ai[k] = sw ? b : a; Ai[i] = sw ? a : b;
+                for (int r = 1; r < NM; ++r) {
+                    const bool sw = (r == p);
+                    TC a = Ar[0], b = Ar[r]; Ar[0] = sw ? b : a; Ar[r] = sw ? a : b;
+                    a = Ai[0]; b = Ai[r]; Ai[0] = sw ? b : a; Ai[r] = sw ? a : b;
                 }
-                src = (src == k) ? p : ((src == p) ? k : src);
-                TC pr = hshfl(Ar[k], k), pi = hshfl(Ai[k], k);
+                const int pk = k + p;
+                src = (src == k) ? pk : ((src == pk) ? k : src);
+                TC pr = hshfl(Ar[0], k), pi = hshfl(Ai[0], k);
                 TC pa = pr * pr + pi * pi;
                 if (!(pa > TC(0))) { ok = false; pr = 1; pi = 0; pa = 1; }
                 if constexpr (std::is_same<TC, ff>::value) {
@@ -666,18 +680,26 @@ __device__ __forceinline__ double khw_measure_walker(const SysH<TC>& S, A& a, TC
                 TC tr, ti;
                 if (lane == k) {
                     tr = TC(1) + ipr; ti = ipi;
-                    Ar[k] = ipr; Ai[k] = ipi;
+                    Ar[0] = ipr; Ai[0] = ipi;
                 } else {
-                    tr = Ar[k] * ipr - Ai[k] * ipi; ti = Ar[k] * ipi + Ai[k] * ipr;
-                    Ar[k] = tr; Ai[k] = ti;
+                    tr = Ar[0] * ipr - Ai[0] * ipi; ti = Ar[0] * ipi + Ai[0] * ipr;
+                    Ar[0] = tr; Ai[0] = ti;
                 }
 #pragma unroll
-                for (int i = 0; i < NM; ++i) {
-                    if (i == k || i >= NS) continue;
+                for (int i = 1; i < NM; ++i) {
+                    if (i >= NS) continue;
                     TC fr = hshfl(Ar[i], k), fi = hshfl(Ai[i], k);
                     Ar[i] -= fr * tr - fi * ti; Ai[i] -= fr * ti + fi * tr;
                 }
-            });
+                // rotate registers 0..NS-1 by one: the pivoted row goes last
+                const TC r0 = Ar[0], i0 = Ai[0];
+#pragma unroll
+                for (int i = 0; i + 1 < NM; ++i) {
+                    if (i + 1 < NS) { Ar[i] = Ar[i + 1]; Ai[i] = Ai[i + 1]; }
+                    else if (i + 1 == NS) { Ar[i] = r0; Ai[i] = i0; }
+                }
+                if (NS == NM) { Ar[NM - 1] = r0; Ai[NM - 1] = i0; }
+            }
             // unscramble: lane j takes column src(j)
 #pragma unroll
             for (int i = 0; i < NM; ++i) {

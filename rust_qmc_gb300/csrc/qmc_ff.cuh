@@ -111,6 +111,12 @@ __device__ __forceinline__ bool operator!=(ff a, ff b) { return !(a == b); }
 using ::fabs;
 __device__ __forceinline__ ff fabs(ff a) { return a.hi < 0.0f ? ff(-a.hi, -a.lo) : a; }
 
+// Leading part as a float (pivot choices and other comparisons that need no
+// more than FP32 resolution).
+__device__ __forceinline__ float lead(ff a) { return a.hi; }
+__device__ __forceinline__ float lead(float a) { return a; }
+__device__ __forceinline__ float lead(double a) { return (float)a; }
+
 // ---- square roots and reciprocals (one Newton correction) ------------------
 __device__ __forceinline__ ff frcp(ff b) {
     const float x = __frcp_rn(b.hi);

@@ -513,31 +513,35 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
             // -D[i][k]/a (1/a on the diagonal), the rest loses D[i][k] x row k
             // -- lane k's update takes the same form with t = 1 + 1/a.  The row
             // interchanges are undone as column interchanges: lane j gathers
-            // column src(j), src = tau_{n-1}( ... tau_0(j)).
+            // column src(j), src = tau_{n-1}( ... tau_0(j)).  The pivot loop is
+            // rolled, one copy of the step's code for all NS steps: the
+            // registers hold the rows rotated so that row k sits in register 0
+            // at step k (rows not yet pivoted first, in the order an unrolled
+            // loop would have them), and each step moves register 0 to the back.
             TC A[NM];
 #pragma unroll
             for (int i = 0; i < NM; ++i) A[i] = (i < NS && lane < NS) ? Mrow[i * 32 + lane] : TC(i == lane ? 1 : 0);
             int src = lane;
-            static_for<NM>([&](auto kc) {
-                constexpr int k = decltype(kc)::value;
-                if (k >= NS) return;
-                int p = k;
-                TC best = fabs(A[k]);
+#pragma unroll 1
+            for (int k = 0; k < NS; ++k) {
+                int p = 0;
+                float best = fabsf(lead(A[0]));
 #pragma unroll
-                for (int i = k + 1; i < NM; ++i) {
-                    TC a = fabs(A[i]);
-                    if (i < NS && a > best) { best = a; p = i; }
+                for (int r = 1; r < NM; ++r) {
+                    const float m = fabsf(lead(A[r]));
+                    if (r < NS - k && m > best) { best = m; p = r; }
                 }
                 p = wshfl(p, k);
 #pragma unroll
-                for (int i = k + 1; i < NM; ++i) {
-                    bool sw = (i == p);
-                    TC a = A[k], b = A[i];
-                    A[k] = sw ? b : a; A[i] = sw ? a : b;
+                for (int r = 1; r < NM; ++r) {
+                    bool sw = (r == p);
+                    TC a = A[0], b = A[r];
+                    A[0] = sw ? b : a; A[r] = sw ? a : b;
                 }
-                if (p != k) sg = -sg;
-                src = (src == k) ? p : ((src == p) ? k : src);
-                TC piv = wshfl(A[k], k);
+                if (p != 0) sg = -sg;
+                const int pk = k + p;
+                src = (src == k) ? pk : ((src == pk) ? k : src);
+                TC piv = wshfl(A[0], k);
                 if (!(piv != TC(0))) { ok = false; piv = TC(1); }
                 if (piv < 0) sg = -sg;
                 if constexpr (std::is_same<TC, ff>::value) {
@@ -547,15 +551,23 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
                     logdet += log(fabs((double)piv));
                 }
                 const TC ip = TC(1) / piv;
-                const TC t = (lane == k) ? TC(1) + ip : A[k] * ip;
-                A[k] = (lane == k) ? ip : t;
+                const TC t = (lane == k) ? TC(1) + ip : A[0] * ip;
+                A[0] = (lane == k) ? ip : t;
 #pragma unroll
-                for (int i = 0; i < NM; ++i) {
-                    if (i == k || i >= NS) continue;
+                for (int i = 1; i < NM; ++i) {
+                    if (i >= NS) continue;
                     const TC f = wshfl(A[i], k);
                     A[i] -= f * t;
                 }
-            });
+                // rotate registers 0..NS-1 by one: the pivoted row goes last
+                const TC r0 = A[0];
+#pragma unroll
+                for (int i = 0; i + 1 < NM; ++i) {
+                    if (i + 1 < NS) A[i] = A[i + 1];
+                    else if (i + 1 == NS) A[i] = r0;
+                }
+                if (NS == NM) A[NM - 1] = r0;
+            }
             // unscramble: lane j takes column src(j); then A[k] = D^-1[k][lane]
 #pragma unroll
             for (int i = 0; i < NM; ++i) {

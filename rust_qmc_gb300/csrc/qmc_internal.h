@@ -204,7 +204,8 @@ struct BatchClass {
                                          // (0: one block per tile); other launches: one block per tile
 };
 
-// Walkers per tile for a shape (threads per walker block or walkers per warp block).
+// Walkers per tile for a shape: threads per block for the thread-per-walker
+// shapes, a multiple of the warps per sweep block for the warp-per-walker ones.
 int batch_tile_width(int shape);
 // The launches of one class; `ctl` is device-resident.
 int launch_batch_sweep(const BatchClass& bc, int move_kind, const BatchCtl* ctl, cudaStream_t st);

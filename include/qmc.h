@@ -213,7 +213,10 @@ int qmc_logderiv_batch(qmc_sys_t sys, int W, const double* pos, double* O, doubl
 
 /* ForceCalculator::hellmann_feynman_force and wfn_nuclear_gradient
  * (src/sampling/traits.rs:38,50; src/systems/methane.rs:1007-1101,1241-1272):
- * F_hf [W x n_nuc x 3], omega = d ln|psi| / dR_I [W x n_nuc x 3]. */
+ * F_hf [W x n_nuc x 3], omega = d ln|psi| / dR_I [W x n_nuc x 3].
+ * Benzene has the Hellmann-Feynman force only (src/systems/benzene.rs:828-858;
+ * its wfn_nuclear_gradient is the trait's unimplemented default): omega must
+ * be NULL for it (QMC_ERR_UNSUPPORTED otherwise). */
 int qmc_forces_batch(qmc_sys_t sys, int W, const double* pos, double* F_hf, double* omega);
 
 /* ---- resident walker ensembles (the sampler state: Vec<MCMCState>,

@@ -173,11 +173,14 @@ class System:
                 "qmc_ratio_batch")
         return ratio, grad
 
-    def forces_batch(self, pos):
+    def forces_batch(self, pos, omega=True):
+        """(F_hf, omega) per configuration; omega=False skips the wave
+        function's nuclear gradient (and returns None for it), which benzene
+        does not have (its ForceCalculator has the Hellmann-Feynman force only)."""
         pos = self._pos(pos)
         W = pos.shape[0]
         F = np.zeros((W, self.spec.n_nuc, 3))
-        Om = np.zeros((W, self.spec.n_nuc, 3))
+        Om = np.zeros((W, self.spec.n_nuc, 3)) if omega else None
         L.check(self.lib.qmc_forces_batch(self.h, W, _d(pos), _d(F), _d(Om)), "qmc_forces_batch")
         return F, Om
 

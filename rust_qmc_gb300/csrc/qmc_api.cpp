@@ -751,6 +751,27 @@ int qmc_forces_batch(qmc_sys_t s, int W, const double* pos, double* F_hf, double
     CK(scratch_walkers(s, W, QMC_FP64, &wk));
     const HostSys& hs = s->hs;
     size_t per = (size_t)W * hs.n_nuc * 3;
+    if (hs.shape == SHAPE_C6H6 || hs.shape == SHAPE_HEG54) {
+        // ForceCalculator of BenzeneGTO (src/systems/benzene.rs:811-858):
+        // the Hellmann-Feynman force only; wfn_nuclear_gradient is the
+        // trait's unimplemented default (src/sampling/traits.rs:50-55).  The
+        // electron gas has no nuclei.
+        if (omega) return QMC_ERR_UNSUPPORTED;
+        if (!F_hf || per == 0) return QMC_OK;
+        CK(upload_positions(wk, pos));
+        CK(ensure_out(wk, per + 4 * (size_t)hs.n_nuc));
+        std::vector<double> nuc(4 * (size_t)hs.n_nuc);
+        for (int I = 0; I < hs.n_nuc; ++I) {
+            for (int c = 0; c < 3; ++c) nuc[4 * I + c] = hs.R[3 * I + c];
+            nuc[4 * I + 3] = hs.Z[I];
+        }
+        double* d_nuc = wk->d_out + per;
+        CU(cudaMemcpyAsync(d_nuc, nuc.data(), 8 * nuc.size(), cudaMemcpyHostToDevice, st));
+        if (launch_hf_force_walkers(wk->dw, hs.N, hs.n_nuc, d_nuc, wk->d_out, st)) return QMC_ERR_CUDA;
+        CU(cudaMemcpyAsync(F_hf, wk->d_out, 8 * per, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        return QMC_OK;
+    }
     CK(upload_positions(wk, pos));
     CK(ensure_out(wk, 2 * per));
     MeasureOut mo;

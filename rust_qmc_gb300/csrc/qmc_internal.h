@@ -127,6 +127,10 @@ int launch_flush(void* buf, size_t bytes, cudaStream_t st);
 // scratch holds hf_force_scratch_doubles(W, n_nuc) doubles.
 size_t hf_force_scratch_doubles(int W, int n_nuc);
 int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
+// Per-walker Hellmann-Feynman forces d_out [W][n_nuc][3] (electron order is
+// irrelevant: the force sums over all electrons).
+int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_out,
+                            cudaStream_t st);
 int launch_hf_force_sum(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_partial,
                         size_t partial_cap, double* d_out, cudaStream_t st);
 // DMC branching (src/sampling/is_dmc.rs:278-302): copies per walker from the

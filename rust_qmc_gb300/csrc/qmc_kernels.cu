@@ -253,6 +253,61 @@ __global__ void __launch_bounds__(TPB) k_hf_force_partials(const TS* __restrict_
     }
 }
 
+// Per-walker Hellmann-Feynman force for the shapes whose evaluation kernels
+// carry no force outputs (src/systems/benzene.rs:828-858, the form of
+// methane.rs:1241-1272): F[w][I] = Z_I sum_i (r_i - R_I) / |r_i - R_I|^3
+// - sum_{J != I} Z_I Z_J (R_I - R_J) / |R_I - R_J|^3, distances below 1e-10
+// skipped.  One thread per (walker, nucleus), t = w n_nuc + I, which is also
+// the output row; nuc = [n_nuc][4] (x, y, z, Z).
+template <class TS>
+__global__ void k_hf_force_walkers(const TS* __restrict__ pos, int W, int Wcap, int N, int n_nuc,
+                                   const double* __restrict__ nuc, double* __restrict__ F) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= W * n_nuc) return;
+    const int w = t / n_nuc, I = t - w * n_nuc;
+    const double X = nuc[4 * I], Y = nuc[4 * I + 1], Zc = nuc[4 * I + 2], Q = nuc[4 * I + 3];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int i = 0; i < N; ++i) {
+        const double dx = (double)pos[(size_t)(3 * i) * Wcap + w] - X;
+        const double dy = (double)pos[(size_t)(3 * i + 1) * Wcap + w] - Y;
+        const double dz = (double)pos[(size_t)(3 * i + 2) * Wcap + w] - Zc;
+        const double d2 = dx * dx + dy * dy + dz * dz;
+        const double d = sqrt(d2);
+        if (d > 1e-10) {
+            const double f = Q / (d2 * d);
+            fx += f * dx; fy += f * dy; fz += f * dz;
+        }
+    }
+    for (int J = 0; J < n_nuc; ++J) {
+        if (J == I) continue;
+        const double dx = X - nuc[4 * J], dy = Y - nuc[4 * J + 1], dz = Zc - nuc[4 * J + 2];
+        const double d2 = dx * dx + dy * dy + dz * dz;
+        const double d = sqrt(d2);
+        if (d > 1e-10) {
+            const double f = Q * nuc[4 * J + 3] / (d2 * d);
+            fx -= f * dx; fy -= f * dy; fz -= f * dz;
+        }
+    }
+    F[(size_t)t * 3] = fx;
+    F[(size_t)t * 3 + 1] = fy;
+    F[(size_t)t * 3 + 2] = fz;
+}
+
+int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_out,
+                            cudaStream_t st) {
+    const long long n = (long long)dw.W * n_nuc;
+    if (n <= 0) return 0;
+    if (n > 0x7fffffffLL) return 1;
+    const int tpb = 128;
+    const int nb = (int)((n + tpb - 1) / tpb);
+    if (dw.prec == 0)
+        k_hf_force_walkers<double><<<nb, tpb, 0, st>>>((const double*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc, d_out);
+    else
+        k_hf_force_walkers<float><<<nb, tpb, 0, st>>>((const float*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc, d_out);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
 size_t hf_force_scratch_doubles(int W, int n_nuc) { return (size_t)2 * ((W + 127) / 128) * 3 * n_nuc; }
 
 int launch_hf_force_sum(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_partial,

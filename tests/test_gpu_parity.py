@@ -190,6 +190,21 @@ def test_forces_match_oracle_and_fd(ctx, oracle, name):
     np.testing.assert_allclose(Om[:8], fd, rtol=1e-5, atol=1e-6)
 
 
+def test_benzene_hf_force_matches_oracle(ctx, oracle):
+    """BenzeneGTO's ForceCalculator (src/systems/benzene.rs:811-858): the
+    Hellmann-Feynman force per configuration; it has no wave-function nuclear
+    gradient (the trait's unimplemented default), so asking for one fails."""
+    spec = Q.benzene_minimal()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 37, seed=13)
+    F, Om = sysh.forces_batch(cfg, omega=False)
+    assert Om is None
+    Fo, _ = oracle.forces(spec, cfg)
+    assert rel(F, Fo) < 1e-12
+    with pytest.raises(Q.QMCError):
+        sysh.forces_batch(cfg[:2])
+
+
 def test_trait_surface_single_configuration(ctx, oracle):
     """MultiWfn/EnergyCalculator/OptimizableWfn/ForceCalculator methods with
     the reference's value conventions (psi, grad psi, lap psi)."""

@@ -55,6 +55,54 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+class Replicas:
+    """The host-side exchange of an N-replica run (one process per GPU, each
+    advancing its own walkers): a gloo group used only for the barriers
+    around the timed region, the max-over-ranks time and the summed move
+    counts.  The walkers themselves never cross ranks (no data-path
+    collective)."""
+
+    def __init__(self, world):
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def _reduce(self, x, op):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, self.pg.ReduceOp.MAX if self.pg else None)
+
+    def sum(self, x):
+        return self._reduce(x, self.pg.ReduceOp.SUM if self.pg else None)
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+            self.pg = None
+
+
+def replica_seed(base, rank):
+    """Disjoint Philox keys per replica."""
+    return base + 2 + 1000 * rank
+
+
+def whole_job_rate(moves_this_rank, seconds_this_rank, group):
+    """Moves of all ranks over the slowest rank's time."""
+    return group.sum(moves_this_rank) / group.max(seconds_this_rank)
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -181,37 +229,14 @@ def main():
     import rust_qmc_gb300 as Q
     from rust_qmc_gb300 import _lib as L
 
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        pg = dist
-
-    def barrier():
-        if pg:
-            pg.barrier()
-
-    def max_over_ranks(x):
-        if not pg:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(x):
-        if not pg:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.SUM)
-        return float(t.item())
+    group = Replicas(world)
+    barrier, max_over_ranks, sum_over_ranks = group.barrier, group.max, group.sum
 
     ctx = Q.Context(local)
     spec = Q.methane_minimal()
     sysh = Q.System(ctx, spec)
     W, SW = args.walkers, args.sweeps
-    seed = Q.SEED_BASE + 2 + 1000 * rank
+    seed = replica_seed(Q.SEED_BASE, rank)
     moves_per_step = W * N_ELEC * SW
 
     def make(prec):
@@ -254,8 +279,7 @@ def main():
     clk = clocks.stop()
     flush_launches = args.steps
     gpu_launches = ctx.launch_count() - launches0 - flush_launches
-    total_s = max_over_ranks(sum(step_ms) / 1e3)
-    value = sum_over_ranks(moves_per_step * args.steps) / total_s
+    value = whole_job_rate(moves_per_step * args.steps, sum(step_ms) / 1e3, group)
     e_mean = wk.refresh() / W
     flags = wk.status()
 
@@ -366,8 +390,7 @@ def main():
     wk.close()
     sysh.close()
     ctx.close()
-    if pg:
-        pg.destroy_process_group()
+    group.close()
 
 
 if __name__ == "__main__":

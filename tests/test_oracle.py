@@ -176,6 +176,34 @@ def test_methane_ranges():
     assert 10.0 < spec.v_nn() < 20.0
 
 
+def test_benzene_ranges():
+    """The reference's benzene checks (src/systems/benzene.rs:871-913,926-932)
+    on the benzene workload: carbons on a ring of radius C-C = 2.64 bohr,
+    C-C-C angles 120 degrees, a planar molecule, C-H 2.05 bohr (the
+    workload's bond; the reference builds 2.042), V_nn in (180, 230) Ha,
+    and 36 AOs for 21 doubly occupied MOs (the reference: 66 AOs, 6-31G)."""
+    spec = Q.benzene_minimal()
+    R, Z = spec.nuc_pos, spec.nuc_charge
+    C = R[Z == 6]
+    H = R[Z == 1]
+    assert len(C) == 6 and len(H) == 6 and spec.n_elec == 42
+    cc = 2.64
+    for i in range(6):
+        assert abs(np.linalg.norm(C[i]) - cc) < 1e-10
+        assert abs(np.linalg.norm(C[i] - C[(i + 1) % 6]) - cc) < 0.01
+        v1 = C[(i + 5) % 6] - C[i]
+        v2 = C[(i + 1) % 6] - C[i]
+        ang = math.degrees(math.acos(v1 @ v2 / np.linalg.norm(v1) / np.linalg.norm(v2)))
+        assert abs(ang - 120.0) < 0.1
+    assert np.all(np.abs(R[:, 2]) < 1e-10)
+    for i in range(6):
+        assert abs(min(np.linalg.norm(H[i] - c) for c in C) - 2.05) < 0.01
+    assert 180.0 < spec.v_nn() < 230.0
+    occ = np.asarray(spec.occ)
+    assert len(spec.ao_nuc) == 36 and sorted(set(occ.tolist())) == list(range(21))
+    assert np.sum(np.asarray(spec.spins) > 0) == 21
+
+
 def test_synthetic_mo_orthonormal():
     spec = Q.methane_minimal()
     M = spec.mo_coef

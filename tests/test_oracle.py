@@ -246,6 +246,19 @@ def test_heg_box_and_shells():
     assert shells == [0.0, 1.0, round(math.sqrt(2), 8), round(math.sqrt(3), 8)]
 
 
+def test_heg_fourteen_electrons_and_cusp_amplitudes():
+    """heg.rs:943-993: 14 electrons at r_s = 4 (7 per spin): L = (4 pi 14 / 3)^(1/3) r_s,
+    k = 0 then six vectors of the first shell; the Jastrow amplitudes A_same = 0.5,
+    A_anti = 0.25 (heg.rs:146-147)."""
+    spec = Q.electron_gas(14, 4.0)
+    assert abs(spec.box_L - (4 * math.pi / 3 * 14) ** (1 / 3) * 4.0) < 1e-10
+    assert list(spec.spins).count(1) == 7 and list(spec.spins).count(-1) == 7
+    kn = np.linalg.norm(spec.mo_coef, axis=1)
+    assert len(kn) == 7 and kn[0] == 0.0
+    np.testing.assert_allclose(kn[1:], 2 * math.pi / spec.box_L, rtol=1e-12)
+    assert spec.jas[2] == 0.25 and spec.jas[3] == 0.5       # antiparallel, parallel
+
+
 def test_heg_madelung_constant(oracle):
     """One electron in a cubic box with a neutralising background: the Ewald
     energy is -xi / (2 L) with the simple-cubic Madelung constant

@@ -22,6 +22,24 @@ from .api import System, batch_run
 from .systems import electron_gas, monkhorst_pack_grid
 
 
+def hartree_fock_energy(rs):
+    """Hartree-Fock energy per electron of the paramagnetic electron gas
+    (HomogeneousElectronGas::hartree_fock_energy, src/systems/heg.rs:819-831):
+    (3/5) k_F^2 / 2 - 3 k_F / (4 pi) with k_F = (9 pi / 4)^(1/3) / r_s."""
+    kf = (9.0 * math.pi / 4.0) ** (1.0 / 3.0) / rs
+    return 0.3 * kf * kf - 3.0 * kf / (4.0 * math.pi)
+
+
+def correlation_energy(rs):
+    """Perdew-Zunger fit of the Ceperley-Alder correlation energy per electron
+    (paramagnetic), the reference value the twist example prints
+    (src/systems/heg.rs:834-849): gamma / (1 + beta1 sqrt(r_s) + beta2 r_s)
+    for r_s >= 1, A ln r_s + B + C r_s ln r_s + D r_s below."""
+    if rs >= 1.0:
+        return -0.1423 / (1.0 + 1.0529 * math.sqrt(rs) + 0.3334 * rs)
+    return 0.0311 * math.log(rs) - 0.048 + 0.0020 * rs * math.log(rs) - 0.0116 * rs
+
+
 def average_twists(energies, errors):
     """(E, reference error, standard error of the mean) over the twists."""
     e = np.asarray(energies, dtype=np.float64)
@@ -50,5 +68,10 @@ def twist_average(ctx, n_grid, *, walkers_per_twist, n_steps, n_burnin=0, step=2
         for s in systems:
             s.close()
     e, err, err_mean = average_twists([r["energy"] for r in runs], [r["error"] for r in runs])
+    rs = gas.get("rs", 4.0)
+    # the reference values printed beside the result (heg_vmc.rs:137-145)
+    e_hf, e_c = hartree_fock_energy(rs), correlation_energy(rs)
     return dict(energy=e, error=err, error_of_mean=err_mean, energy_per_electron=e / n_elec,
-                error_per_electron=err / n_elec, twists=twists, runs=runs)
+                error_per_electron=err / n_elec, twists=twists, runs=runs,
+                hartree_fock_per_electron=e_hf, correlation_per_electron=e_c,
+                expected_total_per_electron=e_hf + e_c)

@@ -4,6 +4,7 @@ src/systems/heg.rs:176-232; the averages restate examples/heg_vmc.rs:178-186."""
 import math
 
 import numpy as np
+import pytest
 
 import rust_qmc_gb300 as Q
 from rust_qmc_gb300.twist import average_twists
@@ -56,3 +57,22 @@ def test_average_twists_matches_reference_formula():
     assert avg == sum(e) / 4
     assert err == math.sqrt(sum(x * x for x in s) / 4)
     assert err_mean == math.sqrt(sum(x * x for x in s)) / 4
+
+
+def test_hartree_fock_energy_ranges():
+    """The reference's own check (src/systems/heg.rs:1027-1038): E_HF/N in
+    (0.5, 1.0) Ha at r_s = 1 and in (-0.1, 0) at r_s = 4; the closed form
+    1.105/r_s^2 - 0.458/r_s of its docstring."""
+    from rust_qmc_gb300.twist import hartree_fock_energy
+    assert 0.5 < hartree_fock_energy(1.0) < 1.0
+    assert -0.1 < hartree_fock_energy(4.0) < 0.0
+    for rs in (1.0, 2.0, 4.0, 10.0):
+        assert abs(hartree_fock_energy(rs) - (1.105 / rs ** 2 - 0.458 / rs)) < 2e-3 / rs
+
+
+def test_correlation_fit_is_continuous_at_rs_one():
+    """The two branches of the Perdew-Zunger fit meet at r_s = 1 (heg.rs:834-849)."""
+    from rust_qmc_gb300.twist import correlation_energy
+    assert abs(correlation_energy(1.0) - correlation_energy(1.0 - 1e-9)) < 1e-4
+    assert correlation_energy(4.0) == pytest.approx(-0.1423 / (1 + 1.0529 * 2 + 0.3334 * 4))
+    assert correlation_energy(0.5) < correlation_energy(4.0) < 0

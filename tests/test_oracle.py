@@ -95,11 +95,13 @@ def test_lithium_quirks_reproduce_reference_formulas(oracle):
     np.testing.assert_allclose(l, J * lw, rtol=1e-12)
 
 
-@pytest.mark.parametrize("builder", ["ch4_gto", "ch4_min"])
+@pytest.mark.parametrize("builder", ["ch4_gto", "ch4_min", "c6h6"])
 def test_log_derivatives_vs_fd(oracle, builder):
     """O_p = d ln|psi| / dp vs central differences (src/systems/methane.rs:
-    1340-1373), all 8 Jastrow parameters and the MO-rotation angles."""
-    spec = Q.methane_gto(2.0, 3.0) if builder == "ch4_gto" else Q.methane_minimal()
+    1340-1373, benzene.rs:976-1006), all 8 Jastrow parameters and the
+    MO-rotation angles."""
+    spec = {"ch4_gto": lambda: Q.methane_gto(2.0, 3.0), "ch4_min": Q.methane_minimal,
+            "c6h6": Q.benzene_minimal}[builder]()
     if builder == "ch4_min":
         spec = spec.with_params(np.concatenate([spec.jas, [0.1, -0.2, 0.05, 0.3]]))
     r = random_configs(spec, 2, seed=3)
@@ -116,11 +118,13 @@ def test_log_derivatives_vs_fd(oracle, builder):
         np.testing.assert_allclose(O[:, k], fd, rtol=1e-6, atol=1e-7)
 
 
-def test_reference_four_parameter_derivatives(oracle):
-    """MethaneGTO's d_ln_j_d_{bee,ben,a_anti,a_para} (src/correlation/
-    jastrow.rs:326-391) are sums of the generalised derivatives, checked by FD
-    with b_anti=b_para and B0=B1 tied as in the reference."""
-    spec = Q.methane_gto(2.0, 3.0)
+@pytest.mark.parametrize("builder", ["ch4_gto", "c6h6"])
+def test_reference_four_parameter_derivatives(oracle, builder):
+    """The four log-derivatives d_ln_j_d_{bee,ben,a_anti,a_para} of MethaneGTO
+    and BenzeneGTO's OptimizableWfn (src/correlation/jastrow.rs:326-391,
+    src/systems/benzene.rs:726-756) are sums of the generalised derivatives,
+    checked by FD with b_anti=b_para and B0=B1 tied as in the reference."""
+    spec = Q.methane_gto(2.0, 3.0) if builder == "ch4_gto" else Q.benzene_minimal()
     r = random_configs(spec, 1, seed=9)
     O = oracle.log_derivatives(spec, r)[0]
     ref4 = [O[0] + O[1], O[4] + O[5], O[2], O[3]]

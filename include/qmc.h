@@ -205,9 +205,11 @@ int qmc_eval_batch(qmc_sys_t sys, int W, const double* pos, int precision,
                    double* e_local);
 
 /* OptimizableWfn::log_derivatives (src/wavefunction/traits.rs:114;
- * src/systems/methane.rs:1212-1219): O [W x P] plus E_L [W]; optionally the
- * FP64 compensated SR sums over the batch: S [P x P] = <O O^T> - <O><O>^T,
- * f [P] = <E O> - <E><O>, e_mean (any may be NULL). */
+ * src/systems/methane.rs:1212-1219, benzene.rs:748-755): O [W x P] plus
+ * E_L [W]; optionally the FP64 compensated SR sums over the batch:
+ * S [P x P] = <O O^T> - <O><O>^T, f [P] = <E O> - <E><O>, e_mean (any may be
+ * NULL).  Systems with the Jastrow3 factor; benzene without MO-rotation
+ * angles (P = 8). */
 int qmc_logderiv_batch(qmc_sys_t sys, int W, const double* pos, double* O, double* e_local,
                        double* S, double* f, double* e_mean);
 

@@ -708,12 +708,34 @@ int qmc_logderiv_batch(qmc_sys_t s, int W, const double* pos, double* O, double*
     int P = hs.n_params();
     int M = 2 + 2 * P + P * (P + 1) / 2;
     int nblk = std::min(1024, std::max(1, (W + 255) / 256));
-    size_t need = (size_t)W * P + (size_t)M + 2 * (size_t)M * nblk + 64;
+    // benzene (OptimizableWfn of BenzeneGTO, src/systems/benzene.rs:726-756):
+    // the warp kernels give E_L, a per-walker kernel the Jastrow derivatives;
+    // MO-rotation angles would need the determinant and are not compiled
+    const bool warp = hs.shape == SHAPE_C6H6;
+    if (warp && P != 8) return QMC_ERR_UNSUPPORTED;
+    const size_t base = (size_t)W * P + (size_t)M + 2 * (size_t)M * nblk + 64;
+    const size_t extra = warp ? 8 + 5 * (size_t)hs.n_nuc : 0;   // jas[8] and the nuclei [n_nuc][5]
     CK(upload_positions(wk, pos));
-    CK(ensure_out(wk, need));
+    CK(ensure_out(wk, base + extra));
     MeasureOut mo;
-    mo.O = wk->d_out;
-    CK(launch_measure(hs, wk->dw, 0, true, mo, st));
+    std::vector<double> tab;
+    if (warp) {
+        CK(launch_measure(hs, wk->dw, 0, true, mo, st));          // FP64 refresh: E_L into dw.el
+        tab.assign(hs.jas, hs.jas + 8);
+        for (int I = 0; I < hs.n_nuc; ++I) {
+            for (int c = 0; c < 3; ++c) tab.push_back(hs.R[3 * I + c]);
+            tab.push_back(hs.Z[I]);
+            tab.push_back((double)hs.species[I]);
+        }
+        double* d_tab = wk->d_out + base;
+        CU(cudaMemcpyAsync(d_tab, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice, st));
+        if (launch_jastrow3_logderiv(wk->dw, hs.N, hs.n_up, hs.n_nuc, d_tab + 8, d_tab, P, wk->d_out, st))
+            return QMC_ERR_CUDA;
+        mo.O = wk->d_out;
+    } else {
+        mo.O = wk->d_out;
+        CK(launch_measure(hs, wk->dw, 0, true, mo, st));
+    }
     double* d_sums = wk->d_out + (size_t)W * P;
     double* d_scr = d_sums + M;
     if (S || f || e_mean)

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include "qmc_internal.h"
 #include "qmc_device.cuh"
+#include "qmc_jastrow3_logderiv.h"
 
 namespace qmc {
 
@@ -304,6 +305,38 @@ int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double
         k_hf_force_walkers<double><<<nb, tpb, 0, st>>>((const double*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc, d_out);
     else
         k_hf_force_walkers<float><<<nb, tpb, 0, st>>>((const float*)dw.pos, dw.W, dw.Wcap, N, n_nuc, d_nuc, d_out);
+    ++g_launch_count;
+    return cuda_status(cudaGetLastError());
+}
+
+// Jastrow3 parameter log-derivatives, one thread per walker, for the shapes
+// whose evaluation kernels carry no O_p outputs (qmc_jastrow3_logderiv.h):
+// O[w][0..7] with row stride P; par = p[8], nuc = [n_nuc][5].
+template <class TS>
+__global__ void k_jastrow3_logderiv(const TS* __restrict__ pos, int W, int Wcap, int N, int n_up, int n_nuc,
+                                    const double* __restrict__ nuc, const double* __restrict__ par, int P,
+                                    double* __restrict__ O) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= W) return;
+    auto at = [&](int i, int c) { return (double)pos[(size_t)(3 * i + c) * Wcap + w]; };
+    double o[8];
+    jastrow3_log_derivatives(N, n_up, n_nuc, nuc, par, at, o);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) O[(size_t)w * P + k] = o[k];
+}
+
+int launch_jastrow3_logderiv(const DevWalkers& dw, int N, int n_up, int n_nuc, const double* d_nuc,
+                             const double* d_par, int P, double* d_O, cudaStream_t st) {
+    if (dw.W <= 0) return 0;
+    if (P < 8) return 1;
+    const int tpb = 128;
+    const int nb = (dw.W + tpb - 1) / tpb;
+    if (dw.prec == 0)
+        k_jastrow3_logderiv<double><<<nb, tpb, 0, st>>>((const double*)dw.pos, dw.W, dw.Wcap, N, n_up, n_nuc, d_nuc,
+                                                        d_par, P, d_O);
+    else
+        k_jastrow3_logderiv<float><<<nb, tpb, 0, st>>>((const float*)dw.pos, dw.W, dw.Wcap, N, n_up, n_nuc, d_nuc,
+                                                       d_par, P, d_O);
     ++g_launch_count;
     return cuda_status(cudaGetLastError());
 }

@@ -335,6 +335,28 @@ def test_benzene_eval_fp64_matches_oracle(ctx, oracle):
     assert rel(g["e_local"], o["e_local"]) < 1e-10
 
 
+def test_benzene_log_derivatives_and_sr_sums(ctx, oracle):
+    """BenzeneGTO's OptimizableWfn (src/systems/benzene.rs:726-756) on the
+    device: the eight Jastrow log-derivatives per configuration, E_L from the
+    FP64 refresh, and the SR sums S, f over the batch."""
+    spec = Q.benzene_minimal()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 96, seed=15)
+    O, E, S, f, em = sysh.logderiv_batch(cfg, sums=True)
+    Oo = oracle.log_derivatives(spec, cfg)
+    Eo = oracle.evaluate(spec, cfg)["e_local"]
+    assert O.shape == (96, 8)
+    assert rel(O, Oo) < 1e-10
+    assert rel(E, Eo) < 1e-9
+    n = len(E)
+    Om = Oo.mean(0)
+    S_ref = Oo.T @ Oo / n - np.outer(Om, Om)
+    f_ref = (Eo[:, None] * Oo).mean(0) - Eo.mean() * Om
+    np.testing.assert_allclose(S, S_ref, rtol=1e-8, atol=1e-8 * np.abs(S_ref).max())
+    np.testing.assert_allclose(f, f_ref, rtol=1e-7, atol=1e-7 * np.abs(f_ref).max())
+    assert abs(em - Eo.mean()) < 1e-9 * max(1.0, np.abs(Eo).mean())
+
+
 @pytest.mark.parametrize("move", [L.QMC_MOVE_ONE_GAUSS, L.QMC_MOVE_ONE_DRIFT])
 def test_benzene_fp64_trajectory_matches_oracle(ctx, oracle, move):
     spec = Q.benzene_minimal()

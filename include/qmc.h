@@ -151,6 +151,19 @@ typedef struct {
     int fixed_node;              /* DMC: refuse sign-changing proposals (the reference accepts them) */
     int reference_diffusion;     /* DMC: move with variance 2 tau as the reference does (is_dmc.rs:218-225);
                                     0 = Hartree-unit diffusion (variance tau, drift tau grad ln psi) */
+    /* VMC step adaptation (MCMCParams target_acceptance / adaptation_interval /
+     * min_step_size / max_step_size, src/sampling/vmc.rs:13-21; DDVMCParams
+     * :197-226).  target_acceptance > 0 turns it on: every adaptation_interval
+     * steps (sweeps), through burn-in and production, the acceptance of that
+     * window rescales the all-electron or Gaussian step by sqrt(rate / target)
+     * (MCMCSimulation::adapt_step_size, vmc.rs:122-128) or tau by that factor
+     * clamped to [0.8, 1.2] (DriftDiffusionVMC::adapt_time_step,
+     * vmc.rs:397-402), then clamps it to [min_step, max_step] (0 = the
+     * reference's [0.001, 0.05] for tau, no bound for the step). */
+    double target_acceptance;
+    int adaptation_interval;
+    double min_step;
+    double max_step;
     int reserved[4];
 } qmc_run_params;
 
@@ -163,7 +176,8 @@ typedef struct {
     int n_samples;
     int status_flags;
     double avg_population;
-    double reserved[4];
+    double final_step;           /* VMC: the step (all-electron / Gaussian) or tau (drift) after adaptation */
+    double reserved[3];
 } qmc_run_result;
 
 typedef struct qmc_ctx_s* qmc_ctx_t;
@@ -206,12 +220,16 @@ int qmc_eval_batch(qmc_sys_t sys, int W, const double* pos, int precision,
 
 /* OptimizableWfn::log_derivatives (src/wavefunction/traits.rs:114;
  * src/systems/methane.rs:1212-1219, benzene.rs:748-755): O [W x P] plus
- * E_L [W]; optionally the FP64 compensated SR sums over the batch:
- * S [P x P] = <O O^T> - <O><O>^T, f [P] = <E O> - <E><O>, e_mean (any may be
- * NULL).  Systems with the Jastrow3 factor; benzene without MO-rotation
- * angles (P = 8). */
+ * E_L [W]; dEL [W x P] = d E_L / d p (the derivative of
+ * EnergyCalculator::local_energy, src/systems/methane.rs:1154-1182, in each
+ * optimisable parameter; analytic: through the Jastrow's gradient and
+ * Laplacian and, for MO-rotation angles, through the Slater inverse);
+ * optionally the FP64 compensated SR sums over the batch
+ * (src/sampling/sr_optimize.rs:176-246): S [P x P] = <O O^T> - <O><O>^T,
+ * f [P] = <E O> - <E><O>, e_mean (any output may be NULL).  Systems with the
+ * Jastrow3 factor; benzene without MO-rotation angles (P = 8). */
 int qmc_logderiv_batch(qmc_sys_t sys, int W, const double* pos, double* O, double* e_local,
-                       double* S, double* f, double* e_mean);
+                       double* dEL, double* S, double* f, double* e_mean);
 
 /* ForceCalculator::hellmann_feynman_force and wfn_nuclear_gradient
  * (src/sampling/traits.rs:38,50; src/systems/methane.rs:1007-1101,1241-1272):
@@ -355,7 +373,8 @@ int qmc_batch_refresh(qmc_batch_t batch, double* e_mean);
 int qmc_batch_run_steps(qmc_batch_t batch, int move_kind, int n_steps, int sweeps_per_step, uint64_t step0,
                         double step, double tau, double max_drift, uint64_t seed, double* e_series);
 /* VMC of n_sys systems in one batch (W[i] walkers each, params->n_walkers
- * ignored; single-electron moves): system i follows exactly the schedule of
+ * ignored; single-electron moves; fixed step: QMC_ERR_UNSUPPORTED with
+ * target_acceptance > 0): system i follows exactly the schedule of
  * qmc_vmc_run(systems[i], params, qmc_batch_system_seed(seed, i)) and
  * per_sys[i] holds its result.  energies (may be NULL) receives
  * [ceil(n_steps / refresh_every)][n_sys] per-measurement means. */

@@ -27,11 +27,12 @@ def lib():
         l.orc_eval.argtypes = [vp, C.c_int, _dp, _dp, _ip, _dp, _dp, _dp, C.c_int]
         l.orc_jastrow.argtypes = [vp, _dp, _dp, _dp, _dp]
         l.orc_logderiv.argtypes = [vp, C.c_int, _dp, _dp, C.c_int]
+        l.orc_el_derivs.argtypes = [vp, C.c_int, _dp, _dp, C.c_int]
         l.orc_forces.argtypes = [vp, C.c_int, _dp, _dp, _dp, C.c_int]
         l.orc_forces_fd.argtypes = [vp, C.c_int, _dp, C.c_double, _dp]
         l.orc_init.argtypes = [vp, C.c_int, C.c_uint32, C.c_uint64, _dp]
         l.orc_sweeps.argtypes = [vp, C.c_int, C.c_uint32, _dp, C.c_int, C.c_uint64, C.c_int, C.c_double,
-                                 C.c_double, C.c_double, C.c_uint64, _ip, _dp, C.c_int]
+                                 C.c_double, C.c_double, C.c_uint64, _ip, _dp, _dp, C.c_int]
         l.orc_dmc.argtypes = [vp, C.c_int, _dp, C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_int,
                               C.c_double,
                               C.c_int, C.c_uint64, C.c_int, _dp, _ip, _ip, _dp, _dp, C.c_int]
@@ -96,6 +97,35 @@ def log_derivatives(spec, pos, threads=None):
     return O
 
 
+def el_derivatives(spec, pos, threads=None):
+    """dE_L / dp per configuration [W, P] (analytic, oracle's el_derivs)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    W = pos.shape[0]
+    dE = np.zeros((W, spec.n_params))
+    d = spec.desc()
+    lib().orc_el_derivs(C.byref(d), W, _d(pos), _d(dE), threads or threads_default())
+    return dE
+
+
+def el_derivatives_fd(spec, pos, h=1e-4, threads=None):
+    """Central finite differences of the oracle's E_L in each parameter."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    if pos.ndim == 2:
+        pos = pos[None]
+    p0 = np.asarray(spec.params(), dtype=np.float64)
+    out = np.zeros((pos.shape[0], len(p0)))
+    for k in range(len(p0)):
+        pp, pm = p0.copy(), p0.copy()
+        pp[k] += h
+        pm[k] -= h
+        ep = evaluate(spec.with_params(pp), pos, threads)["e_local"]
+        em = evaluate(spec.with_params(pm), pos, threads)["e_local"]
+        out[:, k] = (ep - em) / (2 * h)
+    return out
+
+
 def forces(spec, pos, threads=None):
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     if pos.ndim == 2:
@@ -127,15 +157,20 @@ def init_positions(spec, W, seed, walker0=0):
 
 
 def sweeps(spec, pos, n_sweeps, sweep0, move_kind, seed, step=0.3, tau=0.01, max_drift=1.0, walker0=0,
-           threads=None, want_energy=True):
-    """Reference-algorithm Monte Carlo sweeps; returns (pos, accepted, e_local)."""
+           threads=None, want_energy=True, want_margin=False):
+    """Reference-algorithm Monte Carlo sweeps; returns (pos, accepted, e_local),
+    plus with want_margin the per-walker smallest relative distance between
+    an acceptance uniform and its acceptance probability."""
     pos = np.array(pos, dtype=np.float64, copy=True)
     W = pos.shape[0]
     acc = np.zeros(W, np.int32)
     el = np.zeros(W) if want_energy else None
+    mg = np.zeros(W) if want_margin else None
     d = spec.desc()
     lib().orc_sweeps(C.byref(d), W, walker0, _d(pos), n_sweeps, sweep0, move_kind, step, tau, max_drift, seed,
-                     _i(acc), _d(el), threads or threads_default())
+                     _i(acc), _d(el), _d(mg), threads or threads_default())
+    if want_margin:
+        return pos, acc, el, mg
     return pos, acc, el
 
 

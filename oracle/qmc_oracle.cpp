@@ -797,6 +797,98 @@ void log_derivs(const Sys& s, const std::vector<V3>& r, double* O) {
     }
 }
 
+// Parameter derivatives of the local energy, dE_L / dp, in the order of
+// log_derivs.  The reference has no such function; its SR sampling
+// (src/sampling/sr_optimize.rs:104-246) and EnergyCalculator::local_energy
+// (src/systems/methane.rs:1154-1182) define what is differentiated:
+//   E_L = -1/2 sum_i lap_i psi / psi + V,  lap_i psi / psi = l_i + 2 g_i . j_i + lu_i + |j_i|^2
+// with g_i, l_i the determinant's gradient and Laplacian (over psi_D) and j_i,
+// lu_i the Jastrow's.  V does not depend on p, so
+//   Jastrow p:  dE_L/dp = -1/2 sum_i [ d lu_i/dp + 2 (g_i + j_i) . d j_i/dp ]
+//   rotation q (column c of a sector, d phi_c/d theta = psi_c):
+//     with B = A^-1, beta = B psi_c(r_.), for X in {grad, lap} of the MOs,
+//     d (X B)_ii = X_psi(r_i) B_ci - B_ci sum_k X_k(r_i) beta_k,
+//     dE_L/dq = -1/2 sum_i [ d (L B)_ii + 2 d (G B)_ii . j_i ].
+// Checked in the tests against central finite differences of E_L.
+void el_derivs(const Sys& s, const std::vector<V3>& r, double* dE) {
+    int nrot = (int)s.rot_occ.size();
+    for (int p = 0; p < 8 + nrot; ++p) dE[p] = 0.0;
+    Eval ev = evaluate_full(s, r);
+    if (s.jk == 2) {
+        const double* p = s.jas;
+        for (int i = 0; i < s.N; ++i)
+            for (int j = i + 1; j < s.N; ++j) {
+                bool para = s.spins[i] == s.spins[j];
+                int c = para ? 1 : 0;
+                double a = p[2 + c], b = p[c];
+                V3 rij = r[i] - r[j];
+                double d = norm(rij);
+                if (d < 1e-10) continue;
+                double den = 1.0 + b * d;
+                double gdot = dot(ev.grad[i] - ev.grad[j], rij);
+                // d/da: j_i gains rij / (den^2 d); lu_i, lu_j gain 2/(d den^2) - 2b/den^3 each
+                double fa = 1.0 / (den * den * d), la = 2.0 / (d * den * den) - 2.0 * b / (den * den * den);
+                // d/db: j_i gains -2a rij / den^3; lu gains -6a/den^4 each
+                double fb = -2.0 * a / (den * den * den), lb = -6.0 * a / (den * den * den * den);
+                dE[2 + c] += -0.5 * (2.0 * la + 2.0 * fa * gdot);
+                dE[c] += -0.5 * (2.0 * lb + 2.0 * fb * gdot);
+            }
+        for (int i = 0; i < s.N; ++i)
+            for (int I = 0; I < s.n_nuc; ++I) {
+                int sp = s.species[I];
+                double Zi = s.Z[I], A = p[6 + sp] * Zi, B = p[4 + sp];
+                V3 riI = r[i] - s.R[I];
+                double d = norm(riI);
+                if (d < 1e-10) continue;
+                double den = 1.0 + B * d;
+                double gdot = dot(ev.grad[i], riI);
+                // j_i gains -A riI/(den^2 d); lu_i gains -2A/(d den^2) + 2AB/den^3
+                double fA = -Zi / (den * den * d), lA = -2.0 * Zi / (d * den * den) + 2.0 * Zi * B / (den * den * den);
+                double fB = 2.0 * A / (den * den * den), lB = 6.0 * A / (den * den * den * den);
+                dE[6 + sp] += -0.5 * (lA + 2.0 * fA * gdot);
+                dE[4 + sp] += -0.5 * (lB + 2.0 * fB * gdot);
+            }
+    }
+    if (!nrot) return;
+    std::vector<double> dC((size_t)s.n_mo * s.n_ao, 0.0);
+    for (int q = 0; q < nrot; ++q) {
+        int k = s.rot_occ[q], v = s.rot_virt[q];
+        double c = std::cos(s.rot_angle[q]), sn = std::sin(s.rot_angle[q]);
+        for (int a = 0; a < s.n_ao; ++a)
+            dC[(size_t)k * s.n_ao + a] = -sn * s.C0[(size_t)k * s.n_ao + a] + c * s.C0[(size_t)v * s.n_ao + a];
+    }
+    for (int q = 0; q < nrot; ++q) {
+        int k = s.rot_occ[q];
+        double acc = 0.0;
+        for (int sp = 0; sp < 2; ++sp) {
+            const std::vector<int>& idx = s.sec[sp];
+            int n = (int)idx.size();
+            int c = -1;
+            for (int col = 0; col < n; ++col) if (s.occ[idx[col]] == k) c = col;
+            if (c < 0) continue;
+            const std::vector<double>& B = ev.sec[sp].inv;   // B[col * n + row]
+            std::vector<double> beta(n, 0.0);
+            for (int col = 0; col < n; ++col)
+                for (int row = 0; row < n; ++row) beta[col] += B[(size_t)col * n + row] * mo_value(s, dC, k, r[idx[row]]);
+            for (int row = 0; row < n; ++row) {
+                V3 ri = r[idx[row]];
+                double bci = B[(size_t)c * n + row];
+                V3 tg{0, 0, 0};
+                double tl = 0.0;
+                for (int col = 0; col < n; ++col) {
+                    int kc = s.occ[idx[col]];
+                    tg = tg + beta[col] * mo_grad(s, s.C, kc, ri);
+                    tl += beta[col] * mo_lap(s, s.C, kc, ri);
+                }
+                V3 dg = bci * mo_grad(s, dC, k, ri) - bci * tg;
+                double dl = bci * mo_lap(s, dC, k, ri) - bci * tl;
+                acc += dl + 2.0 * dot(dg, ev.J.g[idx[row]]);
+            }
+        }
+        dE[8 + q] = -0.5 * acc;
+    }
+}
+
 // Hellmann-Feynman force (src/systems/methane.rs:1241-1272).
 void hf_force(const Sys& s, const std::vector<V3>& r, double* F) {
     for (int I = 0; I < s.n_nuc; ++I) {
@@ -883,8 +975,12 @@ V3 limit_drift(V3 F, double tau, double max_drift) {   // src/sampling/vmc.rs:30
 // 3 drift-diffusion), with the shared single-draw Philox layout.  With
 // fixed_node a proposal that changes the sign of psi is refused (the
 // reference's IS-DMC, src/sampling/is_dmc.rs:254, accepts it).
+// margin (may be null) receives the smallest relative distance |u - p| / u
+// between an acceptance uniform and its acceptance probability: how close the
+// walker came to the opposite decision.
 int sweep_walker(const Sys& s, const std::vector<int>& order, std::vector<V3>& r, double& lp, int& sg, uint32_t wid,
-                 uint64_t st, int move_kind, double step, double tau, double max_drift, uint64_t seed, int fixed_node) {
+                 uint64_t st, int move_kind, double step, double tau, double max_drift, uint64_t seed, int fixed_node,
+                 double* margin = nullptr) {
     int acc = 0;
     int N = s.N;
     for (int q = 0; q < N; ++q) {
@@ -921,6 +1017,7 @@ int sweep_walker(const Sys& s, const std::vector<int>& order, std::vector<V3>& r
         if (!okn) continue;
         if (fixed_node && sgn != sg) continue;
         double prob = std::exp(2.0 * (lpn - lp) + logG);
+        if (margin) *margin = std::min(*margin, std::fabs(uacc - prob) / uacc);
         if (uacc < prob) {
             if (s.pw) rn[e] = {rn[e].x - s.L * std::floor(rn[e].x / s.L), rn[e].y - s.L * std::floor(rn[e].y / s.L),
                                rn[e].z - s.L * std::floor(rn[e].z / s.L)};
@@ -987,6 +1084,17 @@ int orc_logderiv(const orc_system_desc* d, int W, const double* pos, double* O, 
     return 0;
 }
 
+// dE_L / dp per configuration, [W][8 + n_rot] (el_derivs).
+int orc_el_derivs(const orc_system_desc* d, int W, const double* pos, double* dE, int threads) {
+    Sys s = make_sys(d);
+    int P = 8 + (int)s.rot_occ.size();
+    parallel_for(W, threads, [&](int w) {
+        std::vector<V3> r = load_cfg(pos + (size_t)w * s.N * 3, s.N);
+        el_derivs(s, r, dE + (size_t)w * P);
+    });
+    return 0;
+}
+
 int orc_forces(const orc_system_desc* d, int W, const double* pos, double* F_hf, double* omega, int threads) {
     Sys s = make_sys(d);
     parallel_for(W, threads, [&](int w) {
@@ -1045,9 +1153,11 @@ int orc_init(const orc_system_desc* d, int W, uint32_t walker0, uint64_t seed, d
 // For all-electron moves one "sweep" is one step; step index = sweep0 + t.
 // pos is W x N x 3 in reference order; accepted[w] counts accepted proposals.
 // e_local (optional) receives E_L of the final configuration.
+// margin (may be NULL) receives per walker the smallest relative distance
+// between an acceptance uniform and its acceptance probability over the run.
 int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, int n_sweeps,
                uint64_t sweep0, int move_kind, double step, double tau, double max_drift,
-               uint64_t seed, int* accepted, double* e_local, int threads) {
+               uint64_t seed, int* accepted, double* e_local, double* margin, int threads) {
     Sys s = make_sys(d);
     int N = s.N;
     std::vector<int> order = visit_order(s);
@@ -1057,6 +1167,7 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
         int sg; bool ok;
         double lp = log_psi(s, r, sg, ok);
         int acc = 0;
+        double mg = INFINITY;
         for (int t = 0; t < n_sweeps; ++t) {
             uint64_t st = sweep0 + (uint64_t)t;
             if (move_kind == 0 || move_kind == 1) {
@@ -1077,11 +1188,13 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
                 double lpn = log_psi(s, rn, sgn, okn);
                 double prob = std::exp(2.0 * (lpn - lp));
                 U4 a = draw(seed, wid, st, 0, TAG_ACCEPT);
+                if (okn) mg = std::min(mg, std::fabs(u01(a.v[0]) - prob) / u01(a.v[0]));
                 if (okn && u01(a.v[0]) < prob) { r = rn; lp = lpn; sg = sgn; ++acc; }
                 continue;
             }
-            acc += sweep_walker(s, order, r, lp, sg, wid, st, move_kind, step, tau, max_drift, seed, 0);
+            acc += sweep_walker(s, order, r, lp, sg, wid, st, move_kind, step, tau, max_drift, seed, 0, &mg);
         }
+        if (margin) margin[w] = mg;
         for (int i = 0; i < N; ++i) {
             double* p = pos + ((size_t)w * N + i) * 3;
             p[0] = r[i].x; p[1] = r[i].y; p[2] = r[i].z;

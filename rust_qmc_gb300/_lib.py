@@ -44,7 +44,9 @@ class RunParams(C.Structure):
         ("n_walkers", C.c_int), ("n_steps", C.c_int), ("n_burnin", C.c_int), ("move_kind", C.c_int),
         ("step", C.c_double), ("tau", C.c_double), ("max_drift", C.c_double),
         ("precision", C.c_int), ("refresh_every", C.c_int), ("e_ref_damping", C.c_double),
-        ("fixed_node", C.c_int), ("reference_diffusion", C.c_int), ("reserved", C.c_int * 4),
+        ("fixed_node", C.c_int), ("reference_diffusion", C.c_int),
+        ("target_acceptance", C.c_double), ("adaptation_interval", C.c_int), ("min_step", C.c_double),
+        ("max_step", C.c_double), ("reserved", C.c_int * 4),
     ]
 
 
@@ -61,7 +63,8 @@ class RunResult(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("error", C.c_double), ("autocorrelation_time", C.c_double),
         ("acceptance_rate", C.c_double), ("variance", C.c_double), ("n_samples", C.c_int),
-        ("status_flags", C.c_int), ("avg_population", C.c_double), ("reserved", C.c_double * 4),
+        ("status_flags", C.c_int), ("avg_population", C.c_double), ("final_step", C.c_double),
+        ("reserved", C.c_double * 3),
     ]
 
 
@@ -88,7 +91,7 @@ PROTOTYPES = {
     "qmc_system_set_params": [_vp, _dp, C.c_int],
     "qmc_system_set_nuclei": [_vp, _dp, C.c_int],
     "qmc_eval_batch": [_vp, C.c_int, _dp, C.c_int, _dp, _ip, _dp, _dp, _dp],
-    "qmc_logderiv_batch": [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp],
+    "qmc_logderiv_batch": [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
     "qmc_forces_batch": [_vp, C.c_int, _dp, _dp, _dp],
     "qmc_walkers_create": [_vp, C.c_int, C.c_int, C.POINTER(_vp)],
     "qmc_walkers_destroy": [_vp],

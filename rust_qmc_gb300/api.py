@@ -149,18 +149,27 @@ class System:
                                         _d(out["grad"]), _d(out["lap"]), _d(out["e_local"])), "qmc_eval_batch")
         return out
 
-    def logderiv_batch(self, pos, sums=False):
+    def logderiv_batch(self, pos, sums=False, el_derivs=False):
+        """(O, E_L[, dE_L/dp][, S, f, <E>]) per qmc_logderiv_batch: O [W, P] the
+        log-derivatives, dE_L/dp [W, P] with el_derivs, the SR sums with sums."""
         pos = self._pos(pos)
         W, P = pos.shape[0], self.num_params()
         O, E = np.zeros((W, P)), np.zeros(W)
+        dE = np.zeros((W, P)) if el_derivs else None
         S = np.zeros((P, P)) if sums else None
         f = np.zeros(P) if sums else None
         em = C.c_double()
-        L.check(self.lib.qmc_logderiv_batch(self.h, W, _d(pos), _d(O), _d(E), _d(S), _d(f),
+        L.check(self.lib.qmc_logderiv_batch(self.h, W, _d(pos), _d(O), _d(E), _d(dE), _d(S), _d(f),
                                             C.byref(em) if sums else None), "qmc_logderiv_batch")
+        out = (O, E) + ((dE,) if el_derivs else ())
         if sums:
-            return O, E, S, f, em.value
-        return O, E
+            out += (S, f, em.value)
+        return out
+
+    def local_energy_derivatives(self, r):
+        """d E_L / dp of one configuration (the E_L derivatives behind the SR
+        and force interfaces)."""
+        return self.logderiv_batch(r, el_derivs=True)[2][0]
 
     def ratio_batch(self, pos, e, r_new):
         """psi(moved)/psi for electron e moved to r_new[w] in each configuration,
@@ -410,17 +419,23 @@ def batch_run(ctx, systems, walkers_per_system, *, n_steps, n_burnin=0, move_kin
 
 
 def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_BOX, step=1.0, tau=0.01,
-            max_drift=1.0, precision=L.QMC_FP64, refresh_every=64, seed=1):
-    """MCMCSimulation::run / DriftDiffusionVMC::run on the device."""
+            max_drift=1.0, precision=L.QMC_FP64, refresh_every=64, seed=1, target_acceptance=0.0,
+            adaptation_interval=100, min_step=0.0, max_step=0.0):
+    """MCMCSimulation::run / DriftDiffusionVMC::run on the device; with
+    target_acceptance > 0 the step (or tau) adapts every adaptation_interval
+    steps as the reference's samplers do (src/sampling/vmc.rs:122-128,
+    397-402)."""
     p = L.RunParams()
     p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = n_walkers, n_steps, n_burnin, move_kind
     p.step, p.tau, p.max_drift, p.precision, p.refresh_every = step, tau, max_drift, precision, refresh_every
+    p.target_acceptance, p.adaptation_interval = target_acceptance, adaptation_interval
+    p.min_step, p.max_step = min_step, max_step
     res = L.RunResult()
     energies = np.zeros(n_steps)
     L.check(system.lib.qmc_vmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_vmc_run")
     return dict(energy=res.energy, error=res.error, autocorrelation_time=res.autocorrelation_time,
                 acceptance_rate=res.acceptance_rate, variance=res.variance, n_samples=res.n_samples,
-                status_flags=res.status_flags, energies=energies[:res.n_samples])
+                status_flags=res.status_flags, energies=energies[:res.n_samples], final_step=res.final_step)
 
 
 def _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping, fixed_node,

@@ -235,7 +235,7 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
     if (hs.N == 10 && hs.n_up == 5 && hs.n_nuc == 5 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN)
         hs.shape = layout_matches_ch4min(hs) ? SHAPE_CH4MIN : SHAPE_CH4;
     if (hs.N == 42 && hs.n_up == 21 && hs.n_nuc == 12 && hs.basis == QMC_BASIS_GTO && hs.jk == QMC_JAS_PADE_EEN &&
-        hs.n_ao <= 64)
+        hs.n_ao <= 96)
         hs.shape = SHAPE_C6H6;
     if (hs.shape < 0) return QMC_ERR_UNSUPPORTED;
     return QMC_OK;
@@ -696,8 +696,8 @@ int qmc_ratio_batch(qmc_sys_t s, int W, const double* pos, int e, const double* 
     return QMC_OK;
 }
 
-int qmc_logderiv_batch(qmc_sys_t s, int W, const double* pos, double* O, double* e_local, double* S, double* f,
-                       double* e_mean) {
+int qmc_logderiv_batch(qmc_sys_t s, int W, const double* pos, double* O, double* e_local, double* dEL, double* S,
+                       double* f, double* e_mean) {
     if (!s || W <= 0 || !pos) return QMC_ERR_ARG;
     if (s->hs.jk != QMC_JAS_PADE_EEN) return QMC_ERR_UNSUPPORTED;
     cudaSetDevice(s->ctx->device);
@@ -713,34 +713,49 @@ int qmc_logderiv_batch(qmc_sys_t s, int W, const double* pos, double* O, double*
     // MO-rotation angles would need the determinant and are not compiled
     const bool warp = hs.shape == SHAPE_C6H6;
     if (warp && P != 8) return QMC_ERR_UNSUPPORTED;
+    // device scratch: O [W][P], the SR sums and their block partials, the
+    // Jastrow table (jas[8], nuclei [n_nuc][5]), then with dEL: dEL [W][P] and
+    // grad ln|psi| [W][N][3]
     const size_t base = (size_t)W * P + (size_t)M + 2 * (size_t)M * nblk + 64;
-    const size_t extra = warp ? 8 + 5 * (size_t)hs.n_nuc : 0;   // jas[8] and the nuclei [n_nuc][5]
+    const size_t ntab = 8 + 5 * (size_t)hs.n_nuc;
+    const size_t nd = dEL ? (size_t)W * P + (size_t)W * hs.N * 3 : 0;
     CK(upload_positions(wk, pos));
-    CK(ensure_out(wk, base + extra));
+    CK(ensure_out(wk, base + ntab + nd));
+    double* d_tab = wk->d_out + base;
+    double* d_dEL = dEL ? d_tab + ntab : nullptr;
+    double* d_grad = dEL ? d_dEL + (size_t)W * P : nullptr;
+    std::vector<double> tab(hs.jas, hs.jas + 8);
+    for (int I = 0; I < hs.n_nuc; ++I) {
+        for (int c = 0; c < 3; ++c) tab.push_back(hs.R[3 * I + c]);
+        tab.push_back(hs.Z[I]);
+        tab.push_back((double)hs.species[I]);
+    }
+    if (warp || dEL) CU(cudaMemcpyAsync(d_tab, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice, st));
     MeasureOut mo;
-    std::vector<double> tab;
+    mo.grad = d_grad;
     if (warp) {
-        CK(launch_measure(hs, wk->dw, 0, true, mo, st));          // FP64 refresh: E_L into dw.el
-        tab.assign(hs.jas, hs.jas + 8);
-        for (int I = 0; I < hs.n_nuc; ++I) {
-            for (int c = 0; c < 3; ++c) tab.push_back(hs.R[3 * I + c]);
-            tab.push_back(hs.Z[I]);
-            tab.push_back((double)hs.species[I]);
-        }
-        double* d_tab = wk->d_out + base;
-        CU(cudaMemcpyAsync(d_tab, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice, st));
-        if (launch_jastrow3_logderiv(wk->dw, hs.N, hs.n_up, hs.n_nuc, d_tab + 8, d_tab, P, wk->d_out, st))
+        CK(launch_measure(hs, wk->dw, 0, true, mo, st));          // FP64 refresh: E_L (and grad) on the device
+        if (launch_jastrow3_logderiv(wk->dw, hs.N, hs.n_up, hs.n_nuc, d_tab + 8, d_tab, P, wk->d_out, st, d_grad,
+                                     d_dEL))
             return QMC_ERR_CUDA;
         mo.O = wk->d_out;
     } else {
+        // thread-per-walker shapes: O_p, E_L, grad and the rotation columns of
+        // dE_L/dp in one evaluation; the Jastrow columns of dE_L/dp from the
+        // gradient afterwards
         mo.O = wk->d_out;
+        mo.dEL = d_dEL;
         CK(launch_measure(hs, wk->dw, 0, true, mo, st));
+        if (dEL && launch_jastrow3_logderiv(wk->dw, hs.N, hs.n_up, hs.n_nuc, d_tab + 8, d_tab, P, nullptr, st, d_grad,
+                                            d_dEL))
+            return QMC_ERR_CUDA;
     }
     double* d_sums = wk->d_out + (size_t)W * P;
     double* d_scr = d_sums + M;
     if (S || f || e_mean)
         CK(launch_sr_sums(wk->dw.el, mo.O, W, P, d_sums, d_scr, (int)(2 * (size_t)M * nblk + 64), st));
     if (O) CU(cudaMemcpyAsync(O, mo.O, 8 * (size_t)W * P, cudaMemcpyDeviceToHost, st));
+    if (dEL) CU(cudaMemcpyAsync(dEL, d_dEL, 8 * (size_t)W * P, cudaMemcpyDeviceToHost, st));
     if (e_local) CU(cudaMemcpyAsync(e_local, wk->dw.el, 8 * (size_t)W, cudaMemcpyDeviceToHost, st));
     std::vector<double> sums(M);
     if (S || f || e_mean) CU(cudaMemcpyAsync(sums.data(), d_sums, 8 * (size_t)M, cudaMemcpyDeviceToHost, st));
@@ -943,6 +958,61 @@ int qmc_walkers_status(qmc_walkers_t wk, int* flags) {
     return QMC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Step-size / time-step adaptation of the samplers (no device state: the
+// rule runs on the host between launches, from the device's acceptance count).
+//  MCMCSimulation::adapt_step_size (src/sampling/vmc.rs:122-128):
+//    step <- clamp(step * sqrt(rate / target), min, max)
+//  DriftDiffusionVMC::adapt_time_step (src/sampling/vmc.rs:397-402):
+//    tau <- clamp(tau * clamp(sqrt(rate / target), 0.8, 1.2), 0.001, 0.05)
+// applied every adaptation_interval steps (sweeps) over the acceptance of
+// that window, through burn-in and production alike (vmc.rs:85-88, 423-428,
+// 458-463).  Single-electron Gaussian moves (no reference sampler) adapt their
+// width by the MCMC rule.
+struct Adapt {
+    bool on = false;
+    int interval = 0;
+    double target = 0.0, lo = 0.0, hi = 0.0;
+    bool drift = false;
+    unsigned long long acc0 = 0;           // device acceptance count at the window start
+    double value = 0.0;                    // current step or tau
+    int init(const qmc_run_params* p, bool is_drift, double start) {
+        value = start;
+        drift = is_drift;
+        if (!(p->target_acceptance > 0)) return QMC_OK;
+        if (p->target_acceptance >= 1.0 || p->adaptation_interval <= 0) return QMC_ERR_ARG;
+        on = true;
+        interval = p->adaptation_interval;
+        target = p->target_acceptance;
+        lo = p->min_step > 0 ? p->min_step : (drift ? 0.001 : 0.0);
+        hi = p->max_step > 0 ? p->max_step : (drift ? 0.05 : INFINITY);
+        if (!(lo <= hi) || !(value > 0)) return QMC_ERR_ARG;
+        return QMC_OK;
+    }
+    // new window: acceptance count acc after `moves` proposals since acc0
+    void update(unsigned long long acc, double moves) {
+        const double rate = moves > 0 ? (double)(acc - acc0) / moves : 0.0;
+        double f = std::sqrt(rate / target);
+        if (drift) f = std::min(1.2, std::max(0.8, f));
+        value = std::min(hi, std::max(lo, value * f));
+        acc0 = acc;
+    }
+};
+
+int read_acc(qmc_walkers_s* wk, unsigned long long* acc) {
+    cudaStream_t st = wk->sys->ctx->stream;
+    CU(cudaMemcpyAsync(acc, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return QMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_result* res, double* energies) {
     if (!s || !p || !res) return QMC_ERR_ARG;
     if (p->n_walkers <= 0 || p->n_steps <= 0 || p->n_burnin < 0 || p->move_kind < 0 || p->move_kind > 3) return QMC_ERR_ARG;
@@ -953,54 +1023,93 @@ int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     CK(alloc_walkers(s, p->n_walkers, p->precision, &wk));
     struct Guard { qmc_walkers_s* w; ~Guard() { if (w) { cudaStreamSynchronize(w->sys->ctx->stream); free_walkers(w); } } } guard{wk};
     const HostSys& hs = s->hs;
+    const bool drift = p->move_kind == QMC_MOVE_ONE_DRIFT;
+    Adapt ad;
+    CK(ad.init(p, drift, drift ? p->tau : p->step));
     CK(launch_init(hs, wk->dw, seed, st));
     MeasureOut none;
     CK(launch_measure(hs, wk->dw, 0, true, none, st));
     std::vector<double> series;
     long long proposals = 0;
+    unsigned long long acc_prod0 = 0;      // acceptance count when production starts
     CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+    const double W = (double)wk->dw.W;
     if (p->move_kind == QMC_MOVE_ALL_GAUSS || p->move_kind == QMC_MOVE_ALL_BOX) {
         if (!(p->step > 0)) return QMC_ERR_ARG;
-        if (p->n_burnin) CK(launch_sweep(hs, wk->dw, p->move_kind, p->n_burnin, 0, p->step, 0, 0, seed, st));
-        CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
+        const int total = p->n_burnin + p->n_steps;
         int nblk = (wk->dw.W + 63) / 64;
         double* d_part = nullptr;
         double* d_mean = nullptr;
         CU(cudaMalloc((void**)&d_part, 16 * (size_t)nblk * p->n_steps));
         cudaError_t e = cudaMalloc((void**)&d_mean, 8 * (size_t)p->n_steps);
         if (e != cudaSuccess) { cudaFree(d_part); return cuda_rc(e); }
-        int rc = launch_step_all_recorded(hs, wk->dw, p->move_kind, p->n_steps, (uint64_t)p->n_burnin, p->step, seed, d_part, st);
-        if (!rc) rc = launch_sum_partials(d_part, nblk, p->n_steps, d_mean, st);
+        struct Bufs { double* a; double* b; ~Bufs() { cudaFree(a); cudaFree(b); } } bufs{d_part, d_mean};
+        // steps t = 0 .. total-1 in launches that end at adaptation points and
+        // at the end of the burn-in; production steps record their mean E_L
+        int t = 0;
+        while (t < total) {
+            int end = total;
+            if (t < p->n_burnin) end = std::min(end, p->n_burnin);
+            if (ad.on) end = std::min(end, (t / ad.interval + 1) * ad.interval);
+            const int n = end - t;
+            if (t >= p->n_burnin)
+                CK(launch_step_all_recorded(hs, wk->dw, p->move_kind, n, (uint64_t)t, ad.value, seed,
+                                            d_part + 2 * (size_t)nblk * (t - p->n_burnin), st));
+            else
+                CK(launch_sweep(hs, wk->dw, p->move_kind, n, (uint64_t)t, ad.value, 0, 0, seed, st));
+            t = end;
+            if (t == p->n_burnin) CK(read_acc(wk, &acc_prod0));
+            if (ad.on && t % ad.interval == 0) {
+                unsigned long long acc;
+                CK(read_acc(wk, &acc));
+                ad.update(acc, (double)ad.interval * W);
+            }
+        }
+        CK(launch_sum_partials(d_part, nblk, p->n_steps, d_mean, st));
         series.resize(p->n_steps);
-        if (!rc) rc = cuda_rc(cudaMemcpyAsync(series.data(), d_mean, 8 * (size_t)p->n_steps, cudaMemcpyDeviceToHost, st));
-        if (!rc) rc = cuda_rc(cudaStreamSynchronize(st));
-        cudaFree(d_part);
-        cudaFree(d_mean);
-        if (rc) return rc;
-        for (double& v : series) v /= (double)wk->dw.W;
+        CU(cudaMemcpyAsync(series.data(), d_mean, 8 * (size_t)p->n_steps, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        for (double& v : series) v /= W;
         proposals = (long long)p->n_steps * wk->dw.W;
     } else {
-        int every = p->refresh_every > 0 ? p->refresh_every : 1;
-        uint64_t sweep = 0;
-        for (int done = 0; done < p->n_burnin; done += every) {
-            int n = std::min(every, p->n_burnin - done);
-            CK(launch_sweep(hs, wk->dw, p->move_kind, n, sweep, p->step, p->tau, p->max_drift, seed, st));
-            sweep += n;
-            CK(launch_measure(hs, wk->dw, 0, true, none, st));
-        }
-        CU(cudaMemsetAsync(wk->dw.acc, 0, 8, st));
-        for (int done = 0; done < p->n_steps; done += every) {
-            int n = std::min(every, p->n_steps - done);
-            CK(launch_sweep(hs, wk->dw, p->move_kind, n, sweep, p->step, p->tau, p->max_drift, seed, st));
-            sweep += n;
-            CK(launch_measure(hs, wk->dw, 0, true, none, st));
-            double esum = 0.0;
-            CU(cudaMemcpyAsync(&esum, wk->dw.partial + wk->dw.partial_cap - 1, 8, cudaMemcpyDeviceToHost, st));
-            CU(cudaStreamSynchronize(st));
-            series.push_back(esum / (double)wk->dw.W);
-            proposals += (long long)n * hs.N * wk->dw.W;
+        // single-electron sweeps: the refresh (inverse, log|psi|, E_L) every
+        // refresh_every sweeps of the burn-in and of the production, one
+        // energy measurement per production refresh; launches also end at
+        // adaptation points
+        const int every = p->refresh_every > 0 ? p->refresh_every : 1;
+        const int total = p->n_burnin + p->n_steps;
+        int t = 0, since_refresh = 0;
+        while (t < total) {
+            int end = total;
+            if (t < p->n_burnin) end = std::min(end, p->n_burnin);
+            end = std::min(end, t + (every - since_refresh));
+            if (ad.on) end = std::min(end, (t / ad.interval + 1) * ad.interval);
+            const int n = end - t;
+            const double stp = drift ? p->step : ad.value, tau = drift ? ad.value : p->tau;
+            CK(launch_sweep(hs, wk->dw, p->move_kind, n, (uint64_t)t, stp, tau, p->max_drift, seed, st));
+            if (t >= p->n_burnin) proposals += (long long)n * hs.N * wk->dw.W;
+            t = end;
+            since_refresh += n;
+            const bool burn_end = t == p->n_burnin;
+            if (since_refresh == every || burn_end || t == total) {
+                CK(launch_measure(hs, wk->dw, 0, true, none, st));
+                if (t > p->n_burnin || (t == p->n_burnin && p->n_burnin == 0)) {
+                    double esum = 0.0;
+                    CU(cudaMemcpyAsync(&esum, wk->dw.partial + wk->dw.partial_cap - 1, 8, cudaMemcpyDeviceToHost, st));
+                    CU(cudaStreamSynchronize(st));
+                    series.push_back(esum / W);
+                }
+                since_refresh = 0;
+            }
+            if (burn_end) CK(read_acc(wk, &acc_prod0));
+            if (ad.on && t % ad.interval == 0) {
+                unsigned long long acc;
+                CK(read_acc(wk, &acc));
+                ad.update(acc, (double)ad.interval * hs.N * W);
+            }
         }
     }
+    res->final_step = ad.value;
     unsigned long long acc = 0;
     int flags = 0;
     CU(cudaMemcpyAsync(&acc, wk->dw.acc, 8, cudaMemcpyDeviceToHost, st));
@@ -1015,7 +1124,7 @@ int qmc_vmc_run(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc_run_res
     res->variance = series.size() ? var / (double)series.size() : 0.0;
     res->autocorrelation_time = autocorrelation_time(series);
     res->error = blocking_error(series, res->autocorrelation_time);
-    res->acceptance_rate = proposals ? (double)acc / (double)proposals : 0.0;
+    res->acceptance_rate = proposals ? (double)(acc - acc_prod0) / (double)proposals : 0.0;
     res->n_samples = (int)series.size();
     res->status_flags = flags;
     if (energies) for (size_t i = 0; i < series.size(); ++i) energies[i] = series[i];
@@ -1624,6 +1733,8 @@ int qmc_batch_run(qmc_ctx_t ctx, int n_sys, const qmc_sys_t* systems, const int*
     if (p->move_kind == QMC_MOVE_ONE_DRIFT && !(p->tau > 0 && p->max_drift > 0)) return QMC_ERR_ARG;
     if (p->move_kind == QMC_MOVE_ONE_GAUSS && !(p->step > 0)) return QMC_ERR_ARG;
     if (p->precision != QMC_FP64 && p->precision != QMC_FP32_REFINE) return QMC_ERR_ARG;
+    // one captured graph replays a fixed step for every system: no per-system adaptation
+    if (p->target_acceptance > 0) return QMC_ERR_UNSUPPORTED;
     for (int i = 0; i < n_sys; ++i)
         if (!systems[i] || systems[i]->released || systems[i]->ctx != ctx || W[i] <= 0) return QMC_ERR_ARG;
     std::memset(per_sys, 0, sizeof(qmc_run_result) * n_sys);

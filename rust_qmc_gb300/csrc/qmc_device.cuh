@@ -224,11 +224,15 @@ __device__ __forceinline__ float gauss_prim(const SysT<SH, float>& S, int p, flo
     return ex2_approx(S.pexp2[p] * r2);
 }
 
+// MODE 3 adds the gradients and Laplacians of the NR rotation rows (the
+// parameter derivatives of the local energy need them).
 template <class SH, class T, int SIG, int MODE, int NR>
 struct MOEval {
     static constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
+    static constexpr int NRD = (MODE >= 3 && NR > 0) ? NR : 1;
     T v[SH::NMAX], gx[SH::NMAX], gy[SH::NMAX], gz[SH::NMAX], l[SH::NMAX];
     T dv[NR > 0 ? NR : 1];
+    T dgx[NRD], dgy[NRD], dgz[NRD], dl[NRD];
 
     __device__ __forceinline__ void add(const SysT<SH, T>& S, int a, T chi, T ax, T ay, T az, T la) {
 #pragma unroll
@@ -239,7 +243,11 @@ struct MOEval {
             if (MODE >= 2) l[k] += c * la;
         }
 #pragma unroll
-        for (int q = 0; q < NR; ++q) dv[q] += S.dC[q][a] * chi;
+        for (int q = 0; q < NR; ++q) {
+            const T c = S.dC[q][a];
+            dv[q] += c * chi;
+            if (MODE >= 3) { dgx[q] += c * ax; dgy[q] += c * ay; dgz[q] += c * az; dl[q] += c * la; }
+        }
     }
 
     // GTO shell: accumulate one shell's s AO (index a) and optional p triplet.
@@ -260,6 +268,8 @@ struct MOEval {
         for (int k = 0; k < SH::NMAX; ++k) { v[k] = 0; gx[k] = 0; gy[k] = 0; gz[k] = 0; l[k] = 0; }
 #pragma unroll
         for (int q = 0; q < (NR > 0 ? NR : 1); ++q) dv[q] = 0;
+#pragma unroll
+        for (int q = 0; q < NRD; ++q) { dgx[q] = 0; dgy[q] = 0; dgz[q] = 0; dl[q] = 0; }
         if constexpr (!std::is_void<typename SH::Layout>::value) {
             using LY = typename SH::Layout;
 #pragma unroll

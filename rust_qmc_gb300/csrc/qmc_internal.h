@@ -95,6 +95,7 @@ struct MeasureOut {
     double* O = nullptr;                 // [W][P]
     double* fhf = nullptr;               // [W][n_nuc][3]
     double* omega = nullptr;             // [W][n_nuc][3]
+    double* dEL = nullptr;               // [W][P] d E_L / dp: rotation columns 8.. (with O)
     // only the inverse, sign and log|psi| are wanted (E_L may be skipped)
     bool inverse_only = false;
 };
@@ -127,10 +128,14 @@ int launch_flush(void* buf, size_t bytes, cudaStream_t st);
 // scratch holds hf_force_scratch_doubles(W, n_nuc) doubles.
 size_t hf_force_scratch_doubles(int W, int n_nuc);
 int launch_sum_partials(const double* partial, int nblk, int nrows, double* out, cudaStream_t st);
-// Jastrow3 parameter log-derivatives d_O [W][P] (columns 0..7) from the
-// walkers' positions; d_par = jas[8], d_nuc = [n_nuc][5] (x, y, z, Z, species).
+// Jastrow3 parameter log-derivatives d_O [W][P] (columns 0..7; skipped when
+// null) from the walkers' positions; d_par = jas[8], d_nuc = [n_nuc][5]
+// (x, y, z, Z, species 0 or 1 -- two species only, as build_hostsys
+// enforces).  With d_grad ([W][N][3] grad ln|psi|, internal order) also the
+// Jastrow-parameter derivatives of E_L into d_dEL [W][P] (columns 0..7).
 int launch_jastrow3_logderiv(const DevWalkers& dw, int N, int n_up, int n_nuc, const double* d_nuc,
-                             const double* d_par, int P, double* d_O, cudaStream_t st);
+                             const double* d_par, int P, double* d_O, cudaStream_t st,
+                             const double* d_grad = nullptr, double* d_dEL = nullptr);
 // Per-walker Hellmann-Feynman forces d_out [W][n_nuc][3] (electron order is
 // irrelevant: the force sums over all electrons).
 int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_out,

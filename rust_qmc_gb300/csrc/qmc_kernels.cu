@@ -311,32 +311,47 @@ int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double
 
 // Jastrow3 parameter log-derivatives, one thread per walker, for the shapes
 // whose evaluation kernels carry no O_p outputs (qmc_jastrow3_logderiv.h):
-// O[w][0..7] with row stride P; par = p[8], nuc = [n_nuc][5].
+// O[w][0..7] with row stride P (skipped when O is null); par = p[8],
+// nuc = [n_nuc][5] (x, y, z, Z, species 0 or 1: the host rejects other
+// species when it builds a system).  With grad ([W][N][3], grad_i ln|psi| in
+// the internal electron order) the Jastrow-parameter derivatives of the
+// local energy go to dEL[w][0..7], same stride.
 template <class TS>
 __global__ void k_jastrow3_logderiv(const TS* __restrict__ pos, int W, int Wcap, int N, int n_up, int n_nuc,
                                     const double* __restrict__ nuc, const double* __restrict__ par, int P,
-                                    double* __restrict__ O) {
+                                    double* __restrict__ O, const double* __restrict__ grad,
+                                    double* __restrict__ dEL) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
     auto at = [&](int i, int c) { return (double)pos[(size_t)(3 * i + c) * Wcap + w]; };
     double o[8];
-    jastrow3_log_derivatives(N, n_up, n_nuc, nuc, par, at, o);
+    if (O) {
+        jastrow3_log_derivatives(N, n_up, n_nuc, nuc, par, at, o);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) O[(size_t)w * P + k] = o[k];
+        for (int k = 0; k < 8; ++k) O[(size_t)w * P + k] = o[k];
+    }
+    if (grad && dEL) {
+        const double* g = grad + (size_t)w * N * 3;
+        auto gr = [&](int i, int c) { return g[3 * i + c]; };
+        jastrow3_el_derivatives(N, n_up, n_nuc, nuc, par, at, gr, o);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dEL[(size_t)w * P + k] = o[k];
+    }
 }
 
 int launch_jastrow3_logderiv(const DevWalkers& dw, int N, int n_up, int n_nuc, const double* d_nuc,
-                             const double* d_par, int P, double* d_O, cudaStream_t st) {
+                             const double* d_par, int P, double* d_O, cudaStream_t st, const double* d_grad,
+                             double* d_dEL) {
     if (dw.W <= 0) return 0;
     if (P < 8) return 1;
     const int tpb = 128;
     const int nb = (dw.W + tpb - 1) / tpb;
     if (dw.prec == 0)
         k_jastrow3_logderiv<double><<<nb, tpb, 0, st>>>((const double*)dw.pos, dw.W, dw.Wcap, N, n_up, n_nuc, d_nuc,
-                                                        d_par, P, d_O);
+                                                        d_par, P, d_O, d_grad, d_dEL);
     else
         k_jastrow3_logderiv<float><<<nb, tpb, 0, st>>>((const float*)dw.pos, dw.W, dw.Wcap, N, n_up, n_nuc, d_nuc,
-                                                       d_par, P, d_O);
+                                                       d_par, P, d_O, d_grad, d_dEL);
     ++g_launch_count;
     return cuda_status(cudaGetLastError());
 }

@@ -1,5 +1,5 @@
 // qmc_shape_c6h6.cu -- warp-per-walker kernels for the benzene shape
-// (42 electrons, 21 + 21, 12 nuclei, up to 64 Gaussian AOs, Jastrow3 form).
+// (42 electrons, 21 + 21, 12 nuclei, up to 96 Gaussian AOs, Jastrow3 form).
 #include "qmc_warp_kernels.cuh"
 
 namespace qmc {

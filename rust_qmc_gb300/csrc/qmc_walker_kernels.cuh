@@ -337,27 +337,46 @@ struct FullEval {
     TC el;
     TC gx[SH::NE], gy[SH::NE], gz[SH::NE], lap[SH::NE];   // grad psi/psi, lap psi/psi
     TC O[8 + (NR > 0 ? NR : 1)];
+    TC dE[NR > 0 ? NR : 1];                               // d E_L / d theta_q (DEL evaluations)
 };
 
-template <class SH, class TC, int SIG, int NR, class DinvStore>
+// One spin sector.  With DEL (and NR > 0) it also accumulates into dErot the
+// rotation-angle derivatives of the local energy: for column c of the sector
+// rotated by theta_q, with B = A^-1, beta = B (d phi_c / d theta)(r_.),
+//   d (X B)_ii = X_psi(r_i) B_ci - B_ci sum_k X_k(r_i) beta_k   (X = grad, lap),
+//   d E_L / d theta_q += -1/2 sum_i [ d (L B)_ii + 2 d (G B)_ii . j_i ],
+// j_i the Jastrow gradient of electron i (gjx, gjy, gjz).
+template <class SH, class TC, int SIG, int NR, class DinvStore, bool DEL = false>
 __device__ __forceinline__ void eval_sector(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3], double& logdet,
                                             int& sg, bool& ok, TC (&gdx)[SH::NE], TC (&gdy)[SH::NE],
                                             TC (&gdz)[SH::NE], TC (&ld)[SH::NE], TC* Orot,
-                                            DinvStore store, TC* omega) {
+                                            DinvStore store, TC* omega, const TC* gjx = nullptr,
+                                            const TC* gjy = nullptr, const TC* gjz = nullptr,
+                                            TC* dErot = nullptr) {
     constexpr int NS = SIG == 0 ? SH::NUP : SH::NDN;
     if (NS == 0) return;
     constexpr int NSa = NS > 0 ? NS : 1;
+    constexpr bool WD = DEL && NR > 0;
+    constexpr int NRa = NR > 0 ? NR : 1;
+    constexpr int NRD = WD ? NRa : 1;
     TC D[NSa][NSa], Gx[NSa][NSa], Gy[NSa][NSa], Gz[NSa][NSa], L[NSa][NSa];
-    TC dvr[NSa][NR > 0 ? NR : 1];
+    TC dvr[NSa][NRa];
+    TC dgxr[NSa][NRD], dgyr[NSa][NRD], dgzr[NSa][NRD], dlr[NSa][NRD];
 #pragma unroll 1
     for (int q = 0; q < NS; ++q) {
         const int e = SIG * SH::NUP + q;
-        MOEval<SH, TC, SIG, 2, NR> m;
+        MOEval<SH, TC, SIG, WD ? 3 : 2, NR> m;
         m.run(S, r[e][0], r[e][1], r[e][2]);
 #pragma unroll
         for (int k = 0; k < NS; ++k) { D[q][k] = m.v[k]; Gx[q][k] = m.gx[k]; Gy[q][k] = m.gy[k]; Gz[q][k] = m.gz[k]; L[q][k] = m.l[k]; }
 #pragma unroll
         for (int qq = 0; qq < NR; ++qq) dvr[q][qq] = m.dv[qq];
+        if constexpr (WD) {
+#pragma unroll
+            for (int qq = 0; qq < NR; ++qq) {
+                dgxr[q][qq] = m.dgx[qq]; dgyr[q][qq] = m.dgy[qq]; dgzr[q][qq] = m.dgz[qq]; dlr[q][qq] = m.dl[qq];
+            }
+        }
     }
     TC Di[NSa][NSa];
     double lg;
@@ -393,6 +412,40 @@ __device__ __forceinline__ void eval_sector(const SysT<SH, TC>& S, const TC (&r)
                 for (int row = 0; row < NS; ++row) acc += Di[cc][row] * dvr[row][qq];
             }
             Orot[qq] += acc;
+        }
+    }
+    if constexpr (WD) {
+#pragma unroll 1
+        for (int qq = 0; qq < NR; ++qq) {
+            if (qq >= S.n_rot) continue;
+            const int c = S.rot_col[qq][SIG];
+            if (c < 0) continue;
+            TC beta[NSa];
+#pragma unroll
+            for (int col = 0; col < NS; ++col) {
+                TC b = 0;
+#pragma unroll
+                for (int row = 0; row < NS; ++row) b += Di[col][row] * dvr[row][qq];
+                beta[col] = b;
+            }
+            TC acc = 0;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                const int e = SIG * SH::NUP + q;
+                TC bci = 0;
+#pragma unroll
+                for (int cc = 0; cc < NS; ++cc) bci = (cc == c) ? Di[cc][q] : bci;
+                TC tx = 0, ty = 0, tz = 0, tl = 0;
+#pragma unroll
+                for (int col = 0; col < NS; ++col) {
+                    tx += Gx[q][col] * beta[col]; ty += Gy[q][col] * beta[col];
+                    tz += Gz[q][col] * beta[col]; tl += L[q][col] * beta[col];
+                }
+                const TC dgx = bci * (dgxr[q][qq] - tx), dgy = bci * (dgyr[q][qq] - ty);
+                const TC dgz = bci * (dgzr[q][qq] - tz), dl = bci * (dlr[q][qq] - tl);
+                acc += dl + 2 * (dgx * gjx[e] + dgy * gjy[e] + dgz * gjz[e]);
+            }
+            dErot[qq] += TC(-0.5) * acc;
         }
     }
     if (omega) {
@@ -481,7 +534,7 @@ __device__ __forceinline__ TC jastrow_coulomb(const SysT<SH, TC>& S, const TC (&
     return u;
 }
 
-template <class SH, class TC, int NR, class DinvStore>
+template <class SH, class TC, int NR, class DinvStore, bool DEL = false>
 __device__ __forceinline__ void evaluate_config(const SysT<SH, TC>& S, const TC (&r)[SH::NE][3],
                                                 FullEval<SH, TC, NR>& out, bool want_o, DinvStore store,
                                                 TC* omega) {
@@ -495,8 +548,12 @@ __device__ __forceinline__ void evaluate_config(const SysT<SH, TC>& S, const TC 
     double logdet = 0.0;
     int sg = 1;
     bool ok = true;
-    eval_sector<SH, TC, 0, NR>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega);
-    eval_sector<SH, TC, 1, NR>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega);
+#pragma unroll
+    for (int q = 0; q < (NR > 0 ? NR : 1); ++q) out.dE[q] = 0;
+    eval_sector<SH, TC, 0, NR, DinvStore, DEL>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega, gjx,
+                                              gjy, gjz, out.dE);
+    eval_sector<SH, TC, 1, NR, DinvStore, DEL>(S, r, logdet, sg, ok, gdx, gdy, gdz, ld, out.O + 8, store, omega, gjx,
+                                              gjy, gjz, out.dE);
     TC kin = 0;
 #pragma unroll
     for (int e = 0; e < SH::NE; ++e) {
@@ -538,7 +595,7 @@ __global__ void k_init(const __grid_constant__ SysT<SH, double> S, TS* __restric
 // Full evaluation of walker w (refresh of the inverse, log|psi|, E_L and the
 // requested extras); returns E_L (0 for an inactive lane, which still runs the
 // arithmetic on a dummy configuration so that the block stays converged).
-template <class SH, class TC, class TS, int NR>
+template <class SH, class TC, class TS, int NR, bool DEL = false>
 __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS* __restrict__ pos,
                                                  TS* __restrict__ dinv, double* __restrict__ logabs,
                                                  int* __restrict__ sign, double* __restrict__ el, int w, bool act,
@@ -557,7 +614,8 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
 #pragma unroll
     for (int i = 0; i < 3 * SH::NNUC; ++i) omega[i] = 0;
     FullEval<SH, TC, NR> ev;
-    evaluate_config<SH, TC, NR>(S, r, ev, out.O != nullptr, store, (act && out.omega) ? omega : (TC*)nullptr);
+    evaluate_config<SH, TC, NR, decltype(store), DEL>(S, r, ev, out.O != nullptr, store,
+                                                      (act && out.omega) ? omega : (TC*)nullptr);
     double e_l = (double)ev.el;
     if (act) {
         int fl = 0;
@@ -579,6 +637,10 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
         }
         if (out.O) {
             for (int p = 0; p < P; ++p) out.O[(size_t)w * P + p] = (double)ev.O[p];
+        }
+        if (DEL && out.dEL) {
+            // rotation columns; the Jastrow columns 0..7 come from k_jastrow3_logderiv
+            for (int p = 8; p < P; ++p) out.dEL[(size_t)w * P + p] = (double)ev.dE[p - 8];
         }
         if (out.fhf) {
 #pragma unroll
@@ -623,15 +685,15 @@ __device__ __forceinline__ double measure_walker(const SysT<SH, TC>& S, const TS
     return act ? e_l : 0.0;
 }
 
-template <class SH, class TC, class TS, int TPB, int NR>
+template <class SH, class TC, class TS, int TPB, int NR, bool DEL = false>
 __global__ void __launch_bounds__(TPB) k_measure(const __grid_constant__ SysT<SH, TC> S,
                                                  const TS* __restrict__ pos, TS* __restrict__ dinv,
                                                  double* __restrict__ logabs, int* __restrict__ sign,
                                                  double* __restrict__ el, int W, int Wcap, int write_state,
                                                  MeasureOut out, int P, double* partial, int* flags) {
     const int w = blockIdx.x * TPB + threadIdx.x;
-    double e_l = measure_walker<SH, TC, TS, NR>(S, pos, dinv, logabs, sign, el, w, w < W, Wcap, write_state, out, P,
-                                                flags);
+    double e_l = measure_walker<SH, TC, TS, NR, DEL>(S, pos, dinv, logabs, sign, el, w, w < W, Wcap, write_state,
+                                                     out, P, flags);
     if (partial) block_partial<TPB>(e_l, partial, blockIdx.x);
 }
 
@@ -1340,7 +1402,7 @@ struct ShapeOps {
         return cuda_status(cudaGetLastError());
     }
 
-    template <class TC, class TS, int NR>
+    template <class TC, class TS, int NR, bool DEL = false>
     static int measure2(const HostSys& hs, DevWalkers& dw, bool write_state, const MeasureOut& out, cudaStream_t st) {
         SysT<SH, TC> S;
         if (!fill_sys(hs, S)) return 7;
@@ -1348,7 +1410,7 @@ struct ShapeOps {
         int nb = (dw.W + TPB - 1) / TPB;
         double* partial = nullptr;
         if (write_state && dw.partial && dw.partial_cap >= 2 * nb + 1) partial = dw.partial;
-        k_measure<SH, TC, TS, TPB, NR><<<nb, TPB, 0, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign,
+        k_measure<SH, TC, TS, TPB, NR, DEL><<<nb, TPB, 0, st>>>(S, (const TS*)dw.pos, (TS*)dw.dinv, dw.logabs, dw.sign,
                                                             dw.el, dw.W, dw.Wcap, write_state ? 1 : 0, out,
                                                             hs.n_params(), partial, dw.flags);
         ++g_launch_count;
@@ -1383,6 +1445,7 @@ struct ShapeOps {
     static int measure(const HostSys& hs, DevWalkers& dw, int cp, bool ws, const MeasureOut& out, cudaStream_t st) {
         if (out.O) {
             if (SH::JAS != JAS_PADE_EEN || cp != 0 || dw.prec != 0) return 7;
+            if (out.dEL) return measure2<double, double, SH::NROT, true>(hs, dw, ws, out, st);
             return measure2<double, double, SH::NROT>(hs, dw, ws, out, st);
         }
         if (cp == 0) {

@@ -18,7 +18,9 @@
 
 namespace qmc {
 
-constexpr int WMAX_AO = 64;       // two rounds of 32 AOs
+constexpr int WMAX_AO = 96;       // up to three rounds of 32 AOs (BenzeneGTO's 6-31G basis has 66)
+constexpr int WAO_ROUNDS = WMAX_AO / 32;
+constexpr int WNCOL = 24;         // Slater columns held per sector (lanes >= WNCOL read no coefficients)
 constexpr int WMAX_PRIM = 256;
 constexpr int WMAX_NUC = 16;
 
@@ -33,7 +35,7 @@ struct SysW {
     T Z[WMAX_NUC], enA[WMAX_NUC], enB[WMAX_NUC];
     int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];   // type 0 s, 1..3 p_x..p_z
     T pexp[WMAX_PRIM], pcoef[WMAX_PRIM];
-    T C[2][WMAX_AO][32];        // [sector][AO][column]
+    T C[2][WMAX_AO][WNCOL];     // [sector][AO][column]
     T init_sigma;
     int init_nuc[64];           // internal electron order
     int perm[64];
@@ -43,6 +45,7 @@ template <class T>
 static bool fill_sysw(const HostSys& hs, int NE, int NUP, int NNUC, SysW<T>& S) {
     std::memset(&S, 0, sizeof(S));
     if (hs.N != NE || hs.n_up != NUP || hs.n_nuc != NNUC || hs.n_ao > WMAX_AO || NNUC > WMAX_NUC) return false;
+    if (NUP > WNCOL || NE - NUP > WNCOL) return false;
     if (hs.basis != BASIS_GTO) return false;
     S.n_ao = hs.n_ao;
     S.quirk_lap = (hs.quirks & 2) ? 1 : 0;
@@ -112,21 +115,22 @@ __device__ __forceinline__ void load_sysw(SysW<T>* dst, const SysW<T>* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Lane-parallel AO evaluation: lane l evaluates AO l (round 0) and AO l+32
-// (round 1) at point (x,y,z): value, gradient, Laplacian (MODE >= 1 / 2).
+// Lane-parallel AO evaluation: lane l evaluates AO l + 32 r in round r at
+// point (x,y,z): value, gradient, Laplacian (MODE >= 1 / 2).  Rounds past the
+// basis are skipped (a warp-uniform branch).
 // ---------------------------------------------------------------------------
 template <class T, int MODE>
 struct AOLane {
-    T v[2], gx[2], gy[2], gz[2], l[2];
+    T v[WAO_ROUNDS], gx[WAO_ROUNDS], gy[WAO_ROUNDS], gz[WAO_ROUNDS], l[WAO_ROUNDS];
 };
 
 template <class T, int MODE>
 __device__ __forceinline__ void ao_lane(const SysW<T>& S, T x, T y, T z, int lane, AOLane<T, MODE>& o) {
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < WAO_ROUNDS; ++r) {
         const int a = lane + 32 * r;
         T v = 0, gxx = 0, gyy = 0, gzz = 0, lp = 0;
-        if (a < S.n_ao) {
+        if (32 * r < S.n_ao && a < S.n_ao) {
             const int I = S.ao_nuc[a], type = S.ao_type[a], p0 = S.ao_p0[a], np = S.ao_np[a];
             T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
             T r2 = dx * dx + dy * dy + dz * dz;
@@ -170,18 +174,22 @@ __device__ __forceinline__ T wsum(T v) {
 }
 
 // MO contraction: lane k receives phi_k = sum_a C[sig][a][k] chi_a (and
-// gradient / Laplacian), chi_a broadcast from lane a % 32.
+// gradient / Laplacian), chi_a broadcast from lane a % 32; lanes past the
+// table's columns accumulate zeros.
 template <class T, int MODE>
 __device__ __forceinline__ void mo_lane(const SysW<T>& S, int sig, int lane, const AOLane<T, MODE>& ao, T& v, T& gx,
                                         T& gy, T& gz, T& l) {
     v = 0; gx = 0; gy = 0; gz = 0; l = 0;
+    const bool own = lane < WNCOL;
+    const int col = own ? lane : 0;
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < WAO_ROUNDS; ++r) {
         const int base = 32 * r;
         if (base >= S.n_ao) break;
         const int cnt = min(32, S.n_ao - base);
         for (int t = 0; t < cnt; ++t) {
-            T c = S.C[sig][base + t][lane];
+            const T cl = S.C[sig][base + t][col];
+            const T c = own ? cl : T(0);
             if (MODE != 3) v += c * wshfl(ao.v[r], t);
             if (MODE >= 1) {
                 gx += c * wshfl(ao.gx[r], t);

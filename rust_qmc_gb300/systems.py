@@ -12,6 +12,8 @@ Builders:
                          (65 536-walker single-electron workload)
   * ``benzene_minimal``  planar C6H6, 42 electrons, 36 contracted Gaussians,
                          seeded QR-orthonormal MOs (16 384-walker VMC/DMC workload)
+  * ``benzene_gto``      BenzeneGTO: 6-31G (66 AOs), the hand-built MO table,
+                         src/systems/benzene.rs:48-470
   * ``electron_gas``     periodic homogeneous electron gas, src/systems/heg.rs
 """
 import ctypes as C
@@ -371,6 +373,76 @@ def benzene_minimal(seed=SEED_BASE + 4, b_ee=1.5, b_en=2.0, cc=2.64, ch=2.05):
         name="C6H6-min", spins=[1] * 21 + [-1] * 21, nuc_pos=R, nuc_charge=[6.0] * 6 + [1.0] * 6,
         nuc_species=[0] * 6 + [1] * 6, basis_kind=L.QMC_BASIS_GTO, ao_nuc=ao_nuc, ao_l=ao_l, ao_m=ao_m,
         ao_prims=prims, mo_coef=Q.T.copy(), occ=list(range(21)) * 2, jastrow_kind=L.QMC_JAS_PADE_EEN,
+        jas=jastrow3_params(b_ee, b_en), init_nuc=init, init_sigma=0.5)
+
+
+def _benzene_631g_mos(R):
+    """The 21 occupied MOs of BenzeneGTO::build_mo_coefficients
+    (src/systems/benzene.rs:247-470) over the 66 AOs in the order of
+    ``benzene_gto``: per carbon [1s, 2s in, 2p in (x, y, z), 2s out, 2p out
+    (x, y, z)] at 9 n, per hydrogen [1s in, 1s out] at 54 + 2 n.  Core 1s per
+    carbon; ring sigma (a1g and the cos/sin e1u pair over 2s and radial 2p);
+    one C-H sigma per bond (2s, 2p along C->H, H 1s); pi (a2u, e1g cos/sin over
+    2pz); tangential ring sigma (uniform, cos 2t, sin 2t)."""
+    C, H = R[:6], R[6:]
+    mo = np.zeros((21, 66))
+    s6, s3 = 1.0 / math.sqrt(6.0), 1.0 / math.sqrt(3.0)
+    ang = [math.pi / 3.0 * n for n in range(6)]
+    for n in range(6):                                   # MOs 0-5: carbon cores
+        mo[n, 9 * n], mo[n, 9 * n + 1], mo[n, 9 * n + 5] = 0.9943, 0.0234, 0.0020
+    for n in range(6):                                   # MOs 6-8: ring sigma from 2s (+ radial 2p)
+        mo[6, 9 * n + 1], mo[6, 9 * n + 5] = 0.20 * s6, 0.80 * s6
+        for k, f, pm in ((7, math.cos(ang[n]), 0), (8, math.sin(ang[n]), 1)):
+            w = f * s3
+            mo[k, 9 * n + 1], mo[k, 9 * n + 5] = 0.20 * w, 0.80 * w
+            mo[k, 9 * n + 2 + pm], mo[k, 9 * n + 6 + pm] = 0.50 * w, 0.55 * w
+    for n in range(6):                                   # MOs 9-14: C-H bonds
+        d = (H[n] - C[n]) / np.linalg.norm(H[n] - C[n])
+        k = 9 + n
+        mo[k, 9 * n + 1], mo[k, 9 * n + 5] = 0.15, 0.30
+        for m in range(3):
+            mo[k, 9 * n + 2 + m], mo[k, 9 * n + 6 + m] = 0.20 * d[m], 0.55 * d[m]
+        mo[k, 54 + 2 * n], mo[k, 54 + 2 * n + 1] = 0.25, 0.15
+    for n in range(6):                                   # MOs 15-17: pi
+        for k, w in ((15, s6), (16, math.cos(ang[n]) * s3), (17, math.sin(ang[n]) * s3)):
+            mo[k, 9 * n + 4], mo[k, 9 * n + 8] = 0.30 * w, 0.70 * w
+    for n in range(6):                                   # MOs 18-20: tangential ring sigma
+        tx, ty = -math.sin(ang[n]), math.cos(ang[n])
+        for k, w in ((18, s6), (19, math.cos(2 * ang[n]) * s3), (20, math.sin(2 * ang[n]) * s3)):
+            mo[k, 9 * n + 2], mo[k, 9 * n + 3] = 0.25 * tx * w, 0.25 * ty * w
+            mo[k, 9 * n + 6], mo[k, 9 * n + 7] = 0.60 * tx * w, 0.60 * ty * w
+    return mo
+
+
+def benzene_gto(b_ee=1.5, b_en=2.0):
+    """BenzeneGTO (src/systems/benzene.rs:48-470): D6h ring with C-C 2.640
+    and C-H 2.042 bohr, the 6-31G basis of MethaneGTO on every atom (66 AOs,
+    build_631g_basis at benzene.rs:152-245), the hand-built 21-MO table,
+    Jastrow3 (a_anti 0.5, a_para 0.25, A = 1, one b_en for both species).
+    Electrons 0-20 spin up, 21-41 spin down, both sectors over MOs 0-20;
+    initial centres as benzene.rs:642-655."""
+    R = hexagonal_c6h6(2.640, 2.042)
+    ao_nuc, ao_l, ao_m, prims = [], [], [], []
+
+    def add(n, l, m, p):
+        ao_nuc.append(n); ao_l.append(l); ao_m.append(m); prims.append(p)
+
+    for c in range(6):
+        add(c, 0, 0, C_1S)
+        add(c, 0, 0, list(zip(C_SP_INNER_EXP, C_SP_INNER_S)))
+        for m in range(3):
+            add(c, 1, m, list(zip(C_SP_INNER_EXP, C_SP_INNER_P)))
+        add(c, 0, 0, [(C_SP_OUTER_EXP, 1.0)])
+        for m in range(3):
+            add(c, 1, m, [(C_SP_OUTER_EXP, 1.0)])
+    for h in range(6):
+        add(6 + h, 0, 0, H_INNER)
+        add(6 + h, 0, 0, [(H_OUTER_EXP, 1.0)])
+    init = [i // 6 for i in range(36)] + [6 + h for h in range(6)]
+    return SystemSpec(
+        name="C6H6-6-31G", spins=[1] * 21 + [-1] * 21, nuc_pos=R, nuc_charge=[6.0] * 6 + [1.0] * 6,
+        nuc_species=[0] * 6 + [1] * 6, basis_kind=L.QMC_BASIS_GTO, ao_nuc=ao_nuc, ao_l=ao_l, ao_m=ao_m,
+        ao_prims=prims, mo_coef=_benzene_631g_mos(R), occ=list(range(21)) * 2, jastrow_kind=L.QMC_JAS_PADE_EEN,
         jas=jastrow3_params(b_ee, b_en), init_nuc=init, init_sigma=0.5)
 
 

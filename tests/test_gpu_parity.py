@@ -8,7 +8,13 @@ Tolerances (stated per test):
     configuration.
   * Trajectories: the counter-based Philox stream makes FP64 GPU sweeps and
     the oracle's reference-algorithm sweeps follow the same chain; positions
-    agree to 1e-9 and accepted-move counts exactly.
+    agree to 1e-9 and accepted-move counts exactly.  A walker may leave the
+    oracle's chain only where the oracle shows one of its acceptance
+    decisions within 1e-9 (relative) of the threshold, the only place two
+    FP64 evaluations that agree to ~1e-12 can decide differently.
+  * Statistics: FP32+refine and FP64 energies agree within 4 combined
+    standard errors (blocking errors, src/sampling/vmc.rs:166-188), with
+    runs long enough that the combined error is a few mHa.
 """
 import numpy as np
 import pytest
@@ -30,6 +36,26 @@ BUILDERS = {
 
 def rel(a, b):
     return np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b)))
+
+
+def assert_same_chain(got, want, margin, acc, acc_o, tol=1e-9):
+    """Every walker of the device chain follows the oracle's chain, except a
+    walker whose oracle run came within 1e-9 (relative) of an opposite
+    acceptance decision; accepted counts agree exactly when all walkers do."""
+    same = np.all(np.abs(got - want) < tol, axis=(1, 2))
+    unexplained = ~same & (margin > 1e-9)
+    assert not unexplained.any(), ("walkers off the oracle's chain", np.where(unexplained)[0],
+                                   margin[unexplained])
+    if same.all():
+        assert acc == acc_o.sum(), (acc, acc_o.sum())
+    return same
+
+
+def assert_energies_agree(a, b, max_sigma):
+    """|E_a - E_b| < 4 sigma_combined, with sigma_combined below max_sigma."""
+    sig = np.hypot(a["error"], b["error"])
+    assert 0 < sig < max_sigma, (a, b)
+    assert abs(a["energy"] - b["energy"]) < 4 * sig, (a["energy"], b["energy"], sig)
 
 
 @pytest.mark.parametrize("name", list(BUILDERS))
@@ -104,18 +130,16 @@ def test_fp32_walkers_refresh_energy_within_1e6(ctx, oracle, name):
 def test_fp64_single_electron_trajectory_matches_oracle(ctx, oracle, name, move):
     spec = BUILDERS[name]()
     sysh = Q.System(ctx, spec)
-    W, n = 64, 4
+    W, n = 256, 4
     wk = Q.Walkers(sysh, W, L.QMC_FP64)
     wk.init(seed=31)
     wk.refresh()
     pos0 = wk.get_positions()
     acc = wk.sweep(move, n, 10, seed=4242, step=0.3, tau=0.02, max_drift=1.0)
     got = wk.get_positions()
-    want, acc_o, _ = oracle.sweeps(spec, pos0, n, 10, move, 4242, step=0.3, tau=0.02, max_drift=1.0,
-                                   want_energy=False)
-    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
-    assert same.mean() >= 0.98, same.mean()
-    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, n, 10, move, 4242, step=0.3, tau=0.02, max_drift=1.0,
+                                       want_energy=False, want_margin=True)
+    assert_same_chain(got, want, mg, acc, acc_o)
     assert acc > 0
 
 
@@ -130,10 +154,8 @@ def test_fp64_all_electron_trajectory_matches_oracle(ctx, oracle, move):
     pos0 = wk.get_positions()
     acc = wk.sweep(move, n, 0, seed=99, step=1.0)
     got = wk.get_positions()
-    want, acc_o, el_o = oracle.sweeps(spec, pos0, n, 0, move, 99, step=1.0)
-    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
-    assert same.mean() >= 0.98
-    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))
+    want, acc_o, el_o, mg = oracle.sweeps(spec, pos0, n, 0, move, 99, step=1.0, want_margin=True)
+    same = assert_same_chain(got, want, mg, acc, acc_o)
     _, _, el = wk.state()
     np.testing.assert_allclose(el[same], el_o[same], rtol=1e-10, atol=1e-10)
 
@@ -244,17 +266,22 @@ def test_vmc_run_h2_box_moves(ctx):
     assert r["n_samples"] == 400
 
 
-def test_vmc_run_precisions_agree_ch4(ctx):
-    """FP32+refine and FP64 chains give statistically indistinguishable
-    energies (combined 4 sigma)."""
-    sysh = Q.System(ctx, Q.methane_minimal())
+@pytest.mark.parametrize("name", ["ch4_min", "c6h6", "heg"])
+def test_vmc_run_precisions_agree(ctx, name):
+    """FP32+refine and FP64 chains (independent seeds) give statistically
+    indistinguishable energies: within 4 combined standard errors, with no
+    slack beyond the error bars, and runs long enough that the combined
+    error is below 5 mHa (CH4, the electron gas) or 15 mHa (benzene, whose
+    synthetic wave function has a large E_L variance)."""
+    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal, "heg": Q.electron_gas}[name]()
+    sysh = Q.System(ctx, spec)
+    W, n, burn, step, cap = {"ch4_min": (32768, 1024, 128, 0.3, 5e-3), "c6h6": (4096, 512, 64, 0.3, 15e-3),
+                             "heg": (2048, 512, 64, 1.0, 5e-3)}[name]
     res = {}
     for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
-        res[prec] = Q.vmc_run(sysh, n_walkers=8192, n_steps=256, n_burnin=64, move_kind=L.QMC_MOVE_ONE_GAUSS,
-                              step=0.3, precision=prec, refresh_every=8, seed=11 + prec)
-    a, b = res[L.QMC_FP64], res[L.QMC_FP32_REFINE]
-    sig = np.hypot(max(a["error"], 1e-6), max(b["error"], 1e-6))
-    assert abs(a["energy"] - b["energy"]) < 4 * sig + 1e-3 * abs(a["energy"]), (a, b)
+        res[prec] = Q.vmc_run(sysh, n_walkers=W, n_steps=n, n_burnin=burn, move_kind=L.QMC_MOVE_ONE_GAUSS,
+                              step=step, precision=prec, refresh_every=8, seed=11 + prec)
+    assert_energies_agree(res[L.QMC_FP64], res[L.QMC_FP32_REFINE], cap)
 
 
 @pytest.mark.parametrize("name,fixed_node,refdiff", [("h2", True, False), ("ch4_min", True, False),
@@ -305,18 +332,21 @@ def test_dmc_run_h2_energy(ctx):
     assert 0.9 < d["acceptance_rate"] <= 1.0
 
 
-def test_dmc_precisions_agree_ch4(ctx):
-    """FP32+refine and FP64 DMC populations give statistically compatible
-    energies; the FP32 form measures E_L in FP64 every 8 steps."""
-    sysh = Q.System(ctx, Q.methane_minimal())
+@pytest.mark.parametrize("name", ["ch4_min", "c6h6"])
+def test_dmc_precisions_agree(ctx, name):
+    """FP32+refine and FP64 DMC populations (independent seeds) give energies
+    within 4 combined standard errors, no slack beyond the error bars; the
+    FP32 form measures E_L in FP64-class arithmetic every 8 steps."""
+    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal}[name]()
+    sysh = Q.System(ctx, spec)
+    W, n, burn, cap = {"ch4_min": (8192, 400, 100, 5e-3), "c6h6": (2048, 300, 100, 20e-3)}[name]
     r = {}
     for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
-        r[prec] = Q.dmc_run(sysh, n_walkers=4096, n_steps=120, n_burnin=40, tau=0.005, precision=prec,
+        r[prec] = Q.dmc_run(sysh, n_walkers=W, n_steps=n, n_burnin=burn, tau=0.005, precision=prec,
                             refresh_every=8, seed=5 + prec)
     a, b = r[L.QMC_FP64], r[L.QMC_FP32_REFINE]
     assert np.isfinite(a["energy"]) and np.isfinite(b["energy"])
-    sig = np.hypot(max(a["error"], 1e-4), max(b["error"], 1e-4))
-    assert abs(a["energy"] - b["energy"]) < 5 * sig + 2e-3 * abs(a["energy"]), (a, b)
+    assert_energies_agree(a, b, cap)
 
 
 # ---------------------------------------------------------------------------
@@ -361,18 +391,16 @@ def test_benzene_log_derivatives_and_sr_sums(ctx, oracle):
 def test_benzene_fp64_trajectory_matches_oracle(ctx, oracle, move):
     spec = Q.benzene_minimal()
     sysh = Q.System(ctx, spec)
-    W = 12
+    W, n = 256, 4
     wk = Q.Walkers(sysh, W, L.QMC_FP64)
     wk.init(seed=5)
     wk.refresh()
     pos0 = wk.get_positions()
-    acc = wk.sweep(move, 1, 3, seed=606, step=0.3, tau=0.005, max_drift=1.0)
+    acc = wk.sweep(move, n, 3, seed=606, step=0.3, tau=0.005, max_drift=1.0)
     got = wk.get_positions()
-    want, acc_o, _ = oracle.sweeps(spec, pos0, 1, 3, move, 606, step=0.3, tau=0.005, max_drift=1.0,
-                                   want_energy=False)
-    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
-    assert same.mean() >= 0.9, same.mean()
-    assert abs(acc - acc_o.sum()) <= max(2, int(0.02 * acc_o.sum()))
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, n, 3, move, 606, step=0.3, tau=0.005, max_drift=1.0,
+                                       want_energy=False, want_margin=True)
+    assert_same_chain(got, want, mg, acc, acc_o)
 
 
 def test_benzene_fp32_refresh_energy_within_1e6(ctx, oracle):
@@ -437,19 +465,18 @@ def test_heg_eval_fp64_matches_oracle(ctx, oracle, name):
 def test_heg_fp64_trajectory_matches_oracle(ctx, oracle, move):
     spec = Q.electron_gas()
     sysh = Q.System(ctx, spec)
-    W = 6
+    W, n = 256, 4
     wk = Q.Walkers(sysh, W, L.QMC_FP64)
     wk.init(seed=15)
     wk.refresh()
     pos0 = wk.get_positions()
     init = oracle.init_positions(spec, W, seed=15)
     np.testing.assert_allclose(pos0, init, atol=1e-12)
-    acc = wk.sweep(move, 1, 2, seed=616, step=1.0, tau=0.05, max_drift=1.0)
+    acc = wk.sweep(move, n, 2, seed=616, step=1.0, tau=0.05, max_drift=1.0)
     got = wk.get_positions()
-    want, acc_o, _ = oracle.sweeps(spec, pos0, 1, 2, move, 616, step=1.0, tau=0.05, max_drift=1.0, want_energy=False)
-    same = np.all(np.abs(got - want) < 1e-8, axis=(1, 2))
-    assert same.mean() >= 0.8, same.mean()
-    assert abs(acc - acc_o.sum()) <= max(2, int(0.03 * acc_o.sum()))
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, n, 2, move, 616, step=1.0, tau=0.05, max_drift=1.0,
+                                       want_energy=False, want_margin=True)
+    assert_same_chain(got, want, mg, acc, acc_o, tol=1e-8)
 
 
 def test_heg_fp32_refresh_energy_within_1e6(ctx, oracle):
@@ -583,8 +610,63 @@ def test_fp64_gaussian_sweeps_ragged_walker_count(ctx, oracle, name):
     pos0 = wk.get_positions()
     acc = wk.sweep(L.QMC_MOVE_ONE_GAUSS, n, 3, seed=777, step=0.3)
     got = wk.get_positions()
-    want, acc_o, _ = oracle.sweeps(spec, pos0, n, 3, L.QMC_MOVE_ONE_GAUSS, 777, step=0.3, want_energy=False)
-    same = np.all(np.abs(got - want) < 1e-9, axis=(1, 2))
-    assert same.mean() >= 0.98, same.mean()
-    assert same[-33:].mean() >= 0.95            # the walkers of the partial block
-    assert abs(acc - acc_o.sum()) <= max(1, int(0.02 * acc_o.sum()))
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, n, 3, L.QMC_MOVE_ONE_GAUSS, 777, step=0.3, want_energy=False,
+                                       want_margin=True)
+    assert_same_chain(got, want, mg, acc, acc_o)      # includes the 33 walkers of the partial block
+
+
+def benzene_distinct():
+    """Benzene with every Jastrow parameter distinct (b_anti != b_para,
+    a_anti != a_para, B_C != B_H, A_C != A_H), so that a swap of spin class or
+    species anywhere on the device changes the result."""
+    spec = Q.benzene_minimal()
+    return spec.with_params(np.array([1.3, 1.7, 0.45, 0.3, 1.9, 2.4, 0.8, 1.1]))
+
+
+def test_benzene_distinct_parameters_eval_and_sr(ctx, oracle):
+    spec = benzene_distinct()
+    sysh = Q.System(ctx, spec)
+    cfg = random_configs(spec, 40, seed=44)
+    g = sysh.eval_batch(cfg, L.QMC_FP64)
+    o = oracle.evaluate(spec, cfg)
+    assert np.array_equal(g["sign"], o["sign"])
+    assert rel(g["logabs"], o["logabs"]) < 1e-10
+    assert rel(g["grad"], o["grad"]) < 1e-9
+    assert rel(g["lap"], o["lap"]) < 1e-9
+    assert rel(g["e_local"], o["e_local"]) < 1e-10
+    O, E, S, f, em = sysh.logderiv_batch(cfg, sums=True)
+    Oo = oracle.log_derivatives(spec, cfg)
+    assert rel(O, Oo) < 1e-10
+    Om = Oo.mean(0)
+    np.testing.assert_allclose(S, Oo.T @ Oo / len(E) - np.outer(Om, Om), rtol=1e-8, atol=1e-8 * np.abs(S).max())
+
+
+@pytest.mark.parametrize("move", [L.QMC_MOVE_ONE_GAUSS, L.QMC_MOVE_ONE_DRIFT])
+def test_benzene_distinct_parameters_trajectory(ctx, oracle, move):
+    spec = benzene_distinct()
+    sysh = Q.System(ctx, spec)
+    W, n = 256, 4
+    wk = Q.Walkers(sysh, W, L.QMC_FP64)
+    wk.init(seed=46)
+    wk.refresh()
+    pos0 = wk.get_positions()
+    acc = wk.sweep(move, n, 5, seed=808, step=0.3, tau=0.005, max_drift=1.0)
+    got = wk.get_positions()
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, n, 5, move, 808, step=0.3, tau=0.005, max_drift=1.0,
+                                       want_energy=False, want_margin=True)
+    assert_same_chain(got, want, mg, acc, acc_o)
+
+
+def test_benzene_distinct_parameters_fp32_refresh(ctx, oracle):
+    spec = benzene_distinct()
+    sysh = Q.System(ctx, spec)
+    wk = Q.Walkers(sysh, 256, L.QMC_FP32_REFINE)
+    wk.init(seed=47)
+    wk.refresh()
+    assert wk.sweep(L.QMC_MOVE_ONE_GAUSS, 8, 0, seed=48, step=0.3) > 0
+    _, el = wk.refresh(want_energies=True)
+    la, sg, _ = wk.state()
+    o = oracle.evaluate(spec, wk.get_positions())
+    assert np.max(np.abs(el - o["e_local"])) <= 1e-6
+    assert rel(la, o["logabs"]) < 1e-10
+    assert np.array_equal(sg, o["sign"])

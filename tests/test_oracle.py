@@ -310,3 +310,81 @@ def test_heg_jastrow_gradient_antisymmetric(oracle):
     r = np.random.default_rng(7).uniform(0, spec.box_L, (54, 3))
     o = oracle.evaluate(spec, r)
     assert np.linalg.norm(o["grad"][0].sum(axis=0)) < 1e-6 * np.abs(o["grad"]).max() * 54
+
+
+@pytest.mark.parametrize("name", ["ch4_min", "ch4_gto", "c6h6"])
+def test_el_derivatives_match_finite_differences(oracle, name):
+    """The oracle's analytic dE_L/dp (Jastrow parameters and MO-rotation
+    angles) against Richardson-extrapolated central differences of its E_L
+    (steps 2h and h, h = 1e-4): 1e-6 relative.  Plain central differences at
+    h = 1e-4 carry an O(h^2) truncation error of up to ~1e-4 relative for the
+    rotation angles near a node, which the extrapolation removes."""
+    import rust_qmc_gb300.systems as S
+    spec = {"ch4_min": S.methane_minimal, "ch4_gto": S.methane_gto, "c6h6": S.benzene_minimal}[name]()
+    p = np.asarray(spec.params(), dtype=np.float64)
+    p[:8] = [1.3, 1.7, 0.45, 0.3, 1.9, 2.4, 0.8, 1.1]
+    if len(p) > 8:
+        p[8:] = [0.1, -0.2, 0.05, 0.3][: len(p) - 8]
+    spec = spec.with_params(p)
+    cfg = random_configs(spec, 3 if name == "c6h6" else 8, seed=3)
+    a = oracle.el_derivatives(spec, cfg)
+    f1 = oracle.el_derivatives_fd(spec, cfg, h=2e-4)
+    f2 = oracle.el_derivatives_fd(spec, cfg, h=1e-4)
+    fd = (4 * f2 - f1) / 3
+    np.testing.assert_allclose(a, fd, rtol=1e-6, atol=1e-6 * np.abs(fd).max())
+
+
+def test_benzene_gto_reference_checks(oracle):
+    """The reference's own BenzeneGTO tests (src/systems/benzene.rs:871-1006)
+    on benzene_gto: geometry (ring of radius 2.640, 120 degree angles, planar,
+    C-H 2.042), 66 AOs and 21 MOs, V_nn in (180, 230), 21 + 21 electrons,
+    psi finite at an initial configuration, analytic gradient against
+    central differences, and the four reference log-derivatives (b_ee, b_en,
+    a_anti, a_para at BenzeneGTO::new(2.0, 3.0)) against finite differences."""
+    spec = Q.benzene_gto()
+    R, Z = spec.nuc_pos, spec.nuc_charge
+    C, H = R[Z == 6], R[Z == 1]
+    for i in range(6):
+        assert abs(np.linalg.norm(C[i]) - 2.640) < 1e-10
+        assert abs(np.linalg.norm(C[i] - C[(i + 1) % 6]) - 2.640) < 0.01
+        v1, v2 = C[(i + 5) % 6] - C[i], C[(i + 1) % 6] - C[i]
+        assert abs(math.degrees(math.acos(v1 @ v2 / np.linalg.norm(v1) / np.linalg.norm(v2))) - 120.0) < 0.1
+        assert abs(np.linalg.norm(C[i] - H[i]) - 2.042) < 0.01
+    assert np.all(np.abs(R[:, 2]) < 1e-10)
+    assert len(spec.ao_nuc) == 66 and spec.mo_coef.shape == (21, 66)
+    assert 180.0 < spec.v_nn() < 230.0
+    assert spec.n_elec == 42 and np.sum(np.asarray(spec.spins) > 0) == 21
+    r = oracle.init_positions(spec, 2, seed=12)
+    ev = oracle.evaluate(spec, r)
+    assert np.all(np.isfinite(ev["logabs"])) and np.all(np.isfinite(ev["e_local"]))
+    g, _ = fd_grad_lap(oracle, spec, r[0], h=1e-5)
+    for i in (0, 10, 20, 30, 40):
+        np.testing.assert_allclose(ev["grad"][0, i], g[i], rtol=1e-5, atol=1e-6 * (1 + np.abs(g[i]).max()))
+    spec2 = Q.benzene_gto(2.0, 3.0)
+    r2 = oracle.init_positions(spec2, 1, seed=13)
+    O = oracle.log_derivatives(spec2, r2)[0]
+    ref4 = [O[0] + O[1], O[4] + O[5], O[2], O[3]]
+    p = Q.reference_params_from_general(spec2.params())
+    h = 1e-5
+    for k in range(4):
+        pp, pm = list(p), list(p)
+        pp[k] += h
+        pm[k] -= h
+        lp = oracle.evaluate(spec2.with_params(Q.jastrow3_params(*pp)), r2)["logabs"][0]
+        lm = oracle.evaluate(spec2.with_params(Q.jastrow3_params(*pm)), r2)["logabs"][0]
+        assert abs(ref4[k] - (lp - lm) / (2 * h)) <= 1e-6 * max(1.0, abs(ref4[k]))
+
+
+def test_benzene_gto_mo_table_structure():
+    """The hand-built MO table of src/systems/benzene.rs:262-470: core MOs on
+    one carbon each, the pi MOs only on 2pz AOs, the C-H MOs touching one
+    hydrogen each, and the ring MOs normalised over their phase patterns."""
+    M = Q.benzene_gto().mo_coef
+    for n in range(6):
+        assert np.count_nonzero(M[n]) == 3 and M[n, 9 * n] == 0.9943
+        nz = np.nonzero(M[9 + n])[0]
+        assert set(nz[nz >= 54].tolist()) == {54 + 2 * n, 55 + 2 * n}
+    pz = [9 * n + 4 for n in range(6)] + [9 * n + 8 for n in range(6)]
+    for k in (15, 16, 17):
+        assert set(np.nonzero(M[k])[0].tolist()) <= set(pz)
+    assert np.all(M[15:18, [9 * n + 2 for n in range(6)]] == 0)

@@ -333,9 +333,10 @@ def other_configs(ctx, args, fp32_peak, fp64_peak, cpu=True, cpu_seconds=2.0):
                                     "unit": "TFLOP/s", "frac": tf / fp32_peak if fp32_peak else None,
                                     "flops_per_move": c["sweep_flops_per_move"]}}
     e_ref = wk.refresh() / W
+    cut = 2.0 / np.sqrt(0.005)
     step = 0
     for _ in range(5):
-        n, em = wk.dmc_step(0.005, e_ref, seed=0x51A7E5 + 4, step=step, fp64_measure=True)
+        n, em = wk.dmc_step(0.005, e_ref, seed=0x51A7E5 + 4, step=step, fp64_measure=True, branch_cut=cut)
         step += 1
         e_ref = em - 0.5 * np.log(n / W) / 0.005
     ctx.synchronize()
@@ -344,7 +345,7 @@ def other_configs(ctx, args, fp32_peak, fp64_peak, cpu=True, cpu_seconds=2.0):
     ctx.record(5)
     for _ in range(20):
         nb = wk.W
-        n, em = wk.dmc_step(0.005, e_ref, seed=0x51A7E5 + 4, step=step, fp64_measure=True)
+        n, em = wk.dmc_step(0.005, e_ref, seed=0x51A7E5 + 4, step=step, fp64_measure=True, branch_cut=cut)
         step += 1
         dmoves += nb * 42
         pops.append(n)
@@ -352,8 +353,8 @@ def other_configs(ctx, args, fp32_peak, fp64_peak, cpu=True, cpu_seconds=2.0):
     ctx.record(6)
     dms = ctx.elapsed_ms(5, 6)
     out["c6h6_dmc"] = {"workload": "benzene IS-DMC, target 16384, tau 0.005: drift-diffusion sweep with fixed-node "
-                                   "rejection, FP64-class E_L, FP64 log-weight branching and on-device compaction "
-                                   "per step (FP32 walkers)", "value": dmoves / (dms / 1e3), "unit": UNIT,
+                                   "rejection, FP64-class E_L, FP64 log-weight branching (branching energy clamped "
+                                   "to E_ref +- 2/sqrt(tau)) and on-device compaction per step (FP32 walkers)", "value": dmoves / (dms / 1e3), "unit": UNIT,
                        "ms_per_step": dms / 20, "population": [min(pops), max(pops)]}
     wk.close()
     if cpu:

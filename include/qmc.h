@@ -164,7 +164,13 @@ typedef struct {
     int adaptation_interval;
     double min_step;
     double max_step;
-    int reserved[4];
+    /* DMC: > 0 clamps the branching energy (E_L + E_L,old)/2 to E_ref +- branch_cut
+     * (the reference branches on it unclamped, is_dmc.rs:278-302; a cut of
+     * 2 / sqrt(tau) in the manner of Umrigar, Nightingale and Runge, J. Chem. Phys.
+     * 99, 2865 (1993), keeps populations of trial functions with nodal E_L
+     * divergences finite); 0 = the reference's branching */
+    double branch_cut;
+    int reserved[2];
 } qmc_run_params;
 
 typedef struct {
@@ -275,7 +281,8 @@ int qmc_walkers_status(qmc_walkers_t wk, int* flags);
 int qmc_walkers_create_dmc(qmc_sys_t sys, int W, int capacity, int precision, qmc_walkers_t* out);
 /* Current population size. */
 int qmc_walkers_count(qmc_walkers_t wk, int* W);
-/* One IS-DMC step (src/sampling/is_dmc.rs:208-302): one drift-diffusion sweep
+/* One IS-DMC step (src/sampling/is_dmc.rs:208-302; branch_cut as in
+ * qmc_run_params, 0 = the reference's branching): one drift-diffusion sweep
  * per walker made with the reference-convention move at tau_move (variance
  * 2 tau_move, drift 2 tau_move grad ln psi; tau_move = tau / 2 is the
  * Hartree-unit projector, tau_move = tau the reference's), fixed-node
@@ -287,7 +294,8 @@ int qmc_walkers_count(qmc_walkers_t wk, int* W);
  * (0 = collapse), *e_mean its mean E_L.  QMC_ERR_POPULATION if the new
  * population exceeds the capacity (the population is then left unchanged). */
 int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double max_drift, int fixed_node,
-                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean);
+                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, double branch_cut, int* n_new,
+                         double* e_mean);
 
 /* ---- drivers --------------------------------------------------------------- */
 /* VMC run: MCMCSimulation::run (src/sampling/vmc.rs:69-92) for all-electron

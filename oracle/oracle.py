@@ -34,7 +34,7 @@ def lib():
         l.orc_sweeps.argtypes = [vp, C.c_int, C.c_uint32, _dp, C.c_int, C.c_uint64, C.c_int, C.c_double,
                                  C.c_double, C.c_double, C.c_uint64, _ip, _dp, _dp, C.c_int]
         l.orc_dmc.argtypes = [vp, C.c_int, _dp, C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_int,
-                              C.c_double,
+                              C.c_double, C.c_double,
                               C.c_int, C.c_uint64, C.c_int, _dp, _ip, _ip, _dp, _dp, C.c_int]
         l.orc_dmc.restype = C.c_int
         l.orc_heg_ewald.argtypes = [vp, _dp, C.c_double, C.c_int]
@@ -175,7 +175,7 @@ def sweeps(spec, pos, n_sweeps, sweep0, move_kind, seed, step=0.3, tau=0.01, max
 
 
 def dmc(spec, pos, n_steps, tau, e_ref, target, seed, step0=0, max_drift=1.0, fixed_node=True, kappa=0.5,
-        cap=None, threads=None, reference_diffusion=False):
+        cap=None, threads=None, reference_diffusion=False, branch_cut=0.0):
     """Reference-algorithm IS-DMC with the shared random stream.
     Returns (final positions, per-step populations, per-step mean E_L, E_ref)."""
     pos = np.ascontiguousarray(pos, dtype=np.float64)
@@ -189,7 +189,7 @@ def dmc(spec, pos, n_steps, tau, e_ref, target, seed, step0=0, max_drift=1.0, fi
     d = spec.desc()
     tau_move = tau if reference_diffusion else 0.5 * tau
     done = lib().orc_dmc(C.byref(d), W0, _d(pos), n_steps, step0, tau, tau_move, max_drift, int(bool(fixed_node)),
-                         kappa, target,
+                         kappa, float(branch_cut), target,
                          seed, cap, _d(out), C.byref(Wout), _i(pops), _d(en), C.byref(er), threads or threads_default())
     return out[:Wout.value], pops[:done], en[:done], er.value
 

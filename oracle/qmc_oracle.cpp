@@ -1214,10 +1214,12 @@ int orc_sweeps(const orc_system_desc* d, int W, uint32_t walker0, double* pos, i
 // with xi from tag-4 draws, populations rebuilt in slot order, and
 // E_ref = <E_L> - kappa ln(N / N_target) / tau.  Stops early if the population
 // collapses or exceeds `cap`.  Returns the number of steps done; pos_out
-// receives the final population, pops/energies the per-step values.
+// receives the final population, pops/energies the per-step values.  e_cut > 0
+// clamps the branching energy (E_L + E_old)/2 to e_ref +- e_cut (an option of
+// the device path; the reference branches unclamped).
 int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps, uint64_t step0, double tau,
-            double tau_move, double max_drift, int fixed_node, double kappa, int target, uint64_t seed, int cap,
-            double* pos_out,
+            double tau_move, double max_drift, int fixed_node, double kappa, double e_cut, int target, uint64_t seed,
+            int cap, double* pos_out,
             int* W_out, int* pops, double* energies, double* e_ref_io, int threads) {
     Sys s = make_sys(d);
     int N = s.N;
@@ -1249,7 +1251,9 @@ int orc_dmc(const orc_system_desc* d, int W0, const double* pos_in, int n_steps,
         for (int w = 0; w < W; ++w) {
             int m = 0;
             if (std::isfinite(E[w]) && std::isfinite(Eold[w])) {
-                double wgt = std::exp(tau * (e_ref - 0.5 * (E[w] + Eold[w])));
+                double eb = 0.5 * (E[w] + Eold[w]);
+                if (e_cut > 0.0) eb = std::min(e_ref + e_cut, std::max(e_ref - e_cut, eb));
+                double wgt = std::exp(tau * (e_ref - eb));
                 U4 x = draw(seed, (uint32_t)w, st, 0, TAG_BRANCH);
                 double f = std::floor(wgt + u01(x.v[0]));
                 m = f >= 3.0 ? 3 : (int)f;

@@ -46,7 +46,7 @@ class RunParams(C.Structure):
         ("precision", C.c_int), ("refresh_every", C.c_int), ("e_ref_damping", C.c_double),
         ("fixed_node", C.c_int), ("reference_diffusion", C.c_int),
         ("target_acceptance", C.c_double), ("adaptation_interval", C.c_int), ("min_step", C.c_double),
-        ("max_step", C.c_double), ("reserved", C.c_int * 4),
+        ("max_step", C.c_double), ("branch_cut", C.c_double), ("reserved", C.c_int * 2),
     ]
 
 
@@ -110,8 +110,8 @@ PROTOTYPES = {
                            _dp],
     "qmc_walkers_create_dmc": [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)],
     "qmc_walkers_count": [_vp, _ip],
-    "qmc_walkers_dmc_step": [_vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _u64, _u64, C.c_int, _ip,
-                             _dp],
+    "qmc_walkers_dmc_step": [_vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _u64, _u64, C.c_int,
+                             C.c_double, _ip, _dp],
     "qmc_ctx_event_record": [_vp, C.c_int],
     "qmc_ctx_event_elapsed": [_vp, C.c_int, C.c_int, C.POINTER(C.c_float)],
     "qmc_ctx_synchronize": [_vp],

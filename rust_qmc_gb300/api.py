@@ -322,12 +322,13 @@ class Walkers:
         return n.value
 
     def dmc_step(self, tau, e_ref, seed, step, max_drift=1.0, fixed_node=True, fp64_measure=False,
-                 reference_diffusion=False):
-        """One IS-DMC step; returns (new population, mean E_L of it)."""
+                 reference_diffusion=False, branch_cut=0.0):
+        """One IS-DMC step; returns (new population, mean E_L of it).
+        branch_cut > 0 clamps the branching energy to e_ref +- branch_cut."""
         n, em = C.c_int(), C.c_double()
         tau_move = tau if reference_diffusion else 0.5 * tau
         L.check(self.lib.qmc_walkers_dmc_step(self.h, tau, tau_move, max_drift, int(bool(fixed_node)), e_ref, seed, step,
-                                              int(bool(fp64_measure)), C.byref(n), C.byref(em)),
+                                              int(bool(fp64_measure)), float(branch_cut), C.byref(n), C.byref(em)),
                 "qmc_walkers_dmc_step")
         self.W = n.value
         return n.value, em.value
@@ -439,12 +440,13 @@ def vmc_run(system, *, n_walkers, n_steps, n_burnin=0, move_kind=L.QMC_MOVE_ALL_
 
 
 def _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping, fixed_node,
-                reference_diffusion):
+                reference_diffusion, branch_cut=0.0):
     p = L.RunParams()
     p.n_walkers, p.n_steps, p.n_burnin, p.move_kind = n_walkers, n_steps, n_burnin, L.QMC_MOVE_ONE_DRIFT
     p.tau, p.max_drift, p.precision, p.refresh_every = tau, max_drift, precision, refresh_every
     p.e_ref_damping, p.fixed_node = e_ref_damping, int(bool(fixed_node))
     p.reference_diffusion = int(bool(reference_diffusion))
+    p.branch_cut = float(branch_cut)
     return p
 
 
@@ -456,10 +458,12 @@ def _run_dict(res, energies):
 
 
 def dmc_run(system, *, n_walkers, n_steps, n_burnin=0, tau=0.005, max_drift=1.0, precision=L.QMC_FP64,
-            refresh_every=1, e_ref_damping=0.5, fixed_node=True, reference_diffusion=False, seed=1):
-    """ImportanceSampledDMC::run (energy part) on the device."""
+            refresh_every=1, e_ref_damping=0.5, fixed_node=True, reference_diffusion=False, seed=1, branch_cut=0.0):
+    """ImportanceSampledDMC::run (energy part) on the device; branch_cut > 0
+    clamps the branching energy to E_ref +- branch_cut (0: the reference's
+    branching)."""
     p = _dmc_params(n_walkers, n_steps, n_burnin, tau, max_drift, precision, refresh_every, e_ref_damping,
-                    fixed_node, reference_diffusion)
+                    fixed_node, reference_diffusion, branch_cut)
     res = L.RunResult()
     energies = np.zeros(n_steps)
     L.check(system.lib.qmc_dmc_run(system.h, C.byref(p), seed, C.byref(res), _d(energies)), "qmc_dmc_run")

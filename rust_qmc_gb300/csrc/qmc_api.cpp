@@ -419,7 +419,7 @@ double dmc_block_error(const std::vector<double>& x) {
 // sweep, E_L in the walkers' precision (FP64 when fp64_measure), branching
 // and compaction into the alternate buffer, swap.
 int dmc_step(qmc_walkers_s* wk, double tau, double tau_move, double max_drift, int fixed_node, double e_ref,
-             uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+             uint64_t seed, uint64_t step, int fp64_measure, double e_cut, int* n_new, double* e_mean) {
     CK(ensure_dmc(wk));
     const HostSys& hs = wk->sys->hs;
     cudaStream_t st = wk->sys->ctx->stream;
@@ -431,7 +431,7 @@ int dmc_step(qmc_walkers_s* wk, double tau, double tau_move, double max_drift, i
     CK(rc);
     MeasureOut none;
     CK(launch_measure(hs, dw, (fp64_measure || dw.prec == QMC_FP64) ? 0 : 1, true, none, st));
-    CK(launch_branch(dw, wk->alt, wk->br, hs.N, dinv_elems_of_shape(hs.shape), e_ref, tau, seed, step, st));
+    CK(launch_branch(dw, wk->alt, wk->br, hs.N, dinv_elems_of_shape(hs.shape), e_ref, tau, e_cut, seed, step, st));
     double stats[2] = {0, 0};
     CU(cudaMemcpyAsync(stats, wk->br.stats, 16, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
@@ -844,11 +844,14 @@ int qmc_walkers_count(qmc_walkers_t wk, int* W) {
 }
 
 int qmc_walkers_dmc_step(qmc_walkers_t wk, double tau, double tau_move, double max_drift, int fixed_node,
-                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, int* n_new, double* e_mean) {
+                         double e_ref, uint64_t seed, uint64_t step, int fp64_measure, double branch_cut, int* n_new,
+                         double* e_mean) {
     if (!wk || !n_new || !e_mean || !(tau > 0) || !(tau_move > 0) || !(max_drift > 0) || wk->dw.W <= 0)
         return QMC_ERR_ARG;
+    if (!(branch_cut >= 0)) return QMC_ERR_ARG;
     cudaSetDevice(wk->sys->ctx->device);
-    return dmc_step(wk, tau, tau_move, max_drift, fixed_node, e_ref, seed, step, fp64_measure, n_new, e_mean);
+    return dmc_step(wk, tau, tau_move, max_drift, fixed_node, e_ref, seed, step, fp64_measure, branch_cut, n_new,
+                    e_mean);
 }
 
 namespace {
@@ -1241,6 +1244,7 @@ static int dmc_run_impl(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc
                         double* forces_mixed) {
     if (!s || !p || !res) return QMC_ERR_ARG;
     if (p->n_walkers <= 0 || p->n_steps <= 0 || p->n_burnin < 0 || !(p->tau > 0) || !(p->max_drift > 0)) return QMC_ERR_ARG;
+    if (!(p->branch_cut >= 0)) return QMC_ERR_ARG;
     std::memset(res, 0, sizeof(*res));
     cudaSetDevice(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
@@ -1286,8 +1290,8 @@ static int dmc_run_impl(qmc_sys_t s, const qmc_run_params* p, uint64_t seed, qmc
         // projector needs variance tau and drift tau grad ln psi, i.e. the
         // reference-convention move at tau / 2.
         const double tau_move = p->reference_diffusion ? p->tau : 0.5 * p->tau;
-        CK(dmc_step(wk, p->tau, tau_move, p->max_drift, p->fixed_node, e_ref, seed, (uint64_t)t, fp64, &n_new,
-                    &em));
+        CK(dmc_step(wk, p->tau, tau_move, p->max_drift, p->fixed_node, e_ref, seed, (uint64_t)t, fp64, p->branch_cut,
+                    &n_new, &em));
         if (t >= p->n_burnin) moves += (long long)Wcur * hs.N;
         if (n_new == 0) {                                // collapse: re-initialise, is_dmc.rs:428-437
             ++collapses;

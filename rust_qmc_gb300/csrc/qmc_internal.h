@@ -143,10 +143,11 @@ int launch_hf_force_walkers(const DevWalkers& dw, int N, int n_nuc, const double
 int launch_hf_force_sum(const DevWalkers& dw, int N, int n_nuc, const double* d_nuc, double* d_partial,
                         size_t partial_cap, double* d_out, cudaStream_t st);
 // DMC branching (src/sampling/is_dmc.rs:278-302): copies per walker from the
-// FP64 log-weight, exclusive scan, order-stable gather into `dst`.
+// FP64 log-weight, exclusive scan, order-stable gather into `dst`.  e_cut > 0
+// clamps the branching energy (E_L + E_old)/2 to e_ref +- e_cut.
 // stats[0] = new population, stats[1] = sum of copies x E_L, stats[2] = flags.
 int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, int nmax, double e_ref,
-                  double tau, uint64_t seed, uint64_t step, cudaStream_t st);
+                  double tau, double e_cut, uint64_t seed, uint64_t step, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Uneven batches: many systems, each with its own walker set, advanced by a

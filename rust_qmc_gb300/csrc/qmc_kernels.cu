@@ -522,14 +522,16 @@ int launch_sum_partials(const double* partial, int nblk, int nrows, double* out,
 // FP64 log-weight, xi from the tag-4 Philox draw of (walker slot, step).
 // Walkers with a non-finite energy get no copy.
 __global__ void k_branch_counts(const double* __restrict__ el, const double* __restrict__ el_old, int W,
-                                double e_ref, double tau, uint64_t seed, uint64_t step, int* __restrict__ counts,
-                                int* flags) {
+                                double e_ref, double tau, double e_cut, uint64_t seed, uint64_t step,
+                                int* __restrict__ counts, int* flags) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= W) return;
     double e = el[w], eo = el_old[w];
     int m = 0;
     if (isfinite(e) && isfinite(eo)) {
-        double logw = tau * (e_ref - 0.5 * (e + eo));
+        double eb = 0.5 * (e + eo);
+        if (e_cut > 0.0) eb = fmin(e_ref + e_cut, fmax(e_ref - e_cut, eb));
+        double logw = tau * (e_ref - eb);
         U4 x = rng_draw(seed, (uint32_t)w, step, 0, TAG_BRANCH);
         double f = floor(exp(logw) + to_u01(x.x, 0.0));
         m = f >= 3.0 ? 3 : (f <= 0.0 ? 0 : (int)f);
@@ -608,11 +610,11 @@ __global__ void k_branch_gather(const int* __restrict__ offsets, int W, const do
 }
 
 int launch_branch(DevWalkers& src, DevWalkers& dst, DevBranch& br, int n_elec, int nmax, double e_ref, double tau,
-                  uint64_t seed, uint64_t step, cudaStream_t st) {
+                  double e_cut, uint64_t seed, uint64_t step, cudaStream_t st) {
     int W = src.W;
     if (W <= 0 || W > br.cap) return 1;
-    k_branch_counts<<<(W + 255) / 256, 256, 0, st>>>(src.el, br.el_old, W, e_ref, tau, seed, step, br.counts,
-                                                       src.flags);
+    k_branch_counts<<<(W + 255) / 256, 256, 0, st>>>(src.el, br.el_old, W, e_ref, tau, e_cut, seed, step,
+                                                       br.counts, src.flags);
     k_branch_scan<<<1, 1024, 0, st>>>(br.counts, src.el, W, br.offsets, br.stats);
     int most = std::min(3 * W, dst.Wcap);
     int npos = 3 * n_elec, ndinv = nmax;   // caller passes the per-walker inverse-block size

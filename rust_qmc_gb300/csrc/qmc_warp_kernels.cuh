@@ -21,6 +21,7 @@ namespace qmc {
 constexpr int WMAX_AO = 96;       // up to three rounds of 32 AOs (BenzeneGTO's 6-31G basis has 66)
 constexpr int WAO_ROUNDS = WMAX_AO / 32;
 constexpr int WNCOL = 24;         // Slater columns held per sector (lanes >= WNCOL read no coefficients)
+constexpr int AO_REP = 16;        // ao_type flag: radial part equal to the previous AO's
 constexpr int WMAX_PRIM = 256;
 constexpr int WMAX_NUC = 16;
 
@@ -33,7 +34,9 @@ struct SysW {
     T b_ee[2], a_ee[2];
     T nuc[WMAX_NUC][3];
     T Z[WMAX_NUC], enA[WMAX_NUC], enB[WMAX_NUC];
-    int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];   // type 0 s, 1..3 p_x..p_z
+    // ao_type: bits 0-3 the kind (0 s, 1..3 p_x..p_z); AO_REP set when the AO has the
+    // centre and primitives of the previous AO (p_y and p_z after p_x share its radial part)
+    int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];
     T pexp[WMAX_PRIM], pcoef[WMAX_PRIM];
     T C[2][WMAX_AO][WNCOL];     // [sector][AO][column]
     T init_sigma;
@@ -77,9 +80,11 @@ static bool fill_sysw(const HostSys& hs, int NE, int NUP, int NNUC, SysW<T>& S) 
         };
         for (int k = 0; k < 2; ++k)
             if (sh.s_ao[k] >= 0 && !put(sh.s_ao[k], 0, sh.s_coef[k])) return false;
+        // the p triplet's members are consecutive in the internal order and share
+        // one radial part: p_y and p_z reuse p_x's
         if (sh.p_ao[0] >= 0)
             for (int m = 0; m < 3; ++m)
-                if (!put(sh.p_ao[m], 1 + m, sh.p_coef)) return false;
+                if (!put(sh.p_ao[m], (1 + m) | (m > 0 ? AO_REP : 0), sh.p_coef)) return false;
     }
     std::vector<double> Ce = hs.effective_mo();
     for (int sig = 0; sig < 2; ++sig) {
@@ -131,7 +136,7 @@ __device__ __forceinline__ void ao_lane(const SysW<T>& S, T x, T y, T z, int lan
         const int a = lane + 32 * r;
         T v = 0, gxx = 0, gyy = 0, gzz = 0, lp = 0;
         if (32 * r < S.n_ao && a < S.n_ao) {
-            const int I = S.ao_nuc[a], type = S.ao_type[a], p0 = S.ao_p0[a], np = S.ao_np[a];
+            const int I = S.ao_nuc[a], type = S.ao_type[a] & 15, p0 = S.ao_p0[a], np = S.ao_np[a];
             T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
             T r2 = dx * dx + dy * dy + dz * dz;
             T s0 = 0, s1 = 0, s2 = 0;
@@ -171,6 +176,31 @@ __device__ __forceinline__ T wsum(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += wshfl_xor(v, o);
     return v;
+}
+
+// Four consecutive elements of 16-byte-aligned shared memory as one vector
+// access (two for double).
+__device__ __forceinline__ void load4(const float* p, float& a, float& b, float& c, float& d) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double& a, double& b, double& c, double& d) {
+    const double2 u = reinterpret_cast<const double2*>(p)[0], v = reinterpret_cast<const double2*>(p)[1];
+    a = u.x; b = u.y; c = v.x; d = v.y;
+}
+__device__ __forceinline__ void store4(float* p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void store4(double* p, double a, double b, double c, double d) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+
+// Elements of the per-warp scratch of the single-electron sweep: one row of
+// WNCOL orbital values per proposal of a sector.
+template <int NE, int NUP>
+__host__ __device__ constexpr int sweep_scratch_elems() {
+    return (NUP > NE - NUP ? NUP : NE - NUP) * WNCOL;
 }
 
 // MO contraction: lane k receives phi_k = sum_a C[sig][a][k] chi_a (and
@@ -293,10 +323,50 @@ __device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, N
     return du;
 }
 
+// Row stride of the per-warp proposal-orbital scratch (a multiple of 4
+// elements, so that rows start 16-byte aligned and read as vectors).
+constexpr int PHS = WNCOL;
+
+// Orbital values phi_k(x, y, z), k < NM, of sector sig by one lane: every AO
+// in turn (its radial part reused across a p triplet), accumulated into the
+// table's columns (broadcast reads: every lane reads the same coefficients);
+// written to out[k] as vectors.
+template <class T, int NM>
+__device__ __forceinline__ void proposal_orbitals(const SysW<T>& S, int sig, T x, T y, T z, T* out) {
+    constexpr int NV = (NM + 3) / 4;
+    T acc[4 * NV];
+#pragma unroll
+    for (int k = 0; k < 4 * NV; ++k) acc[k] = 0;
+    T s0 = 0, dx = 0, dy = 0, dz = 0;
+    for (int a = 0; a < S.n_ao; ++a) {
+        const int tf = S.ao_type[a], type = tf & 15;
+        if (!(tf & AO_REP)) {
+            const int I = S.ao_nuc[a], p0 = S.ao_p0[a], np = S.ao_np[a];
+            dx = x - S.nuc[I][0]; dy = y - S.nuc[I][1]; dz = z - S.nuc[I][2];
+            const T r2 = dx * dx + dy * dy + dz * dz;
+            s0 = 0;
+            for (int p = p0; p < p0 + np; ++p) s0 += S.pcoef[p] * fexp(-S.pexp[p] * r2);
+        }
+        const T chi = (type == 0 ? T(1) : (type == 1 ? dx : (type == 2 ? dy : dz))) * s0;
+        const T* c = S.C[sig][a];
+#pragma unroll
+        for (int k = 0; k < 4 * NV; ++k) acc[k] += c[k] * chi;
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) store4(out + 4 * v, acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+}
+
 // Single-electron sweeps, one warp per walker, WPB walkers per block.  A is
-// const SweepArgs<T> or const volatile SweepArgs<T>.
+// const SweepArgs<T> or const volatile SweepArgs<T>.  Gaussian moves take a
+// sector's proposals together: an electron of the sector keeps its position
+// until its own proposal, so all NS proposed positions are known when the
+// sector's turn starts; lane i evaluates the orbitals at proposal i into the
+// warp's scratch ph (proposal_orbitals), and each proposal then reads its row
+// as a broadcast instead of contracting AO values broadcast lane to lane.
+// Drift-diffusion proposals depend on the current drift and stay one at a
+// time.
 template <int NE, int NUP, int NNUC, class T, int MOVE, class A>
-__device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w) {
+__device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T* ph) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
     const int lane = threadIdx.x & 31;
@@ -326,6 +396,16 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w) {
             const int NS = sig == 0 ? NUP : NDN;
             static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
             const MoveDraw<T> draws = sector_draws<T>(a.seed, (uint32_t)w, st, sig * NUP, NS, lane);
+            T pnx = 0, pny = 0, pnz = 0;              // this lane's proposal (Gaussian moves)
+            if constexpr (MOVE == MOVE_ONE_GAUSS) {
+                T ex, ey, ez;
+                P.get_own(min(sig * NUP + lane, NE - 1), ex, ey, ez);
+                const T step = a.step;
+                pnx = ex + step * draws.n0; pny = ey + step * draws.n1; pnz = ez + step * draws.n2;
+                __syncwarp();                          // the previous sector's rows are read
+                if (lane < NS) proposal_orbitals<T, NM>(S, sig, pnx, pny, pnz, ph + lane * PHS);
+                __syncwarp();
+            }
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
@@ -354,20 +434,34 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w) {
                     T sd2 = fsqrt(2 * tau);
                     nx = rx + dlx + sd2 * md.n0; ny = ry + dly + sd2 * md.n1; nz = rz + dlz + sd2 * md.n2;
                 } else {
-                    const T step = a.step;
-                    nx = rx + step * md.n0; ny = ry + step * md.n1; nz = rz + step * md.n2;
+                    nx = wshfl(pnx, q); ny = wshfl(pny, q); nz = wshfl(pnz, q);
                 }
-                AOLane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0> ao;
-                ao_lane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0>(S, nx, ny, nz, lane, ao);
-                T phi, pgx, pgy, pgz, pl;
-                mo_lane<T, (MOVE == MOVE_ONE_DRIFT) ? 1 : 0>(S, sig, lane, ao, phi, pgx, pgy, pgz, pl);
                 // t_j = sum_k phi_k Dinv[k][j]; R = t_q
                 T tj = 0, bx = 0, by = 0, bz = 0;
+                if constexpr (MOVE == MOVE_ONE_DRIFT) {
+                    AOLane<T, 1> ao;
+                    ao_lane<T, 1>(S, nx, ny, nz, lane, ao);
+                    T phi, pgx, pgy, pgz, pl;
+                    mo_lane<T, 1>(S, sig, lane, ao, phi, pgx, pgy, pgz, pl);
 #pragma unroll
-                for (int k = 0; k < NM; ++k) {
-                    T d = D[k];
-                    tj += wshfl(phi, k) * d;
-                    if (MOVE == MOVE_ONE_DRIFT) { bx += wshfl(pgx, k) * d; by += wshfl(pgy, k) * d; bz += wshfl(pgz, k) * d; }
+                    for (int k = 0; k < NM; ++k) {
+                        T d = D[k];
+                        tj += wshfl(phi, k) * d;
+                        bx += wshfl(pgx, k) * d; by += wshfl(pgy, k) * d; bz += wshfl(pgz, k) * d;
+                    }
+                } else {
+                    const T* row = ph + q * PHS;
+                    T t0 = 0, t1 = 0;
+#pragma unroll
+                    for (int v = 0; v < (NM + 3) / 4; ++v) {
+                        T f0, f1, f2, f3;
+                        load4(row + 4 * v, f0, f1, f2, f3);
+                        if (4 * v + 0 < NM) t0 += f0 * D[4 * v + 0];
+                        if (4 * v + 1 < NM) t1 += f1 * D[4 * v + 1];
+                        if (4 * v + 2 < NM) t0 += f2 * D[4 * v + 2];
+                        if (4 * v + 3 < NM) t1 += f3 * D[4 * v + 3];
+                    }
+                    tj = t0 + t1;
                 }
                 const T R = wshfl(tj, q);
                 T g0[3], gn[3];
@@ -440,11 +534,13 @@ __global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__
     if (threadIdx.x == 0)
         args = SweepArgs<T>{gpos, gdinv, gsign, acc_out, flags, step0, seed, step, tau, maxd, W, Wcap, n_sweeps,
                             fixed_node};
+    extern __shared__ __align__(16) unsigned char wsm[];
     load_sysw(&S, Sg);                         // ends with a block barrier
     const int w = blockIdx.x * WPB + (threadIdx.x >> 5);
     if (w >= W) return;                        // whole warps only; no block barrier below
     const volatile SweepArgs<T>& a = args;
-    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w);
+    T* ph = reinterpret_cast<T*>(wsm) + (size_t)(threadIdx.x >> 5) * sweep_scratch_elems<NE, NUP>();
+    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w, ph);
 }
 
 // Batched form: TW / WPB blocks per (system, TW-walker tile), each sweeping
@@ -462,11 +558,13 @@ __global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restric
     if ((int)blockIdx.x >= ntiles * BPT) return;
     const BatchTile tl = tiles[blockIdx.x / BPT];
     if (threadIdx.x == 0) args = sweep_args<T>(recs[tl.rec], *ctl);
+    extern __shared__ __align__(16) unsigned char wsm[];
     load_sysw(&S, static_cast<const SysW<T>*>(recs[tl.rec].tab_s));   // ends with a block barrier
     const volatile SweepArgs<T>& a = args;
     const int w = tl.w0 + (int)(blockIdx.x % BPT) * WPB + (int)(threadIdx.x >> 5);
     if (w >= a.W) return;                      // whole warps only; no block barrier below
-    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w);
+    T* ph = reinterpret_cast<T*>(wsm) + (size_t)(threadIdx.x >> 5) * sweep_scratch_elems<NE, NUP>();
+    kw_sweep_walker<NE, NUP, NNUC, T, MOVE>(S, a, w, ph);
 }
 
 // Full evaluation from positions (refresh + E_L), one warp per walker.
@@ -747,6 +845,9 @@ struct WarpShapeOps {
     // refresh block of BTW warps (the wider refresh block shares the large
     // shared-memory table among more warps).
     static constexpr int BTW = 8;
+    // dynamic shared memory of a sweep block: the WPB warps' proposal rows
+    template <class T>
+    static constexpr size_t sweep_smem() { return sizeof(T) * WPB * (size_t)sweep_scratch_elems<NE, NUP>(); }
 
     template <class T>
     static int table(const HostSys& hs, const SysW<T>** out) {
@@ -860,9 +961,16 @@ struct WarpShapeOps {
         int rc = table<T>(hs, &S);
         if (rc) return rc;
         int nb = (dw.W + WPB - 1) / WPB;
-        kw_sweep<NE, NUP, NNUC, T, MOVE, WPB><<<nb, 32 * WPB, 0, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W,
-                                                                     dw.Wcap, n, s0, (T)step, (T)tau, (T)maxd, seed,
-                                                                     dw.acc, dw.flags, dw.fixed_node);
+        auto kern = kw_sweep<NE, NUP, NNUC, T, MOVE, WPB>;
+        const size_t smem = sweep_smem<T>();
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
+        kern<<<nb, 32 * WPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W, dw.Wcap, n, s0, (T)step, (T)tau,
+                                         (T)maxd, seed, dw.acc, dw.flags, dw.fixed_node);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }
@@ -892,9 +1000,16 @@ struct WarpShapeOps {
     template <class T, int MOVE>
     static int batch_sweep_t(const BatchClass& bc, const BatchCtl* ctl, cudaStream_t st, int* occ) {
         auto kern = kwb_sweep<NE, NUP, NNUC, T, MOVE, WPB, BTW>;
-        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, 0) == cudaSuccess ? 0 : 2;
+        const size_t smem = sweep_smem<T>();
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 2;
+            attr = true;
+        }
+        if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
         if (bc.ntiles == 0) return 0;
-        kern<<<bc.ntiles * (BTW / WPB), 32 * WPB, 0, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
+        kern<<<bc.ntiles * (BTW / WPB), 32 * WPB, smem, st>>>(bc.tiles, bc.ntiles, bc.recs, ctl);
         ++g_launch_count;
         return cudaGetLastError() == cudaSuccess ? 0 : 2;
     }

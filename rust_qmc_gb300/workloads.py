@@ -65,7 +65,7 @@ def run_dmc(a, ctx, sysh, prec):
         n_moves = 0
         for _ in range(a.sweeps):
             n_before = wk.W
-            n, em = wk.dmc_step(0.005, e_ref, seed=1, step=t, fp64_measure=True)
+            n, em = wk.dmc_step(0.005, e_ref, seed=1, step=t, fp64_measure=True, branch_cut=2.0 / np.sqrt(0.005))
             t += 1
             n_moves += n_before * sysh.N
             e_ref = em - 0.5 * np.log(n / W) / 0.005

@@ -34,3 +34,33 @@ def _fd(O, spec, r, h):
     grad = (l[:, :, 0] - l[:, :, 1]) / (2 * h)
     lap = np.sum(np.exp(l[:, :, 0] - base) + np.exp(l[:, :, 1] - base) - 2.0, axis=1) / (h * h)
     return grad, lap
+
+
+def autocorrelation_time(x):
+    """Integrated autocorrelation time by the initial positive sequence
+    (src/sampling/vmc.rs:141-163)."""
+    x = np.asarray(x, dtype=np.float64)
+    n = len(x)
+    m = x.mean()
+    v = ((x - m) ** 2).mean()
+    if n == 0 or v == 0.0:
+        return 1.0
+    tau = 1.0
+    for t in range(1, n // 2):
+        a = ((x[:-t] - m) * (x[t:] - m)).sum() / ((n - t) * v)
+        if a < 0:
+            break
+        tau += 2.0 * a
+    return tau
+
+
+def blocking_error(x):
+    """Blocking error with blocks of ceil(2 tau_int) (src/sampling/vmc.rs:166-188);
+    returns (error, number of blocks)."""
+    x = np.asarray(x, dtype=np.float64)
+    bs = max(1, int(np.ceil(2.0 * autocorrelation_time(x))))
+    nb = len(x) // bs
+    if nb < 2:
+        return 0.0, nb
+    m = x[: nb * bs].reshape(nb, bs).mean(axis=1)
+    return float(m.std(ddof=1) / np.sqrt(nb)), nb

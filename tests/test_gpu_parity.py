@@ -21,7 +21,7 @@ import pytest
 
 import rust_qmc_gb300 as Q
 from rust_qmc_gb300 import _lib as L
-from tests.helpers import random_configs
+from tests.helpers import blocking_error, random_configs
 
 pytestmark = pytest.mark.gpu
 
@@ -52,9 +52,17 @@ def assert_same_chain(got, want, margin, acc, acc_o, tol=1e-9):
 
 
 def assert_energies_agree(a, b, max_sigma):
-    """|E_a - E_b| < 4 sigma_combined, with sigma_combined below max_sigma."""
+    """Two runs of the same seed (FP64 and FP32+refine walkers from the same
+    initial configurations and the same Philox stream) sample correlated
+    chains; their per-measurement energy difference d_t = E_b,t - E_a,t has
+    its own blocking error sigma_d, far below either run's.  Asserts
+    |<d>| < 4 sigma_d with sigma_d below max_sigma (and at least 4 blocks),
+    and |E_a - E_b| < 4 sigma_combined of the two runs' own errors."""
+    d = np.asarray(b["energies"]) - np.asarray(a["energies"])
+    sig_d, nb = blocking_error(d)
+    assert nb >= 4 and 0 < sig_d < max_sigma, (sig_d, nb)
+    assert abs(d.mean()) < 4 * sig_d, (d.mean(), sig_d)
     sig = np.hypot(a["error"], b["error"])
-    assert 0 < sig < max_sigma, (a, b)
     assert abs(a["energy"] - b["energy"]) < 4 * sig, (a["energy"], b["energy"], sig)
 
 
@@ -266,21 +274,24 @@ def test_vmc_run_h2_box_moves(ctx):
     assert r["n_samples"] == 400
 
 
-@pytest.mark.parametrize("name", ["ch4_min", "c6h6", "heg"])
+@pytest.mark.parametrize("name", ["ch4_min", "c6h6", "c6h6_gto", "heg"])
 def test_vmc_run_precisions_agree(ctx, name):
-    """FP32+refine and FP64 chains (independent seeds) give statistically
-    indistinguishable energies: within 4 combined standard errors, with no
-    slack beyond the error bars, and runs long enough that the combined
-    error is below 5 mHa (CH4, the electron gas) or 15 mHa (benzene, whose
-    synthetic wave function has a large E_L variance)."""
-    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal, "heg": Q.electron_gas}[name]()
+    """FP32+refine and FP64 chains give statistically indistinguishable
+    energies: the paired energy difference of two same-seed runs within 4
+    of its blocking errors, no slack beyond the error bars.  The error caps
+    follow the E_L variance of each trial function (the synthetic benzene's
+    seeded MOs give E_L a standard deviation near 50 Ha; the electron gas
+    decorrelates over hundreds of sweeps): 2 mHa for CH4, 10 mHa for the
+    benzenes, 20 mHa for the electron gas."""
+    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal, "c6h6_gto": Q.benzene_gto,
+            "heg": Q.electron_gas}[name]()
     sysh = Q.System(ctx, spec)
-    W, n, burn, step, cap = {"ch4_min": (32768, 1024, 128, 0.3, 5e-3), "c6h6": (4096, 512, 64, 0.3, 15e-3),
-                             "heg": (2048, 512, 64, 1.0, 5e-3)}[name]
+    W, n, burn, step, cap = {"ch4_min": (65536, 2048, 128, 0.3, 2e-3), "c6h6": (8192, 1024, 64, 0.3, 10e-3),
+                             "c6h6_gto": (8192, 1024, 64, 0.3, 10e-3), "heg": (2048, 4096, 64, 0.5, 20e-3)}[name]
     res = {}
     for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
         res[prec] = Q.vmc_run(sysh, n_walkers=W, n_steps=n, n_burnin=burn, move_kind=L.QMC_MOVE_ONE_GAUSS,
-                              step=step, precision=prec, refresh_every=8, seed=11 + prec)
+                              step=step, precision=prec, refresh_every=8, seed=11)
     assert_energies_agree(res[L.QMC_FP64], res[L.QMC_FP32_REFINE], cap)
 
 
@@ -332,21 +343,48 @@ def test_dmc_run_h2_energy(ctx):
     assert 0.9 < d["acceptance_rate"] <= 1.0
 
 
-@pytest.mark.parametrize("name", ["ch4_min", "c6h6"])
+@pytest.mark.parametrize("name", ["h2", "c6h6_gto"])
 def test_dmc_precisions_agree(ctx, name):
-    """FP32+refine and FP64 DMC populations (independent seeds) give energies
-    within 4 combined standard errors, no slack beyond the error bars; the
-    FP32 form measures E_L in FP64-class arithmetic every 8 steps."""
-    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal}[name]()
+    """FP32+refine and FP64 DMC populations (same seed) give statistically
+    indistinguishable energies, no slack beyond the error bars; the FP32
+    form measures E_L in FP64-class arithmetic every 8 steps.  H2 runs the
+    reference's branching; the reference's benzene runs with the branching
+    energy clamped to E_ref +- 2/sqrt(tau) (qmc_run_params.branch_cut), which
+    keeps the population finite where its nodal E_L divergences otherwise
+    explode it."""
+    spec = {"h2": Q.h2_mo, "c6h6_gto": Q.benzene_gto}[name]()
     sysh = Q.System(ctx, spec)
-    W, n, burn, cap = {"ch4_min": (8192, 400, 100, 5e-3), "c6h6": (2048, 300, 100, 20e-3)}[name]
+    W, n, burn, cap, cut = {"h2": (8192, 1000, 200, 2e-3, 0.0),
+                            "c6h6_gto": (2048, 400, 200, 30e-3, 2.0 / np.sqrt(0.005))}[name]
     r = {}
     for prec in (L.QMC_FP64, L.QMC_FP32_REFINE):
         r[prec] = Q.dmc_run(sysh, n_walkers=W, n_steps=n, n_burnin=burn, tau=0.005, precision=prec,
-                            refresh_every=8, seed=5 + prec)
+                            refresh_every=8, seed=5, branch_cut=cut)
     a, b = r[L.QMC_FP64], r[L.QMC_FP32_REFINE]
     assert np.isfinite(a["energy"]) and np.isfinite(b["energy"])
+    assert 0.5 * W < a["avg_population"] < 2 * W and 0.5 * W < b["avg_population"] < 2 * W
     assert_energies_agree(a, b, cap)
+
+
+def test_fp64_dmc_population_with_branch_cut_matches_oracle(ctx, oracle):
+    """The clamped branching (branch_cut) on the device follows the oracle's
+    DMC with the same clamp population for population."""
+    spec = Q.methane_minimal()
+    sysh = Q.System(ctx, spec)
+    target, n_steps, tau, cut = 48, 6, 0.02, 1.5
+    wk = Q.Walkers(sysh, target, L.QMC_FP64, capacity=4 * target)
+    wk.init(seed=21)
+    e_ref = wk.refresh() / target
+    pos0 = wk.get_positions()
+    pops, ens, er = [], [], e_ref
+    for t in range(n_steps):
+        n, em = wk.dmc_step(tau, er, seed=77, step=t, fixed_node=True, branch_cut=cut)
+        pops.append(n)
+        ens.append(em)
+        er = em - 0.5 * np.log(n / target) / tau
+    _, pops_o, ens_o, _ = oracle.dmc(spec, pos0, n_steps, tau, e_ref, target, 77, fixed_node=True, branch_cut=cut)
+    assert list(pops) == list(pops_o)
+    np.testing.assert_allclose(ens, ens_o, rtol=1e-9, atol=1e-9)
 
 
 # ---------------------------------------------------------------------------
@@ -670,3 +708,35 @@ def test_benzene_distinct_parameters_fp32_refresh(ctx, oracle):
     assert np.max(np.abs(el - o["e_local"])) <= 1e-6
     assert rel(la, o["logabs"]) < 1e-10
     assert np.array_equal(sg, o["sign"])
+
+
+@pytest.mark.parametrize("name", ["ch4_min", "c6h6", "heg"])
+@pytest.mark.parametrize("move", [L.QMC_MOVE_ONE_GAUSS, L.QMC_MOVE_ONE_DRIFT])
+def test_fp32_sweep_decisions_match_oracle(ctx, oracle, name, move):
+    """Per-configuration check of the FP32 moving path: FP32 walkers and the
+    oracle's FP64 reference algorithm start from the same (float-valued)
+    configurations and draw the same proposals.  After one sweep every walker
+    whose oracle run kept each acceptance decision more than 1e-3 (relative)
+    away from its threshold must have taken exactly the oracle's decisions,
+    i.e. the FP32 ratio psi'/psi (and, for drift moves, the Green's-function
+    factor of the FP32 drift) is within 1e-3 of the FP64 one at every such
+    proposal; its positions agree to 2e-5 bohr, which for drift-diffusion
+    moves bounds the FP32 drift error by 2e-5 / (2 tau) per accepted move.
+    The few walkers with a decision inside the 1e-3 band may differ."""
+    spec = {"ch4_min": Q.methane_minimal, "c6h6": Q.benzene_minimal, "heg": Q.electron_gas}[name]()
+    sysh = Q.System(ctx, spec)
+    W = 256
+    step, tau = (1.0, 0.05) if name == "heg" else (0.3, 0.02)
+    wk = Q.Walkers(sysh, W, L.QMC_FP32_REFINE)
+    wk.init(seed=61)
+    wk.refresh()
+    pos0 = wk.get_positions()                      # float values
+    acc = wk.sweep(move, 1, 4, seed=909, step=step, tau=tau, max_drift=1.0)
+    got = wk.get_positions()
+    want, acc_o, _, mg = oracle.sweeps(spec, pos0, 1, 4, move, 909, step=step, tau=tau, max_drift=1.0,
+                                       want_energy=False, want_margin=True)
+    same = np.all(np.abs(got - want) < 2e-5, axis=(1, 2))
+    unexplained = ~same & (mg > 1e-3)
+    assert not unexplained.any(), (np.where(unexplained)[0], mg[unexplained])
+    assert same.mean() > 0.9, same.mean()
+    assert acc > 0

@@ -43,7 +43,7 @@ def test_mcmc_step_adaptation_replays_reference_rule(ctx):
         if t >= burn:
             series.append(wk.state()[2].mean())
         if (t + 1) % iv == 0:
-            step = mcmc_rule(step, window / float(W), 0.5, 0.1, 3.0)
+            step = mcmc_rule(step, window / float(iv * W), 0.5, 0.1, 3.0)
             steps.append(step)
             window = 0
     assert len(set(np.round(steps, 12))) > 1                  # the step really moved

@@ -38,7 +38,7 @@ struct SysW {
     // centre and primitives of the previous AO (p_y and p_z after p_x share its radial part)
     int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];
     T pexp[WMAX_PRIM], pcoef[WMAX_PRIM];
-    T C[2][WMAX_AO][WNCOL];     // [sector][AO][column]
+    alignas(16) T C[2][WMAX_AO][WNCOL];     // [sector][AO][column]; 16-byte rows of 4 columns read as vectors
     T init_sigma;
     int init_nuc[64];           // internal electron order
     int perm[64];
@@ -196,11 +196,21 @@ __device__ __forceinline__ void store4(double* p, double a, double b, double c, 
     reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
 }
 
+// Jastrow cache of the Gaussian sweep: u(r_ij) of every electron pair i < j
+// at slot j (j - 1) / 2 + i, then the one-body sum U1_i = sum_I A_I Z_I r/(1 + B_I r)
+// of every electron, rounded up to 4 elements.
+template <int NE>
+__host__ __device__ constexpr int jcache_elems() { return (NE * (NE - 1) / 2 + NE + 3) / 4 * 4; }
+__device__ __forceinline__ int pair_slot(int i, int j) {
+    const int a = i < j ? i : j, b = i < j ? j : i;
+    return b * (b - 1) / 2 + a;
+}
+
 // Elements of the per-warp scratch of the single-electron sweep: one row of
-// WNCOL orbital values per proposal of a sector.
+// WNCOL orbital values per proposal of a sector, then the Jastrow cache.
 template <int NE, int NUP>
 __host__ __device__ constexpr int sweep_scratch_elems() {
-    return (NUP > NE - NUP ? NUP : NE - NUP) * WNCOL;
+    return (NUP > NE - NUP ? NUP : NE - NUP) * WNCOL + jcache_elems<NE>();
 }
 
 // MO contraction: lane k receives phi_k = sum_a C[sig][a][k] chi_a (and
@@ -350,7 +360,12 @@ __device__ __forceinline__ void proposal_orbitals(const SysW<T>& S, int sig, T x
         const T chi = (type == 0 ? T(1) : (type == 1 ? dx : (type == 2 ? dy : dz))) * s0;
         const T* c = S.C[sig][a];
 #pragma unroll
-        for (int k = 0; k < 4 * NV; ++k) acc[k] += c[k] * chi;
+        for (int v = 0; v < NV; ++v) {
+            T c0, c1, c2, c3;
+            load4(c + 4 * v, c0, c1, c2, c3);
+            acc[4 * v + 0] += c0 * chi; acc[4 * v + 1] += c1 * chi;
+            acc[4 * v + 2] += c2 * chi; acc[4 * v + 3] += c3 * chi;
+        }
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) store4(out + 4 * v, acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
@@ -388,6 +403,41 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
     int sgn = a.sign[w];
     unsigned acc = 0;
     int flg = 0;
+    // Gaussian moves keep every pair term and every one-body sum in the
+    // warp's cache (jc), so a proposal evaluates only the moving electron's
+    // new terms; a cached term is the same expression on the same squared
+    // distance as a recomputation, hence the same value.
+    constexpr int NPAIR = NE * (NE - 1) / 2;
+    T* jc = ph + NM * PHS;
+    if constexpr (MOVE == MOVE_ONE_GAUSS) {
+        for (int i = 0; i < NE; ++i) {
+            T xi, yi, zi;
+            P.get(i, xi, yi, zi);
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int j = lane + 32 * r;
+                if (j < NE && j > i) {
+                    T dx = xi - (r ? P.x[1] : P.x[0]), dy = yi - (r ? P.y[1] : P.y[0]), dz = zi - (r ? P.z[1] : P.z[0]);
+                    T d, ri, uu, upr, lt;
+                    dist(dx * dx + dy * dy + dz * dz, d, ri);
+                    const int c = ((j < NUP) == (i < NUP)) ? 1 : 0;
+                    pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+                    jc[pair_slot(i, j)] = uu;
+                }
+            }
+            T en = 0;
+            if (lane < NNUC) {
+                T dx = xi - S.nuc[lane][0], dy = yi - S.nuc[lane][1], dz = zi - S.nuc[lane][2];
+                T d, ri, uu, upr, lt;
+                dist(dx * dx + dy * dy + dz * dz, d, ri);
+                pade_ab(S.enA[lane], S.enB[lane], d, ri, uu, upr, lt);
+                en = uu;
+            }
+            en = wsum(en);
+            if (lane == 0) jc[NPAIR + i] = en;
+        }
+        __syncwarp();
+    }
     for (int it = 0; it < a.n_sweeps; ++it) {
         const uint64_t st = a.step0 + (uint64_t)it;
 #pragma unroll
@@ -465,8 +515,35 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 }
                 const T R = wshfl(tj, q);
                 T g0[3], gn[3];
-                T du = wjastrow_delta<NE, NUP, NNUC, T, MOVE == MOVE_ONE_DRIFT>(S, P, lane, e, rx, ry, rz, nx, ny, nz,
-                                                                               g0, gn);
+                T du, unew[2] = {T(0), T(0)}, enn = 0;
+                if constexpr (MOVE == MOVE_ONE_GAUSS) {
+                    // new terms of the moving electron against the cached old ones
+                    T ds = 0;
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        const int j = lane + 32 * r;
+                        if (j < NE && j != e) {
+                            T dx = nx - (r ? P.x[1] : P.x[0]), dy = ny - (r ? P.y[1] : P.y[0]);
+                            T dz = nz - (r ? P.z[1] : P.z[0]);
+                            T d, ri, uu, upr, lt;
+                            dist(dx * dx + dy * dy + dz * dz, d, ri);
+                            const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
+                            pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+                            unew[r] = uu;
+                            ds += uu - jc[pair_slot(e, j)];
+                        }
+                    }
+                    if (lane < NNUC) {
+                        T dx = nx - S.nuc[lane][0], dy = ny - S.nuc[lane][1], dz = nz - S.nuc[lane][2];
+                        T d, ri, uu, upr, lt;
+                        dist(dx * dx + dy * dy + dz * dz, d, ri);
+                        pade_ab(S.enA[lane], S.enB[lane], d, ri, uu, upr, lt);
+                        enn = uu;
+                    }
+                    du = wsum(ds - enn) + jc[NPAIR + e];
+                } else {
+                    du = wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, nx, ny, nz, g0, gn);
+                }
                 if (MOVE == MOVE_ONE_DRIFT) {
                     bx = wshfl(bx, q); by = wshfl(by, q); bz = wshfl(bz, q);
                     const T tau = a.tau, maxd = a.maxd;
@@ -498,7 +575,17 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     }
                     if (R < 0) sgn = -sgn;
                     ++acc;
+                    if constexpr (MOVE == MOVE_ONE_GAUSS) {
+#pragma unroll
+                        for (int r = 0; r < 2; ++r) {
+                            const int j = lane + 32 * r;
+                            if (j < NE && j != e) jc[pair_slot(e, j)] = unew[r];
+                        }
+                        const T u1 = wsum(enn);
+                        if (lane == 0) jc[NPAIR + e] = u1;
+                    }
                 }
+                __syncwarp();                      // cache writes before the next proposal's reads
             }
         }
     }

@@ -412,6 +412,7 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, A& a, typenam
             const T kx = S.kvec[sig][lane][0], ky = S.kvec[sig][lane][1], kz = S.kvec[sig][lane][2];
             static_assert(NUP <= 32 && NE - NUP <= 32, "one lane per sector electron");
             const MoveDraw<T> draws = sector_draws<T>(a.seed, (uint32_t)w, st, sig * NUP, NS, lane);
+            T csr = 1, csi = 0;                        // pending complex scale of this lane's column (Gaussian moves)
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
@@ -500,17 +501,41 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, A& a, typenam
                     // complex Sherman-Morrison: D'[k][l] = D[k][l] - D[k][q] t_l / R, D'[k][q] = D[k][q] / R
                     const T iR2 = T(1) / R2;
                     const T iRr = Rr * iR2, iRi = -Ri * iR2;              // 1/R
-                    const T fr = tr * iRr - ti * iRi, fi = tr * iRi + ti * iRr;   // t_l / R
+                    T fr = tr * iRr - ti * iRi, fi = tr * iRi + ti * iRr;   // t_l / R
+                    if constexpr (MOVE == MOVE_ONE_GAUSS) {
+                        // column q keeps its values and takes the factor 1/R when the
+                        // sector ends (a column's scale is 1 until its own electron
+                        // moves, so t_q and R are read unscaled)
+                        if (lane == q) { fr = 0; fi = 0; csr = iRr; csi = iRi; }
 #pragma unroll 9
-                    for (int k = 0; k < NM; ++k) {
-                        const C2 d = Dc[k * 32];
-                        T qr = __shfl_sync(0xffffffffu, d.x, q), qi = __shfl_sync(0xffffffffu, d.y, q);
-                        C2 n;
-                        if (lane == q) { n.x = qr * iRr - qi * iRi; n.y = qr * iRi + qi * iRr; }
-                        else { n.x = d.x - (qr * fr - qi * fi); n.y = d.y - (qr * fi + qi * fr); }
-                        Dc[k * 32] = n;
+                        for (int k = 0; k < NM; ++k) {
+                            const C2 d = Dc[k * 32];
+                            T qr = __shfl_sync(0xffffffffu, d.x, q), qi = __shfl_sync(0xffffffffu, d.y, q);
+                            C2 n;
+                            n.x = d.x - (qr * fr - qi * fi); n.y = d.y - (qr * fi + qi * fr);
+                            Dc[k * 32] = n;
+                        }
+                    } else {
+#pragma unroll 9
+                        for (int k = 0; k < NM; ++k) {
+                            const C2 d = Dc[k * 32];
+                            T qr = __shfl_sync(0xffffffffu, d.x, q), qi = __shfl_sync(0xffffffffu, d.y, q);
+                            C2 n;
+                            if (lane == q) { n.x = qr * iRr - qi * iRi; n.y = qr * iRi + qi * iRr; }
+                            else { n.x = d.x - (qr * fr - qi * fi); n.y = d.y - (qr * fi + qi * fr); }
+                            Dc[k * 32] = n;
+                        }
                     }
                     ++acc;
+                }
+            }
+            if constexpr (MOVE == MOVE_ONE_GAUSS) {
+#pragma unroll 9
+                for (int k = 0; k < NM; ++k) {
+                    const C2 d = Dc[k * 32];
+                    C2 n;
+                    n.x = d.x * csr - d.y * csi; n.y = d.x * csi + d.y * csr;
+                    Dc[k * 32] = n;
                 }
             }
         }
@@ -540,7 +565,7 @@ __device__ __forceinline__ void khw_sweep_walker(const SysH<T>& S, A& a, typenam
 template <int NE, int NUP, class T, int MOVE, int WPB>
 // 16 warps per SM for FP32 walkers (four blocks of four: 56 KB of shared
 // memory each, at most 128 registers), 8 for FP64 walkers.
-__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
+__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 16 : 8) / WPB) khw_sweep(const SysH<T>* __restrict__ Sg, T* __restrict__ gpos,
                                                       T* __restrict__ gdinv, int W, int Wcap, int n_sweeps,
                                                       uint64_t step0, T step, T tau, T maxd, uint64_t seed,
                                                       unsigned long long* acc_out, int* flags) {
@@ -561,7 +586,7 @@ __global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khw
 // Batched form: one block per (system, WPB-walker tile); the hardware block
 // scheduler balances uneven systems and classes that run side by side.
 template <int NE, int NUP, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 12 : 8) / WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+__global__ void __launch_bounds__(32 * WPB, (sizeof(T) == 4 ? 16 : 8) / WPB) khwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                        const BatchRec* __restrict__ recs,
                                                        const BatchCtl* __restrict__ ctl) {
     constexpr int NM = NUP > NE - NUP ? NUP : NE - NUP;
@@ -1128,6 +1153,7 @@ struct HegShapeOps {
         if (!attr) {
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
                 return 2;
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
             attr = true;
         }
         if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, 32 * WPB, smem) == cudaSuccess ? 0 : 2;
@@ -1251,6 +1277,7 @@ struct HegShapeOps {
         if (!attr) {
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
                 return 2;
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
             attr = true;
         }
         kern<<<nb, 32 * WPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.W, dw.Wcap, n, s0, (T)step, (T)tau, (T)maxd,

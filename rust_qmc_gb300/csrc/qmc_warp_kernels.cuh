@@ -25,6 +25,14 @@ constexpr int AO_REP = 16;        // ao_type flag: radial part equal to the prev
 constexpr int WMAX_PRIM = 256;
 constexpr int WMAX_NUC = 16;
 
+// Radial-group descriptor: nucleus (bits 0-3), kind (bit 4: 0 s, 1 p triplet),
+// primitive count (bits 5-8), first primitive (bits 9-16), first AO (bits 17-23).
+__host__ __device__ constexpr int grp_pack(int nuc, int kind, int np, int p0, int a0) {
+    return nuc | (kind << 4) | (np << 5) | (p0 << 9) | (a0 << 17);
+}
+__host__ __device__ constexpr int grp_a0(int g) { return (g >> 17) & 127; }
+static_assert(WMAX_NUC <= 16 && WMAX_PRIM <= 256 && WMAX_AO <= 128, "group descriptor fields");
+
 // Shared-memory system table of the warp kernels (one copy per block).
 template <class T>
 struct SysW {
@@ -37,7 +45,11 @@ struct SysW {
     // ao_type: bits 0-3 the kind (0 s, 1..3 p_x..p_z); AO_REP set when the AO has the
     // centre and primitives of the previous AO (p_y and p_z after p_x share its radial part)
     int ao_nuc[WMAX_AO], ao_type[WMAX_AO], ao_p0[WMAX_AO], ao_np[WMAX_AO];
-    T pexp[WMAX_PRIM], pcoef[WMAX_PRIM];
+    // radial groups in AO order: an s AO alone, or a p triplet sharing one
+    // radial part; packed by grp_pack (nucleus, kind, primitives, first AO)
+    int n_grp;
+    int grp[WMAX_AO];
+    alignas(16) T prim[WMAX_PRIM][2];   // (exponent, coefficient) of every primitive
     alignas(16) T C[2][WMAX_AO][WNCOL];     // [sector][AO][column]; 16-byte rows of 4 columns read as vectors
     T init_sigma;
     int init_nuc[64];           // internal electron order
@@ -70,21 +82,30 @@ static bool fill_sysw(const HostSys& hs, int NE, int NUP, int NNUC, SysW<T>& S) 
     for (const HostShell& sh : hs.shells) {
         auto put = [&](int caller_ao, int type, const std::vector<double>& coef) -> bool {
             int a = hs.ao_int[caller_ao];
-            if ((int)(np + sh.exps.size()) > WMAX_PRIM) return false;
+            if ((int)(np + sh.exps.size()) > WMAX_PRIM || sh.exps.size() > 15) return false;
             S.ao_nuc[a] = sh.nuc;
             S.ao_type[a] = type;
             S.ao_p0[a] = np;
             S.ao_np[a] = (int)sh.exps.size();
-            for (size_t p = 0; p < sh.exps.size(); ++p) { S.pexp[np] = (T)sh.exps[p]; S.pcoef[np] = (T)coef[p]; ++np; }
+            for (size_t p = 0; p < sh.exps.size(); ++p) { S.prim[np][0] = (T)sh.exps[p]; S.prim[np][1] = (T)coef[p]; ++np; }
             return true;
         };
-        for (int k = 0; k < 2; ++k)
-            if (sh.s_ao[k] >= 0 && !put(sh.s_ao[k], 0, sh.s_coef[k])) return false;
+        for (int k = 0; k < 2; ++k) {
+            if (sh.s_ao[k] < 0) continue;
+            const int p0 = np;
+            if (!put(sh.s_ao[k], 0, sh.s_coef[k])) return false;
+            S.grp[S.n_grp++] = grp_pack(sh.nuc, 0, (int)sh.exps.size(), p0, hs.ao_int[sh.s_ao[k]]);
+        }
         // the p triplet's members are consecutive in the internal order and share
         // one radial part: p_y and p_z reuse p_x's
-        if (sh.p_ao[0] >= 0)
-            for (int m = 0; m < 3; ++m)
+        if (sh.p_ao[0] >= 0) {
+            const int p0 = np, a0 = hs.ao_int[sh.p_ao[0]];
+            for (int m = 0; m < 3; ++m) {
+                if (hs.ao_int[sh.p_ao[m]] != a0 + m) return false;
                 if (!put(sh.p_ao[m], (1 + m) | (m > 0 ? AO_REP : 0), sh.p_coef)) return false;
+            }
+            S.grp[S.n_grp++] = grp_pack(sh.nuc, 1, (int)sh.exps.size(), p0, a0);
+        }
     }
     std::vector<double> Ce = hs.effective_mo();
     for (int sig = 0; sig < 2; ++sig) {
@@ -119,6 +140,18 @@ __device__ __forceinline__ void load_sysw(SysW<T>* dst, const SysW<T>* __restric
     __syncthreads();
 }
 
+// (exponent, coefficient) pair of a primitive: one 8- or 16-byte shared load.
+template <class T>
+__device__ __forceinline__ void load2(const T (&p)[2], T& a, T& b) { a = p[0]; b = p[1]; }
+__device__ __forceinline__ void load2(const float (&p)[2], float& a, float& b) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    a = v.x; b = v.y;
+}
+__device__ __forceinline__ void load2(const double (&p)[2], double& a, double& b) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    a = v.x; b = v.y;
+}
+
 // ---------------------------------------------------------------------------
 // Lane-parallel AO evaluation: lane l evaluates AO l + 32 r in round r at
 // point (x,y,z): value, gradient, Laplacian (MODE >= 1 / 2).  Rounds past the
@@ -141,8 +174,9 @@ __device__ __forceinline__ void ao_lane(const SysW<T>& S, T x, T y, T z, int lan
             T r2 = dx * dx + dy * dy + dz * dz;
             T s0 = 0, s1 = 0, s2 = 0;
             for (int p = p0; p < p0 + np; ++p) {
-                T al = S.pexp[p];
-                T e = S.pcoef[p] * fexp(-al * r2);
+                T al, cp;
+                load2(S.prim[p], al, cp);
+                T e = cp * fexp(-al * r2);
                 s0 += e;
                 if (MODE >= 1) s1 += al * e;
                 if (MODE >= 2) s2 += al * al * e;
@@ -337,38 +371,54 @@ __device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, N
 // elements, so that rows start 16-byte aligned and read as vectors).
 constexpr int PHS = WNCOL;
 
-// Orbital values phi_k(x, y, z), k < NM, of sector sig by one lane: every AO
-// in turn (its radial part reused across a p triplet), accumulated into the
-// table's columns (broadcast reads: every lane reads the same coefficients);
-// written to out[k] as vectors.
+// acc[k] += c[k] chi for k < NM: coefficient rows are read as 16-byte vectors
+// (NM / 4 of them) and NM % 4 scalars, so no padding column is multiplied.
+template <class T, int NM>
+__device__ __forceinline__ void row_axpy(const T* c, T chi, T (&acc)[NM]) {
+#pragma unroll
+    for (int v = 0; v < NM / 4; ++v) {
+        T c0, c1, c2, c3;
+        load4(c + 4 * v, c0, c1, c2, c3);
+        acc[4 * v + 0] += c0 * chi; acc[4 * v + 1] += c1 * chi;
+        acc[4 * v + 2] += c2 * chi; acc[4 * v + 3] += c3 * chi;
+    }
+#pragma unroll
+    for (int k = 4 * (NM / 4); k < NM; ++k) acc[k] += c[k] * chi;
+}
+
+// Orbital values phi_k(x, y, z), k < NM, of sector sig by one lane: one pass
+// over the radial groups (an s AO, or a p triplet sharing its radial part),
+// each contracted into the table's columns (broadcast reads: every lane reads
+// the same coefficients); written to out[k].
 template <class T, int NM>
 __device__ __forceinline__ void proposal_orbitals(const SysW<T>& S, int sig, T x, T y, T z, T* out) {
-    constexpr int NV = (NM + 3) / 4;
-    T acc[4 * NV];
+    T acc[NM];
 #pragma unroll
-    for (int k = 0; k < 4 * NV; ++k) acc[k] = 0;
-    T s0 = 0, dx = 0, dy = 0, dz = 0;
-    for (int a = 0; a < S.n_ao; ++a) {
-        const int tf = S.ao_type[a], type = tf & 15;
-        if (!(tf & AO_REP)) {
-            const int I = S.ao_nuc[a], p0 = S.ao_p0[a], np = S.ao_np[a];
-            dx = x - S.nuc[I][0]; dy = y - S.nuc[I][1]; dz = z - S.nuc[I][2];
-            const T r2 = dx * dx + dy * dy + dz * dz;
-            s0 = 0;
-            for (int p = p0; p < p0 + np; ++p) s0 += S.pcoef[p] * fexp(-S.pexp[p] * r2);
+    for (int k = 0; k < NM; ++k) acc[k] = 0;
+    for (int g = 0; g < S.n_grp; ++g) {
+        const int d = S.grp[g];
+        const int I = d & 15, kind = (d >> 4) & 1, np = (d >> 5) & 15, p0 = (d >> 9) & 255, a0 = grp_a0(d);
+        const T dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+        const T r2 = dx * dx + dy * dy + dz * dz;
+        T s0 = 0;
+        for (int p = p0; p < p0 + np; ++p) {
+            T al, cp;
+            load2(S.prim[p], al, cp);
+            s0 += cp * fexp(-al * r2);
         }
-        const T chi = (type == 0 ? T(1) : (type == 1 ? dx : (type == 2 ? dy : dz))) * s0;
-        const T* c = S.C[sig][a];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            T c0, c1, c2, c3;
-            load4(c + 4 * v, c0, c1, c2, c3);
-            acc[4 * v + 0] += c0 * chi; acc[4 * v + 1] += c1 * chi;
-            acc[4 * v + 2] += c2 * chi; acc[4 * v + 3] += c3 * chi;
+        const T* c = S.C[sig][a0];
+        if (kind == 0) {
+            row_axpy<T, NM>(c, s0, acc);
+        } else {
+            row_axpy<T, NM>(c, dx * s0, acc);
+            row_axpy<T, NM>(c + WNCOL, dy * s0, acc);
+            row_axpy<T, NM>(c + 2 * WNCOL, dz * s0, acc);
         }
     }
 #pragma unroll
-    for (int v = 0; v < NV; ++v) store4(out + 4 * v, acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+    for (int v = 0; v < NM / 4; ++v) store4(out + 4 * v, acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+#pragma unroll
+    for (int k = 4 * (NM / 4); k < NM; ++k) out[k] = acc[k];
 }
 
 // Single-electron sweeps, one warp per walker, WPB walkers per block.  A is
@@ -384,6 +434,8 @@ template <int NE, int NUP, int NNUC, class T, int MOVE, class A>
 __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T* ph) {
     constexpr int NDN = NE - NUP;
     constexpr int NM = NUP > NDN ? NUP : NDN;
+    constexpr int NE1 = NE > 32 ? NE - 32 : 0;   // partner electrons of the second round
+    static_assert(NE <= 64 && NE1 + NNUC <= 32, "second round: electrons 32.. and the nuclei share the lanes");
     const int lane = threadIdx.x & 31;
     LanePos<T, NE> P;
 #pragma unroll
@@ -456,6 +508,7 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 if (lane < NS) proposal_orbitals<T, NM>(S, sig, pnx, pny, pnz, ph + lane * PHS);
                 __syncwarp();
             }
+            T csc = 1;                                 // pending scale of this lane's column (Gaussian moves)
             for (int q = 0; q < NS; ++q) {
                 const int e = sig * NUP + q;
                 T rx, ry, rz;
@@ -517,34 +570,44 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 T g0[3], gn[3];
                 T du, unew[2] = {T(0), T(0)}, enn = 0;
                 if constexpr (MOVE == MOVE_ONE_GAUSS) {
-                    // new terms of the moving electron against the cached old ones
+                    // new terms of the moving electron against the cached old
+                    // ones: partner electron `lane` in the first round; in the
+                    // second, partner electron 32 + lane on lanes < NE1 and
+                    // nucleus lane - NE1 on the next NNUC lanes
                     T ds = 0;
-#pragma unroll
-                    for (int r = 0; r < 2; ++r) {
-                        const int j = lane + 32 * r;
+                    {
+                        const int j = lane;
                         if (j < NE && j != e) {
-                            T dx = nx - (r ? P.x[1] : P.x[0]), dy = ny - (r ? P.y[1] : P.y[0]);
-                            T dz = nz - (r ? P.z[1] : P.z[0]);
+                            T dx = nx - P.x[0], dy = ny - P.y[0], dz = nz - P.z[0];
                             T d, ri, uu, upr, lt;
                             dist(dx * dx + dy * dy + dz * dz, d, ri);
                             const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
                             pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
-                            unew[r] = uu;
-                            ds += uu - jc[pair_slot(e, j)];
+                            unew[0] = uu;
+                            ds = uu - jc[pair_slot(e, j)];
                         }
                     }
-                    if (lane < NNUC) {
-                        T dx = nx - S.nuc[lane][0], dy = ny - S.nuc[lane][1], dz = nz - S.nuc[lane][2];
-                        T d, ri, uu, upr, lt;
-                        dist(dx * dx + dy * dy + dz * dz, d, ri);
-                        pade_ab(S.enA[lane], S.enB[lane], d, ri, uu, upr, lt);
-                        enn = uu;
+                    {
+                        const bool is_el = lane < NE1, is_nuc = !is_el && lane - NE1 < NNUC;
+                        const int j = 32 + lane, I = is_nuc ? lane - NE1 : 0;
+                        if ((is_el && j != e) || is_nuc) {
+                            const T ox = is_el ? P.x[1] : S.nuc[I][0], oy = is_el ? P.y[1] : S.nuc[I][1];
+                            const T oz = is_el ? P.z[1] : S.nuc[I][2];
+                            const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
+                            const T pa = is_el ? S.a_ee[c] : S.enA[I], pb = is_el ? S.b_ee[c] : S.enB[I];
+                            T dx = nx - ox, dy = ny - oy, dz = nz - oz;
+                            T d, ri, uu, upr, lt;
+                            dist(dx * dx + dy * dy + dz * dz, d, ri);
+                            pade_ab(pa, pb, d, ri, uu, upr, lt);
+                            if (is_el) { unew[1] = uu; ds += uu - jc[pair_slot(e, j)]; }
+                            else { enn = uu; ds -= uu; }
+                        }
                     }
-                    du = wsum(ds - enn) + jc[NPAIR + e];
+                    du = wsum(ds) + jc[NPAIR + e];
                 } else {
                     du = wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, nx, ny, nz, g0, gn);
                 }
-                if (MOVE == MOVE_ONE_DRIFT) {
+                if constexpr (MOVE == MOVE_ONE_DRIFT) {
                     bx = wshfl(bx, q); by = wshfl(by, q); bz = wshfl(bz, q);
                     const T tau = a.tau, maxd = a.maxd;
                     T iR = R != T(0) ? T(1) / R : T(0);
@@ -567,25 +630,37 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                         else { P.x[1] = nx; P.y[1] = ny; P.z[1] = nz; }
                     }
                     const T iR = T(1) / R;
-                    const T f = tj * iR;
+                    if constexpr (MOVE == MOVE_ONE_GAUSS) {
+                        // column q keeps its values and takes the factor 1/R,
+                        // applied when the sector ends (every column's scale is
+                        // 1 until its own electron moves, so t_q and R are read
+                        // unscaled); the others take t_j / R times column q
+                        const T f = lane == q ? T(0) : tj * iR;
+                        if (lane == q) csc = iR;
 #pragma unroll
-                    for (int k = 0; k < NM; ++k) {
-                        T dq = wshfl(D[k], q);
-                        D[k] = (lane == q) ? dq * iR : D[k] - dq * f;
+                        for (int k = 0; k < NM; ++k) D[k] -= wshfl(D[k], q) * f;
+                    } else {
+                        const T f = tj * iR;
+#pragma unroll
+                        for (int k = 0; k < NM; ++k) {
+                            T dq = wshfl(D[k], q);
+                            D[k] = (lane == q) ? dq * iR : D[k] - dq * f;
+                        }
                     }
                     if (R < 0) sgn = -sgn;
                     ++acc;
                     if constexpr (MOVE == MOVE_ONE_GAUSS) {
-#pragma unroll
-                        for (int r = 0; r < 2; ++r) {
-                            const int j = lane + 32 * r;
-                            if (j < NE && j != e) jc[pair_slot(e, j)] = unew[r];
-                        }
+                        if (lane < NE && lane != e) jc[pair_slot(e, lane)] = unew[0];
+                        if (lane < NE1 && 32 + lane != e) jc[pair_slot(e, 32 + lane)] = unew[1];
                         const T u1 = wsum(enn);
                         if (lane == 0) jc[NPAIR + e] = u1;
                     }
                 }
                 __syncwarp();                      // cache writes before the next proposal's reads
+            }
+            if constexpr (MOVE == MOVE_ONE_GAUSS) {
+#pragma unroll
+                for (int k = 0; k < NM; ++k) D[k] *= csc;
             }
         }
     }
@@ -610,8 +685,9 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
     }
 }
 
+// FP32: four 4-walker blocks per SM (<= 128 registers)
 template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB>
-__global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__ Sg, T* __restrict__ gpos,
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == 4 ? 16 / WPB : 1) kw_sweep(const SysW<T>* __restrict__ Sg, T* __restrict__ gpos,
                                                      T* __restrict__ gdinv, int* __restrict__ gsign, int W, int Wcap,
                                                      int n_sweeps, uint64_t step0, T step, T tau, T maxd,
                                                      uint64_t seed, unsigned long long* acc_out, int* flags,
@@ -635,7 +711,7 @@ __global__ void __launch_bounds__(32 * WPB) kw_sweep(const SysW<T>* __restrict__
 // and classes that run side by side, and the kernel carries no tile-loop
 // state into the walker's registers.
 template <int NE, int NUP, int NNUC, class T, int MOVE, int WPB, int TW>
-__global__ void __launch_bounds__(32 * WPB) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == 4 ? 16 / WPB : 1) kwb_sweep(const BatchTile* __restrict__ tiles, int ntiles,
                                                       const BatchRec* __restrict__ recs,
                                                       const BatchCtl* __restrict__ ctl) {
     static_assert(TW % WPB == 0, "a tile splits into whole blocks");

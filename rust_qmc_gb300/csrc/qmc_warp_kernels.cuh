@@ -574,34 +574,37 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     // ones: partner electron `lane` in the first round; in the
                     // second, partner electron 32 + lane on lanes < NE1 and
                     // nucleus lane - NE1 on the next NNUC lanes
-                    T ds = 0;
+                    // Every lane evaluates its terms and the unused ones are
+                    // masked out (no divergent branch; the masked lanes read a
+                    // valid cache slot and may compute non-finite values).
+                    T ds;
                     {
-                        const int j = lane;
-                        if (j < NE && j != e) {
-                            T dx = nx - P.x[0], dy = ny - P.y[0], dz = nz - P.z[0];
-                            T d, ri, uu, upr, lt;
-                            dist(dx * dx + dy * dy + dz * dz, d, ri);
-                            const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
-                            pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
-                            unew[0] = uu;
-                            ds = uu - jc[pair_slot(e, j)];
-                        }
+                        const int j = lane < NE ? lane : NE - 1;
+                        T dx = nx - P.x[0], dy = ny - P.y[0], dz = nz - P.z[0];
+                        T d, ri, uu, upr, lt;
+                        dist(dx * dx + dy * dy + dz * dz, d, ri);
+                        const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
+                        pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+                        unew[0] = uu;
+                        const T old = jc[pair_slot(e, j)];
+                        ds = (lane < NE && lane != e) ? uu - old : T(0);
                     }
                     {
                         const bool is_el = lane < NE1, is_nuc = !is_el && lane - NE1 < NNUC;
-                        const int j = 32 + lane, I = is_nuc ? lane - NE1 : 0;
-                        if ((is_el && j != e) || is_nuc) {
-                            const T ox = is_el ? P.x[1] : S.nuc[I][0], oy = is_el ? P.y[1] : S.nuc[I][1];
-                            const T oz = is_el ? P.z[1] : S.nuc[I][2];
-                            const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
-                            const T pa = is_el ? S.a_ee[c] : S.enA[I], pb = is_el ? S.b_ee[c] : S.enB[I];
-                            T dx = nx - ox, dy = ny - oy, dz = nz - oz;
-                            T d, ri, uu, upr, lt;
-                            dist(dx * dx + dy * dy + dz * dz, d, ri);
-                            pade_ab(pa, pb, d, ri, uu, upr, lt);
-                            if (is_el) { unew[1] = uu; ds += uu - jc[pair_slot(e, j)]; }
-                            else { enn = uu; ds -= uu; }
-                        }
+                        const int j = is_el ? 32 + lane : 0, I = is_nuc ? lane - NE1 : 0;
+                        const T ox = is_el ? P.x[1] : S.nuc[I][0], oy = is_el ? P.y[1] : S.nuc[I][1];
+                        const T oz = is_el ? P.z[1] : S.nuc[I][2];
+                        const int c = ((j < NUP) == (e < NUP)) ? 1 : 0;
+                        const T pa = is_el ? S.a_ee[c] : S.enA[I], pb = is_el ? S.b_ee[c] : S.enB[I];
+                        T dx = nx - ox, dy = ny - oy, dz = nz - oz;
+                        T d, ri, uu, upr, lt;
+                        dist(dx * dx + dy * dy + dz * dz, d, ri);
+                        pade_ab(pa, pb, d, ri, uu, upr, lt);
+                        unew[1] = uu;
+                        const T old = jc[pair_slot(e, j)];
+                        ds += (is_el && j != e) ? uu - old : T(0);
+                        enn = is_nuc ? uu : T(0);
+                        ds -= enn;
                     }
                     du = wsum(ds) + jc[NPAIR + e];
                 } else {

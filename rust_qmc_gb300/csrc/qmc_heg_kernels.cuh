@@ -318,36 +318,68 @@ __device__ __forceinline__ T hsum(T v) {
     return v;
 }
 
+// u(r) alone, heg_u's expression for it, evaluated on every lane and masked
+// (no divergent branch; out-of-range lanes may compute non-finite values).
+template <class T>
+__device__ __forceinline__ T heg_u_value(const SysH<T>& S, T r, T a) {
+    T u;
+    if (S.form == 0) {
+        u = a * r / (1 + r / S.F);
+    } else if (S.form == 1) {
+        const T den = 1 + S.pb * r + S.pc * r * r;
+        u = a * r / den;
+    } else {
+        const T x = r / S.F, ex = fexp(-x), op = 1 + x;
+        u = a * r * ex / op;
+    }
+    return (r < S.halfL && r > T(1e-10)) ? u : T(0);
+}
+
 // Jastrow change (and gradients) for electron e moving o -> n.
 template <int NE, int NUP, class T, bool GRAD>
 __device__ __forceinline__ T hjastrow_delta(const SysH<T>& S, const HLanePos<T, NE>& P, int lane, int e, T ox, T oy,
                                             T oz, T nx, T ny, T nz, T (&go)[3], T (&gn)[3]) {
     T du = 0, g[6] = {0, 0, 0, 0, 0, 0};
+    if constexpr (!GRAD) {
+        // value only: every lane evaluates its partners and masks the unused ones
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int j = lane + 32 * r;
-        if (j < NE && j != e) {
+        for (int r = 0; r < 2; ++r) {
+            const int j = lane + 32 * r;
             const T a = S.a_ee[((j < NUP) == (e < NUP)) ? 1 : 0];
             T ax = min_img(ox - P.x[r], S), ay = min_img(oy - P.y[r], S), az = min_img(oz - P.z[r], S);
             T bx = min_img(nx - P.x[r], S), by = min_img(ny - P.y[r], S), bz = min_img(nz - P.z[r], S);
             T ra = fsqrt(ax * ax + ay * ay + az * az), rb = fsqrt(bx * bx + by * by + bz * bz);
-            T ua, dua, lua, ub, dub, lub;
-            heg_u(S, ra, a, ua, dua, lua);
-            heg_u(S, rb, a, ub, dub, lub);
-            du += ub - ua;
-            if (GRAD) {
-                T fa = ra > 0 ? dua / ra : T(0), fb = rb > 0 ? dub / rb : T(0);
-                g[0] += fa * ax; g[1] += fa * ay; g[2] += fa * az;
-                g[3] += fb * bx; g[4] += fb * by; g[5] += fb * bz;
+            const T d = heg_u_value(S, rb, a) - heg_u_value(S, ra, a);
+            du += (j < NE && j != e) ? d : T(0);
+        }
+        return hsum(du);
+    } else {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int j = lane + 32 * r;
+            if (j < NE && j != e) {
+                const T a = S.a_ee[((j < NUP) == (e < NUP)) ? 1 : 0];
+                T ax = min_img(ox - P.x[r], S), ay = min_img(oy - P.y[r], S), az = min_img(oz - P.z[r], S);
+                T bx = min_img(nx - P.x[r], S), by = min_img(ny - P.y[r], S), bz = min_img(nz - P.z[r], S);
+                T ra = fsqrt(ax * ax + ay * ay + az * az), rb = fsqrt(bx * bx + by * by + bz * bz);
+                T ua, dua, lua, ub, dub, lub;
+                heg_u(S, ra, a, ua, dua, lua);
+                heg_u(S, rb, a, ub, dub, lub);
+                du += ub - ua;
+                if (GRAD) {
+                    T fa = ra > 0 ? dua / ra : T(0), fb = rb > 0 ? dub / rb : T(0);
+                    g[0] += fa * ax; g[1] += fa * ay; g[2] += fa * az;
+                    g[3] += fb * bx; g[4] += fb * by; g[5] += fb * bz;
+                }
             }
         }
+        du = hsum(du);
+        if (GRAD) {
+            go[0] = hsum(g[0]); go[1] = hsum(g[1]); go[2] = hsum(g[2]);
+            gn[0] = hsum(g[3]); gn[1] = hsum(g[4]); gn[2] = hsum(g[5]);
+        }
+        return du;
     }
-    du = hsum(du);
-    if (GRAD) {
-        go[0] = hsum(g[0]); go[1] = hsum(g[1]); go[2] = hsum(g[2]);
-        gn[0] = hsum(g[3]); gn[1] = hsum(g[4]); gn[2] = hsum(g[5]);
-    }
-    return du;
 }
 
 template <class TS>

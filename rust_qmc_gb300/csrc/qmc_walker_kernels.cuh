@@ -928,7 +928,7 @@ __device__ __forceinline__ void assemble_sector(const SysT<SH, ff>& S, const flo
 #pragma unroll
             for (int j = 0; j < NS; ++j) dinv[((size_t)(SIG * NM * NM + k * NM + j)) * Wcap + w] = (TS)Di[k][j];
     }
-    if (VALUES) {
+    if constexpr (VALUES) {
 #pragma unroll
         for (int q = 0; q < NS; ++q) ut += ff_load(rows + ((size_t)(SIG * SH::NUP + q) * RL::QN + RL::J0 + 5) * st + wr);
         return;

@@ -95,6 +95,15 @@ __device__ __forceinline__ void ff_fma_lazy(ff& acc, ff c, ff x) {
 }
 __device__ __forceinline__ ff ff_norm(ff a) { return ff_fast_two_sum(a.hi, a.lo); }
 
+// acc += c x for any compute type: the lazy float-float step for ff (close
+// with macc_norm), a plain multiply-add otherwise.
+template <class T>
+__device__ __forceinline__ void macc(T& acc, T c, T x) { acc += c * x; }
+__device__ __forceinline__ void macc(ff& acc, ff c, ff x) { ff_fma_lazy(acc, c, x); }
+template <class T>
+__device__ __forceinline__ T macc_norm(T a) { return a; }
+__device__ __forceinline__ ff macc_norm(ff a) { return ff_norm(a); }
+
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
 __device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }

@@ -736,6 +736,86 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == 4 ? 16 / WPB : 1) kwb_s
 // Full evaluation from positions (refresh + E_L), one warp per walker.
 // Per-warp shared scratch holds the sector's D rows, then the rows of its
 // inverse; orbital derivatives are evaluated in a second pass.
+// Row stride of the refresh's per-warp matrix scratch: lane q writes row q
+// (element (q, k) at q MRS + k) and lane j reads column j; an odd stride keeps
+// both conflict-free.
+constexpr int MRS = 33;
+
+// Orbital values phi_k(x, y, z), k < NM, of sector sig by one lane: one pass
+// over the radial groups, lazily accumulated in the compute type.
+template <class TC, int NM>
+__device__ __forceinline__ void orbital_values(const SysW<TC>& S, int sig, TC x, TC y, TC z, TC (&v)[NM]) {
+#pragma unroll
+    for (int k = 0; k < NM; ++k) v[k] = 0;
+    for (int g = 0; g < S.n_grp; ++g) {
+        const int d = S.grp[g];
+        const int I = d & 15, kind = (d >> 4) & 1, np = (d >> 5) & 15, p0 = (d >> 9) & 255, a0 = grp_a0(d);
+        const TC dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+        const TC r2 = dx * dx + dy * dy + dz * dz;
+        TC s0 = 0;
+        for (int p = p0; p < p0 + np; ++p) {
+            TC al_p, cp;
+            load2(S.prim[p], al_p, cp);
+            s0 += cp * fexp(-al_p * r2);
+        }
+        for (int m = 0; m < (kind ? 3 : 1); ++m) {
+            const TC chi = kind ? (m == 0 ? dx : (m == 1 ? dy : dz)) * s0 : s0;
+            const TC* c = S.C[sig][a0 + m];
+#pragma unroll
+            for (int k = 0; k < NM; ++k) macc(v[k], c[k], chi);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NM; ++k) v[k] = macc_norm(v[k]);
+}
+
+// sum_a c'_a (grad chi_a, lap chi_a) at (x, y, z) with c'_a = sum_k C[sig][a][k] dcol[k]:
+// one pass over the radial groups (s AO, or p triplet sharing its radial part;
+// s: grad = -2 R1 dr, lap = -6 R1 + 4 r^2 R2; p_m: grad = x_m (-2 R1 dr) + e_m R0,
+// lap = x_m (-10 R1 + 4 r^2 R2), with R0, R1, R2 the radial sums weighted by
+// 1, alpha, alpha^2).
+template <class TC, int NM>
+__device__ __forceinline__ void inverse_weighted_derivatives(const SysW<TC>& S, int sig, TC x, TC y, TC z,
+                                                             const TC (&dcol)[NM], TC& gx, TC& gy, TC& gz, TC& lp) {
+    TC ax = 0, ay = 0, az = 0, al = 0;
+    for (int g = 0; g < S.n_grp; ++g) {
+        const int d = S.grp[g];
+        const int I = d & 15, kind = (d >> 4) & 1, np = (d >> 5) & 15, p0 = (d >> 9) & 255, a0 = grp_a0(d);
+        const TC dx = x - S.nuc[I][0], dy = y - S.nuc[I][1], dz = z - S.nuc[I][2];
+        const TC r2 = dx * dx + dy * dy + dz * dz;
+        TC s0 = 0, s1 = 0, s2 = 0;
+        for (int p = p0; p < p0 + np; ++p) {
+            TC al_p, cp;
+            load2(S.prim[p], al_p, cp);
+            const TC e = cp * fexp(-al_p * r2), ea = al_p * e;
+            s0 += e; s1 += ea; s2 += al_p * ea;
+        }
+        const TC l0 = TC(4) * r2 * s2;
+        for (int m = 0; m < (kind ? 3 : 1); ++m) {
+            const TC* c = S.C[sig][a0 + m];
+            TC cw = 0;
+#pragma unroll
+            for (int k = 0; k < NM; ++k) macc(cw, c[k], dcol[k]);
+            cw = macc_norm(cw);
+            TC gxa, gya, gza, la;
+            if (kind == 0) {
+                const TC t = TC(-2) * s1;
+                gxa = t * dx; gya = t * dy; gza = t * dz;
+                la = TC(-6) * s1 + l0;
+            } else {
+                const TC xm = m == 0 ? dx : (m == 1 ? dy : dz);
+                const TC t = TC(-2) * s1 * xm;
+                gxa = t * dx + (m == 0 ? s0 : TC(0));
+                gya = t * dy + (m == 1 ? s0 : TC(0));
+                gza = t * dz + (m == 2 ? s0 : TC(0));
+                la = xm * (TC(-10) * s1 + l0);
+            }
+            macc(ax, cw, gxa); macc(ay, cw, gya); macc(az, cw, gza); macc(al, cw, la);
+        }
+    }
+    gx = macc_norm(ax); gy = macc_norm(ay); gz = macc_norm(az); lp = macc_norm(al);
+}
+
 template <int NE, int NUP, int NNUC, class TC, class TS>
 __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow, const TS* __restrict__ gpos,
                                                     TS* __restrict__ gdinv, double* __restrict__ glog,
@@ -767,15 +847,16 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
 #pragma unroll
         for (int sig = 0; sig < 2; ++sig) {
             const int NS = sig == 0 ? NUP : NDN;
-            // pass 1: orbital values, row q = electron q, column = lane (MO)
-            for (int q = 0; q < NS; ++q) {
-                TC rx, ry, rz;
-                P.get(sig * NUP + q, rx, ry, rz);
-                AOLane<TC, 0> ao;
-                ao_lane<TC, 0>(S, rx, ry, rz, lane, ao);
-                TC v, gx, gy, gz, l;
-                mo_lane<TC, 0>(S, sig, lane, ao, v, gx, gy, gz, l);
-                Mrow[q * 32 + lane] = v;
+            // pass 1, lane q = electron q of the sector: its orbital values,
+            // written as row q of D
+            TC xq, yq, zq;
+            P.get_own(min(sig * NUP + lane, NE - 1), xq, yq, zq);
+            if (lane < NS) {
+                TC v[NM];
+                orbital_values<TC, NM>(S, sig, xq, yq, zq, v);
+#pragma unroll
+                for (int k = 0; k < NM; ++k)
+                    if (k < NS) Mrow[lane * MRS + k] = v[k];
             }
             __syncwarp();
             // Gauss-Jordan in place with partial pivoting: lane j carries
@@ -792,7 +873,7 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
             // loop would have them), and each step moves register 0 to the back.
             TC A[NM];
 #pragma unroll
-            for (int i = 0; i < NM; ++i) A[i] = (i < NS && lane < NS) ? Mrow[i * 32 + lane] : TC(i == lane ? 1 : 0);
+            for (int i = 0; i < NM; ++i) A[i] = (i < NS && lane < NS) ? Mrow[i * MRS + lane] : TC(i == lane ? 1 : 0);
             int src = lane;
 #pragma unroll 1
             for (int k = 0; k < NS; ++k) {
@@ -852,24 +933,13 @@ __device__ __forceinline__ double kw_measure_walker(const SysW<TC>& S, TC* Mrow,
                     if (k < NS) gdinv[((size_t)(sig * NM * NM + k * NM + lane)) * Wcap + w] = (TS)A[k];
             }
             __syncwarp();
-#pragma unroll
-            for (int k = 0; k < NM; ++k)
-                if (k < NS) Mrow[k * 32 + lane] = A[k];    // row k of D^-1
-            __syncwarp();
-            // pass 2: for electron q, lane k evaluates grad and lap of phi_k(r_q)
-            // and weights them by D^-1[k][q]; warp sums give this sector's
-            // grad ln D and lap D / D of electron q, kept by lane q
-            for (int q = 0; q < NS; ++q) {
-                TC rx, ry, rz;
-                P.get(sig * NUP + q, rx, ry, rz);
-                AOLane<TC, 3> ao;
-                ao_lane<TC, 3>(S, rx, ry, rz, lane, ao);
-                TC v, gx, gy, gz, l;
-                mo_lane<TC, 3>(S, sig, lane, ao, v, gx, gy, gz, l);
-                const TC d = lane < NS ? Mrow[lane * 32 + q] : TC(0);
-                const TC ax = wsum(gx * d), ay = wsum(gy * d), az = wsum(gz * d), al = wsum(l * d);
-                if (lane == q) { gdx[sig] = ax; gdy[sig] = ay; gdz[sig] = az; ld[sig] = al; }
-            }
+            // pass 2, lane q = electron q of the sector, holding column q of
+            // D^-1: grad ln D = sum_k grad phi_k(r_q) D^-1[k][q] = sum_a c'_a
+            // grad chi_a(r_q) with c'_a = sum_k C[a][k] D^-1[k][q] (the inverse
+            // column contracted into the coefficients first), and the same for
+            // lap D / D, over the radial groups at the lane's own electron
+            if (lane < NS)
+                inverse_weighted_derivatives<TC, NM>(S, sig, xq, yq, zq, A, gdx[sig], gdy[sig], gdz[sig], ld[sig]);
             __syncwarp();
         }
         // Jastrow + Coulomb for this lane's electrons (pairs counted from both ends)
@@ -974,7 +1044,7 @@ __global__ void __launch_bounds__(32 * WPB) kw_measure(const SysW<TC>* __restric
     load_sysw(&S, Sg);
     const int wib = threadIdx.x >> 5;
     const int w = blockIdx.x * WPB + wib;
-    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * 32;   // [NM rows][32 lanes]
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * MRS;   // [NM rows][MRS]
     double e_l = kw_measure_walker<NE, NUP, NNUC, TC, TS>(S, Mrow, gpos, gdinv, glog, gsign, gel, w, w < W, Wcap,
                                                           write_state, out_grad, out_lap, flags);
     if (partial) warp_block_partial<WPB>(e_l, partial, blockIdx.x);
@@ -990,7 +1060,7 @@ __global__ void __launch_bounds__(32 * WPB) kwb_measure(const BatchTile* __restr
     extern __shared__ __align__(16) unsigned char wsm[];
     if ((int)blockIdx.x >= ntiles) return;
     const int wib = threadIdx.x >> 5;
-    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * 32;
+    TC* Mrow = reinterpret_cast<TC*>(wsm) + (size_t)wib * NM * MRS;
     const BatchTile tl = tiles[blockIdx.x];
     const BatchRec& R = recs[tl.rec];
     load_sysw(&S, static_cast<const SysW<TC>*>(R.tab_d));
@@ -1052,7 +1122,7 @@ struct WarpShapeOps {
         int rc = table<TC>(hs, &S);
         if (rc) return rc;
         int nb = (dw.W + WB - 1) / WB;
-        size_t smem = sizeof(TC) * WB * NM * 32;
+        size_t smem = sizeof(TC) * WB * NM * MRS;
         auto kern = kw_measure<NE, NUP, NNUC, TC, TS, WB>;
         static bool attr = false;
         if (!attr) {
@@ -1192,7 +1262,7 @@ struct WarpShapeOps {
 
     template <class TC, class TS>
     static int batch_measure_t(const BatchClass& bc, cudaStream_t st, int* occ) {
-        const size_t smem = sizeof(TC) * BTW * NM * 32;
+        const size_t smem = sizeof(TC) * BTW * NM * MRS;
         auto kern = kwb_measure<NE, NUP, NNUC, TC, TS, BTW>;
         static bool attr = false;
         if (!attr) {

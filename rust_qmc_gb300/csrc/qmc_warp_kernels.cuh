@@ -275,6 +275,31 @@ __device__ __forceinline__ void mo_lane(const SysW<T>& S, int sig, int lane, con
     }
 }
 
+// c'_a = sum_k C[sig][a][k] Dinv[k][q] for the lane's AOs a = lane + 32 r: column q of
+// the inverse (lane q's registers) broadcast four entries at a time, the lane's
+// coefficient rows read as 16-byte vectors.  Lanes past the basis get 0.
+template <class T, int NM>
+__device__ __forceinline__ void inverse_column_coefficients(const SysW<T>& S, int sig, int lane, const T (&D)[NM],
+                                                            int q, T (&cw)[WAO_ROUNDS]) {
+#pragma unroll
+    for (int r = 0; r < WAO_ROUNDS; ++r) cw[r] = 0;
+#pragma unroll
+    for (int k0 = 0; k0 < NM; k0 += 4) {
+        T dq[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dq[i] = (k0 + i < NM) ? wshfl(D[k0 + i < NM ? k0 + i : 0], q) : T(0);
+#pragma unroll
+        for (int r = 0; r < WAO_ROUNDS; ++r) {
+            if (32 * r >= S.n_ao) break;
+            const int a = lane + 32 * r;
+            T c0, c1, c2, c3;
+            load4(&S.C[sig][a < S.n_ao ? a : 0][k0], c0, c1, c2, c3);
+            T t = c0 * dq[0] + c1 * dq[1] + c2 * dq[2] + c3 * dq[3];
+            cw[r] += a < S.n_ao ? t : T(0);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
@@ -516,18 +541,17 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 const MoveDraw<T> md = draw_of(draws, q);
                 T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
                 T gq[3];
-                if (MOVE == MOVE_ONE_DRIFT) {
+                // drift: c'_a = sum_k C[sig][a][k] Dinv[k][q] on the lanes of AO a, so that
+                // grad ln D at r and at r' are sums over the AOs (warp sums)
+                T cw[WAO_ROUNDS];
+                if constexpr (MOVE == MOVE_ONE_DRIFT) {
+                    inverse_column_coefficients<T, NM>(S, sig, lane, D, q, cw);
                     AOLane<T, 1> ao;
                     ao_lane<T, 1>(S, rx, ry, rz, lane, ao);
-                    T v, gx, gy, gz, l;
-                    mo_lane<T, 1>(S, sig, lane, ao, v, gx, gy, gz, l);
-                    // lane j: sum_k grad phi_k Dinv[k][j]; lane q holds the drift term
                     T ax = 0, ay = 0, az = 0;
 #pragma unroll
-                    for (int k = 0; k < NM; ++k) {
-                        ax += wshfl(gx, k) * D[k]; ay += wshfl(gy, k) * D[k]; az += wshfl(gz, k) * D[k];
-                    }
-                    ax = wshfl(ax, q); ay = wshfl(ay, q); az = wshfl(az, q);
+                    for (int r = 0; r < WAO_ROUNDS; ++r) { ax += cw[r] * ao.gx[r]; ay += cw[r] * ao.gy[r]; az += cw[r] * ao.gz[r]; }
+                    ax = wsum(ax); ay = wsum(ay); az = wsum(az);
                     T g0[3], g1[3];
                     wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
                     const T tau = a.tau, maxd = a.maxd;
@@ -544,14 +568,18 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 if constexpr (MOVE == MOVE_ONE_DRIFT) {
                     AOLane<T, 1> ao;
                     ao_lane<T, 1>(S, nx, ny, nz, lane, ao);
-                    T phi, pgx, pgy, pgz, pl;
-                    mo_lane<T, 1>(S, sig, lane, ao, phi, pgx, pgy, pgz, pl);
+                    // orbital values at r' (every t_j is needed for the update), the
+                    // gradient term of column q from c'
+                    AOLane<T, 0> av;
 #pragma unroll
-                    for (int k = 0; k < NM; ++k) {
-                        T d = D[k];
-                        tj += wshfl(phi, k) * d;
-                        bx += wshfl(pgx, k) * d; by += wshfl(pgy, k) * d; bz += wshfl(pgz, k) * d;
-                    }
+                    for (int r = 0; r < WAO_ROUNDS; ++r) av.v[r] = ao.v[r];
+                    T phi, pgx, pgy, pgz, pl;
+                    mo_lane<T, 0>(S, sig, lane, av, phi, pgx, pgy, pgz, pl);
+#pragma unroll
+                    for (int k = 0; k < NM; ++k) tj += wshfl(phi, k) * D[k];
+#pragma unroll
+                    for (int r = 0; r < WAO_ROUNDS; ++r) { bx += cw[r] * ao.gx[r]; by += cw[r] * ao.gy[r]; bz += cw[r] * ao.gz[r]; }
+                    bx = wsum(bx); by = wsum(by); bz = wsum(bz);
                 } else {
                     const T* row = ph + q * PHS;
                     T t0 = 0, t1 = 0;
@@ -611,7 +639,6 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     du = wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, nx, ny, nz, g0, gn);
                 }
                 if constexpr (MOVE == MOVE_ONE_DRIFT) {
-                    bx = wshfl(bx, q); by = wshfl(by, q); bz = wshfl(bz, q);
                     const T tau = a.tau, maxd = a.maxd;
                     T iR = R != T(0) ? T(1) / R : T(0);
                     T cx = tau * 2 * (bx * iR + gn[0]), cy = tau * 2 * (by * iR + gn[1]), cz = tau * 2 * (bz * iR + gn[2]);

@@ -339,57 +339,45 @@ struct LanePos {
     }
 };
 
-// Jastrow change for electron e moving (o -> n), lane-parallel over partner
-// electrons (the lane's own two) and nuclei (lane I < NNUC); warp-reduced.
-template <int NE, int NUP, int NNUC, class T, bool GRAD>
-__device__ __forceinline__ T wjastrow_delta(const SysW<T>& S, const LanePos<T, NE>& P, int lane, int e, T ox, T oy,
-                                            T oz, T nx, T ny, T nz, T (&go)[3], T (&gn)[3]) {
-    T du = 0;
-    T g[6] = {0, 0, 0, 0, 0, 0};
+// This lane's share of the Jastrow terms of electron e at (x, y, z): u =
+// sum_j u_ee(r_ej) - sum_I u_en(r_eI) and its gradient with respect to the
+// electron, over partner electron `lane` (first round) and partner electron
+// 32 + lane (lanes < NE1) or nucleus lane - NE1 (the next NNUC lanes; second
+// round).  Every lane evaluates and the unused terms are masked by selects.
+template <int NE, int NUP, int NNUC, class T>
+__device__ __forceinline__ void wjastrow_lane_terms(const SysW<T>& S, const LanePos<T, NE>& P, int lane, int e,
+                                                    T x, T y, T z, T& u, T (&g)[3]) {
+    constexpr int NE1 = NE > 32 ? NE - 32 : 0;
+    static_assert(NE <= 64 && NE1 + NNUC <= 32, "second round: electrons 32.. and the nuclei share the lanes");
     const bool e_up = e < NUP;
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int j = lane + 32 * r;
-        if (j < NE && j != e) {
-            const bool para = ((j < NUP) == e_up);
-            T ax = ox - P.x[r], ay = oy - P.y[r], az = oz - P.z[r];
-            T bx = nx - P.x[r], by = ny - P.y[r], bz = nz - P.z[r];
-            T da, ia, db, ib;
-            dist(ax * ax + ay * ay + az * az, da, ia);
-            dist(bx * bx + by * by + bz * bz, db, ib);
-            T ua, upa, lta, ub, upb, ltb;
-            const int c = para ? 1 : 0;
-            pade_ab(S.a_ee[c], S.b_ee[c], da, ia, ua, upa, lta);
-            pade_ab(S.a_ee[c], S.b_ee[c], db, ib, ub, upb, ltb);
-            du += ub - ua;
-            if (GRAD) {
-                g[0] += upa * ax; g[1] += upa * ay; g[2] += upa * az;
-                g[3] += upb * bx; g[4] += upb * by; g[5] += upb * bz;
-            }
-        }
+    {
+        const int j = lane < NE ? lane : NE - 1;
+        const bool ok = lane < NE && lane != e;
+        const int c = ((j < NUP) == e_up) ? 1 : 0;
+        const T dx = x - P.x[0], dy = y - P.y[0], dz = z - P.z[0];
+        T d, ri, uu, upr, lt;
+        dist(dx * dx + dy * dy + dz * dz, d, ri);
+        pade_ab(S.a_ee[c], S.b_ee[c], d, ri, uu, upr, lt);
+        u = ok ? uu : T(0);
+        const T f = ok ? upr : T(0);
+        g[0] = f * dx; g[1] = f * dy; g[2] = f * dz;
     }
-    if (lane < NNUC) {
-        const int I = lane;
-        T ax = ox - S.nuc[I][0], ay = oy - S.nuc[I][1], az = oz - S.nuc[I][2];
-        T bx = nx - S.nuc[I][0], by = ny - S.nuc[I][1], bz = nz - S.nuc[I][2];
-        T da, ia, db, ib;
-        dist(ax * ax + ay * ay + az * az, da, ia);
-        dist(bx * bx + by * by + bz * bz, db, ib);
-        T ua, upa, lta, ub, upb, ltb;
-        pade_ab(S.enA[I], S.enB[I], da, ia, ua, upa, lta);
-        pade_ab(S.enA[I], S.enB[I], db, ib, ub, upb, ltb);
-        du -= ub - ua;
-        if (GRAD) {
-            g[0] -= upa * ax; g[1] -= upa * ay; g[2] -= upa * az;
-            g[3] -= upb * bx; g[4] -= upb * by; g[5] -= upb * bz;
-        }
+    {
+        const bool is_el = lane < NE1, is_nuc = !is_el && lane - NE1 < NNUC;
+        const int j = is_el ? 32 + lane : 0, I = is_nuc ? lane - NE1 : 0;
+        const bool el_ok = is_el && j != e;
+        const T ox = is_el ? P.x[1] : S.nuc[I][0], oy = is_el ? P.y[1] : S.nuc[I][1];
+        const T oz = is_el ? P.z[1] : S.nuc[I][2];
+        const int c = ((j < NUP) == e_up) ? 1 : 0;
+        const T pa = is_el ? S.a_ee[c] : S.enA[I], pb = is_el ? S.b_ee[c] : S.enB[I];
+        const T dx = x - ox, dy = y - oy, dz = z - oz;
+        T d, ri, uu, upr, lt;
+        dist(dx * dx + dy * dy + dz * dz, d, ri);
+        pade_ab(pa, pb, d, ri, uu, upr, lt);
+        u += el_ok ? uu : (is_nuc ? -uu : T(0));
+        const T f = el_ok ? upr : (is_nuc ? -upr : T(0));
+        g[0] += f * dx; g[1] += f * dy; g[2] += f * dz;
     }
-    du = wsum(du);
-    if (GRAD) {
-        go[0] = wsum(g[0]) * S.qa; go[1] = wsum(g[1]) * S.qa; go[2] = wsum(g[2]) * S.qa;
-        gn[0] = wsum(g[3]) * S.qa; gn[1] = wsum(g[4]) * S.qa; gn[2] = wsum(g[5]) * S.qa;
-    }
-    return du;
 }
 
 // Row stride of the per-warp proposal-orbital scratch (a multiple of 4
@@ -540,10 +528,10 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                 P.get(e, rx, ry, rz);
                 const MoveDraw<T> md = draw_of(draws, q);
                 T nx, ny, nz, logG = 0, dlx = 0, dly = 0, dlz = 0;
-                T gq[3];
                 // drift: c'_a = sum_k C[sig][a][k] Dinv[k][q] on the lanes of AO a, so that
                 // grad ln D at r and at r' are sums over the AOs (warp sums)
                 T cw[WAO_ROUNDS];
+                T u_old = 0;                           // drift: this lane's Jastrow terms at r
                 if constexpr (MOVE == MOVE_ONE_DRIFT) {
                     inverse_column_coefficients<T, NM>(S, sig, lane, D, q, cw);
                     AOLane<T, 1> ao;
@@ -552,8 +540,11 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
 #pragma unroll
                     for (int r = 0; r < WAO_ROUNDS; ++r) { ax += cw[r] * ao.gx[r]; ay += cw[r] * ao.gy[r]; az += cw[r] * ao.gz[r]; }
                     ax = wsum(ax); ay = wsum(ay); az = wsum(az);
-                    T g0[3], g1[3];
-                    wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, rx, ry, rz, g0, g1);
+                    T gl[3];
+                    wjastrow_lane_terms<NE, NUP, NNUC, T>(S, P, lane, e, rx, ry, rz, u_old, gl);
+                    T g0[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) g0[c] = wsum(gl[c]) * S.qa;
                     const T tau = a.tau, maxd = a.maxd;
                     dlx = tau * 2 * (ax + g0[0]); dly = tau * 2 * (ay + g0[1]); dlz = tau * 2 * (az + g0[2]);
                     T m = fsqrt(dlx * dlx + dly * dly + dlz * dlz);
@@ -595,7 +586,7 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     tj = t0 + t1;
                 }
                 const T R = wshfl(tj, q);
-                T g0[3], gn[3];
+                T gn[3];
                 T du, unew[2] = {T(0), T(0)}, enn = 0;
                 if constexpr (MOVE == MOVE_ONE_GAUSS) {
                     // new terms of the moving electron against the cached old
@@ -636,7 +627,12 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     }
                     du = wsum(ds) + jc[NPAIR + e];
                 } else {
-                    du = wjastrow_delta<NE, NUP, NNUC, T, true>(S, P, lane, e, rx, ry, rz, nx, ny, nz, g0, gn);
+                    // new position's terms against the old position's (kept from the drift)
+                    T un, gl[3];
+                    wjastrow_lane_terms<NE, NUP, NNUC, T>(S, P, lane, e, nx, ny, nz, un, gl);
+                    du = wsum(un - u_old);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) gn[c] = wsum(gl[c]) * S.qa;
                 }
                 if constexpr (MOVE == MOVE_ONE_DRIFT) {
                     const T tau = a.tau, maxd = a.maxd;
@@ -648,7 +644,6 @@ __device__ __forceinline__ void kw_sweep_walker(const SysW<T>& S, A& a, int w, T
                     T qx = rx - nx - cx, qy = ry - ny - cy, qz = rz - nz - cz;
                     logG = ((fx * fx + fy * fy + fz * fz) - (qx * qx + qy * qy + qz * qz)) / (4 * tau);
                 }
-                (void)gq;
                 T ratio = R * fexp(du);
                 T prob = ratio * ratio;
                 if (MOVE == MOVE_ONE_DRIFT) prob *= fexp(logG);

@@ -273,7 +273,8 @@ int qmc_walkers_sweep(qmc_walkers_t wk, int move_kind, int n_sweeps, uint64_t st
 /* Per-walker E_L [W] (device values from the last refresh) and logabs/sign. */
 int qmc_walkers_get_state(qmc_walkers_t wk, double* logabs, int* sign, double* e_local);
 /* Bitwise OR of the per-walker status flags raised since the last call
- * (1 singular, 2 non-finite); cleared on read. */
+ * (1 singular, 2 non-finite, 8 a bounded device wait of a sweep gave up);
+ * cleared on read. */
 int qmc_walkers_status(qmc_walkers_t wk, int* flags);
 
 /* Walker set with room for `capacity` walkers (DMC populations grow and

@@ -243,7 +243,8 @@ int build_hostsys(const qmc_system_desc* d, HostSys& hs) {
 
 void free_dev(DevWalkers& dw) {
     cudaFree(dw.pos); cudaFree(dw.dinv); cudaFree(dw.logabs); cudaFree(dw.sign); cudaFree(dw.el);
-    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(dw.rows);
+    cudaFree(dw.flags); cudaFree(dw.acc); cudaFree(dw.partial); cudaFree(dw.rows); cudaFree(dw.chunk_done);
+    cudaFree(dw.chunk_jc);
     dw = DevWalkers();
 }
 
@@ -268,6 +269,7 @@ int alloc_dev(DevWalkers& dw, const HostSys& hs, int W, int Wcap, int prec, cuda
     if (e == cudaSuccess) e = cudaMalloc((void**)&dw.partial, 8 * (size_t)dw.partial_cap);
     const size_t rb = prec == QMC_FP32_REFINE ? refresh_rows_bytes(hs.shape) : 0;
     if (e == cudaSuccess && rb) e = cudaMalloc((void**)&dw.rows, rb * Wc);
+    if (e == cudaSuccess && prec == QMC_FP32_REFINE) e = cudaMalloc((void**)&dw.chunk_done, 4 * (Wc / 32));
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.flags, 0, 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.acc, 0, 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dw.sign, 0, 4 * Wc, st);

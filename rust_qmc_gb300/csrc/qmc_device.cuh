@@ -17,7 +17,7 @@ enum { BASIS_GTO = 0, BASIS_STO = 1 };
 enum { JAS_NONE = 0, JAS_PADE_F = 1, JAS_PADE_EEN = 2 };
 enum { MOVE_ALL_GAUSS = 0, MOVE_ALL_BOX = 1, MOVE_ONE_GAUSS = 2, MOVE_ONE_DRIFT = 3 };
 enum { TAG_PROPOSE = 1, TAG_ACCEPT = 2, TAG_INIT = 3, TAG_BRANCH = 4 };
-enum { FLAG_SINGULAR = 1, FLAG_NONFINITE = 2 };
+enum { FLAG_SINGULAR = 1, FLAG_NONFINITE = 2, FLAG_TIMEOUT = 8 };
 
 // Compile-time basis layout of the 9-function CH4 workload: shell s sits on
 // nucleus nuc(s), has np(s) primitives and is kind 1 (one s AO) or kind 2

@@ -78,6 +78,8 @@ struct DevWalkers {
     int partial_cap = 0;
     int fixed_node = 0;                  // sweeps refuse sign-changing proposals (DMC)
     float2* rows = nullptr;              // two-pass refresh scratch [N][row quantities][Wcap] (FP32 walkers)
+    unsigned* chunk_done = nullptr;      // [Wcap / 32] chunked sweeps: chunks published per 32-walker group (FP32 walkers)
+    float* chunk_jc = nullptr;           // chunked Gaussian sweeps: pair cache + one-body terms between chunks (allocated on first use)
 };
 
 // Device buffers of the DMC branching step (population control).

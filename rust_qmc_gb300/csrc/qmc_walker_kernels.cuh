@@ -1190,34 +1190,59 @@ __device__ __forceinline__ void sweep_sector(const SysT<SH, T>& S, T* sp, T* sd,
 #undef DI
 }
 
+// A global load, at the L2 when CG (state that another SM wrote during the same
+// kernel: this SM's L1 may hold an older copy).
+template <bool CG, class V>
+__device__ __forceinline__ V ld_state(const V* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+
 // n_sweeps single-electron sweeps of walker w, staged through the calling
-// thread's shared-memory columns sp / sd.
+// thread's shared-memory columns sp / sd; the accepted moves and status bits
+// are added to acc_out / flg_out.
 // a: the walker arrays, c: the sweep controls; both the same const SweepArgs<T>
 // of kernel parameters, or the same block-shared const volatile one.
-template <class SH, class T, int MOVE, int TPB, class A, class C>
-__device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, A& a, C& c, int w) {
+// jcache (chunked sweeps only): the walker's pair cache and one-body terms as
+// the previous chunk left them, [slot][Wcap], read instead of recomputed when
+// jc_load and written back when jc_store (recomputing them gives the same
+// values: the same expressions on the same positions).
+template <class SH, class T, int MOVE, int TPB, bool CG = false, class A, class C>
+__device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, A& a, C& c, int w,
+                                             unsigned& acc_out, int& flg_out, T* jcache = nullptr,
+                                             bool jc_load = false, bool jc_store = false) {
+    constexpr int NPC = sweep_pairs<SH, MOVE>();
     constexpr int NM = SH::NMAX;
     const int t = threadIdx.x;
     const PosCols<T, TPB, SH::NE> P(sp, t);
 #pragma unroll
     for (int e = 0; e < SH::NE; ++e)
-        P.set(e, a.pos[(size_t)(3 * e) * a.Wcap + w], a.pos[(size_t)(3 * e + 1) * a.Wcap + w],
-              a.pos[(size_t)(3 * e + 2) * a.Wcap + w]);
+        P.set(e, ld_state<CG>(&a.pos[(size_t)(3 * e) * a.Wcap + w]), ld_state<CG>(&a.pos[(size_t)(3 * e + 1) * a.Wcap + w]),
+              ld_state<CG>(&a.pos[(size_t)(3 * e + 2) * a.Wcap + w]));
 #pragma unroll
-    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = a.dinv[(size_t)i * a.Wcap + w];
+    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = ld_state<CG>(&a.dinv[(size_t)i * a.Wcap + w]);
     T* pc = sd + 2 * NM * NM * TPB + t;
     // one-body terms of the electrons (thread-local; the pair cache fills the
     // shared-memory budget of a walker)
     T u1c[SH::NE];
-    if constexpr (sweep_pairs<SH, MOVE>() > 0) {
-        pair_cache_fill<SH, T, TPB>(S, P, pc);
-        if (SH::JAS == JAS_PADE_EEN) {
+    if constexpr (NPC > 0) {
+        if (CG && jc_load) {
+#pragma unroll
+            for (int k = 0; k < NPC; ++k) pc[k * TPB] = __ldcg(&jcache[(size_t)k * a.Wcap + w]);
+            if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+                for (int e = 0; e < SH::NE; ++e) u1c[e] = __ldcg(&jcache[(size_t)(NPC + e) * a.Wcap + w]);
+            }
+        } else {
+            pair_cache_fill<SH, T, TPB>(S, P, pc);
+            if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll 1
-            for (int e = 0; e < SH::NE; ++e)
-                u1c[e] = one_body_u(S, P(e, 0), P(e, 1), P(e, 2));
+                for (int e = 0; e < SH::NE; ++e)
+                    u1c[e] = one_body_u(S, P(e, 0), P(e, 1), P(e, 2));
+            }
         }
     }
-    int sgn = a.sign[w];
+    int sgn = ld_state<CG>(&a.sign[w]);
     unsigned acc = 0;
     int flg = 0;
     for (int it = 0; it < c.n_sweeps; ++it) {
@@ -1234,8 +1259,18 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
 #pragma unroll
     for (int i = 0; i < 2 * NM * NM; ++i) a.dinv[(size_t)i * a.Wcap + w] = sd[i * TPB + t];
     a.sign[w] = sgn;
-    if (acc) atomicAdd(a.acc, (unsigned long long)acc);
-    if (flg) atomicOr(a.flags, flg);
+    if constexpr (NPC > 0) {
+        if (CG && jc_store) {
+#pragma unroll
+            for (int k = 0; k < NPC; ++k) jcache[(size_t)k * a.Wcap + w] = pc[k * TPB];
+            if (SH::JAS == JAS_PADE_EEN) {
+#pragma unroll
+                for (int e = 0; e < SH::NE; ++e) jcache[(size_t)(NPC + e) * a.Wcap + w] = u1c[e];
+            }
+        }
+    }
+    acc_out += acc;
+    flg_out |= flg;
 }
 
 // Occupancy target: all walkers of the 65 536-walker workload resident in
@@ -1255,7 +1290,80 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
     // volatile arguments use fewer registers here but issue slower)
     const SweepArgs<T> a{gpos, gdinv, gsign, acc_out, flags, step0, seed, step, tau, maxd, W, Wcap, n_sweeps,
                          fixed_node};
-    sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w);
+    unsigned acc = 0;
+    int flg = 0;
+    sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w, acc, flg);
+    if (acc) atomicAdd(acc_out, (unsigned long long)acc);
+    if (flg) atomicOr(flags, flg);
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Upper bound on the polls of a chunk's wait (with a 256 ns back-off: about a
+// second) before it gives up and raises FLAG_TIMEOUT.
+constexpr unsigned CHUNK_WAIT_POLLS = 1u << 22;
+
+// The same sweeps as k_sweep_one, as (32-walker group g, chunk c of CH sweeps)
+// units taken in the order u = c G + g by persistent warps (warp p: units p,
+// p + P, p + 2P, ...), with P a whole number of warps per SM sub-partition.
+// A group's chunks move between warps, so every sub-partition carries the same
+// share of the work, where one warp per group for the whole launch leaves the
+// sub-partitions with 3 or 4 warps each.  A unit starts once the group's
+// previous chunk is published (done[g] = c, a bounded wait that raises
+// FLAG_TIMEOUT and goes on when it gives up), reads the group's walker state at
+// the L2, writes it back and publishes done[g] = c + 1.  It is launched
+// cooperatively, so every warp is resident; a unit waits only for a unit with
+// a smaller index, so the waits end.  done[] is zero at the launch.
+template <class SH, class T, int MOVE, int TPB>
+__global__ void __launch_bounds__(TPB, (MOVE == MOVE_ONE_GAUSS ? 16 : 12) * 32 / TPB) k_sweep_chunks(
+    const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos, T* __restrict__ gdinv, int* __restrict__ gsign, int W,
+    int Wcap, int n_sweeps, int chunk, uint64_t step0, T step, T tau, T maxd, uint64_t seed,
+    unsigned long long* acc_out, int* flags, int fixed_node, unsigned* __restrict__ done, T* __restrict__ jcache) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* sp = reinterpret_cast<T*>(smraw);
+    T* sd = sp + 3 * SH::NE * TPB;
+    const int lane = threadIdx.x & 31;
+    const int G = (W + 31) / 32, n_chunks = (n_sweeps + chunk - 1) / chunk;
+    const long long P = (long long)gridDim.x * (TPB / 32);
+    const long long U = (long long)G * n_chunks;
+    for (long long u = (long long)blockIdx.x * (TPB / 32) + (threadIdx.x >> 5); u < U; u += P) {
+        const int g = (int)(u % G), c = (int)(u / G);
+        if (c > 0) {
+            if (lane == 0) {
+                unsigned polls = 0;
+                while (ld_acquire_gpu(done + g) < (unsigned)c) {
+                    if (++polls > CHUNK_WAIT_POLLS) { atomicOr(flags, FLAG_TIMEOUT); break; }
+                    __nanosleep(256);
+                }
+            }
+            __syncwarp();
+        }
+        const int w = g * 32 + lane;
+        const int s0 = c * chunk, ns = min(chunk, n_sweeps - s0);
+        unsigned acc = 0;
+        int flg = 0;
+        if (w < W) {
+            const SweepArgs<T> a{gpos, gdinv, gsign, acc_out, flags, step0 + (uint64_t)s0, seed, step, tau, maxd, W,
+                                 Wcap, ns, fixed_node};
+            sweep_walker<SH, T, MOVE, TPB, true>(S, sp, sd, a, a, w, acc, flg, jcache, c > 0, c + 1 < n_chunks);
+        }
+        acc = __reduce_add_sync(0xffffffffu, acc);
+        flg = (int)__reduce_or_sync(0xffffffffu, (unsigned)flg);
+        __syncwarp();                          // the lanes' state writes before lane 0's release
+        if (lane == 0) {
+            __threadfence();
+            st_release_gpu(done + g, (unsigned)(c + 1));
+            if (acc) atomicAdd(acc_out, (unsigned long long)acc);
+            if (flg) atomicOr(flags, flg);
+        }
+    }
 }
 
 // Batched form: one block per (system, TPB-walker tile); the system table is
@@ -1276,7 +1384,11 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) kb_sw
     __syncthreads();
     const volatile SweepArgs<T>& a = args;
     const int w = tl.w0 + (int)threadIdx.x;
-    if (w < a.W) sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w);
+    unsigned acc = 0;
+    int flg = 0;
+    if (w < a.W) sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w, acc, flg);
+    if (acc) atomicAdd(a.acc, (unsigned long long)acc);
+    if (flg) atomicOr(a.flags, flg);
 }
 
 // Batched refresh + E_L (compute type TC) with one compensated partial per tile.
@@ -1474,11 +1586,68 @@ struct ShapeOps {
             cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
             attr_set = true;
         }
+        if constexpr (std::is_same<T, float>::value) {
+            int rc = 0;
+            if (sweep_chunks<T, MOVE>(S, dw, n, s0, step, tau, maxd, seed, smem, st, rc)) return rc;
+        }
         int nb = (dw.W + TPB - 1) / TPB;
         kern<<<nb, TPB, smem, st>>>(S, (T*)dw.pos, (T*)dw.dinv, dw.sign, dw.W, dw.Wcap, n, s0, (T)step, (T)tau,
                                     (T)maxd, seed, dw.acc, dw.flags, dw.fixed_node);
         ++g_launch_count;
         return cuda_status(cudaGetLastError());
+    }
+
+    // The chunked form of sweep_one (k_sweep_chunks) when the set fills every SM
+    // sub-partition with CHUNK_WARPS warps at least once and the stream is not
+    // being captured; false leaves the launch to the one-warp-per-group kernel.
+    static constexpr int CHUNK_SWEEPS = 8, CHUNK_WARPS = 3;
+    template <class T, int MOVE>
+    static bool sweep_chunks(const SysT<SH, T>& S, DevWalkers& dw, int n, uint64_t s0, double step, double tau,
+                             double maxd, uint64_t seed, size_t smem, cudaStream_t st, int& rc) {
+        constexpr int TPB = 64, BPS = 4 * CHUNK_WARPS * 32 / TPB;   // blocks per SM
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                return false;
+        }
+        const int G = (dw.W + 31) / 32;
+        if (!dw.chunk_done || n < 2 * CHUNK_SWEEPS || G < nsm * BPS * (TPB / 32)) return false;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+        auto kern = k_sweep_chunks<SH, T, MOVE, TPB>;
+        static int occ = -1;
+        if (occ < 0) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem) != cudaSuccess) occ = 0;
+        }
+        if (occ < BPS) return false;
+        constexpr int NJC = sweep_pairs<SH, MOVE>() > 0 ? sweep_pairs<SH, MOVE>() + SH::NE : 0;
+        if (NJC > 0 && !dw.chunk_jc) {
+            if (cudaMalloc((void**)&dw.chunk_jc, sizeof(float) * NJC * (size_t)dw.Wcap) != cudaSuccess) {
+                dw.chunk_jc = nullptr;
+                return false;
+            }
+        }
+        rc = cuda_status(cudaMemsetAsync(dw.chunk_done, 0, 4 * (size_t)G, st));
+        if (rc) return true;
+        T* pos = (T*)dw.pos;
+        T* dinv = (T*)dw.dinv;
+        int* sign = dw.sign;
+        int W = dw.W, Wcap = dw.Wcap, ns = n, ch = CHUNK_SWEEPS, fixed = dw.fixed_node;
+        T stp = (T)step, ta = (T)tau, md = (T)maxd;
+        uint64_t step0 = s0, sd = seed;
+        unsigned long long* acc = dw.acc;
+        int* flags = dw.flags;
+        unsigned* done = dw.chunk_done;
+        T* jc = (T*)dw.chunk_jc;
+        void* args[] = {(void*)&S, &pos,   &dinv, &sign,  &W,   &Wcap, &ns,    &ch,    &step0,
+                        &stp,      &ta,    &md,   &sd,    &acc, &flags, &fixed, &done, &jc};
+        rc = cuda_status(cudaLaunchCooperativeKernel((const void*)kern, dim3(nsm * BPS), dim3(TPB), args, smem, st));
+        ++g_launch_count;
+        return true;
     }
 
     template <class T, int MOVE>

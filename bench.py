@@ -562,11 +562,15 @@ def main():
     fp32_peak, fp64_peak = ctx.measure_peaks()
     flops_launch = moves_per_step * counts["sweep_flops_per_move"]
     achieved_tf = flops_launch / launch_s / 1e12
-    traffic = None
+    # the library takes the chunked sweep (k_sweep_chunks) for sets that give
+    # every SM sub-partition three warps, as 65 536 walkers do on 152 SMs
+    traffic, sweep_kernel = None, "k_sweep_chunks<ShapeCH4Min,float,ONE_GAUSS,64>"
     tpath = os.path.join(ROOT, "profiles", "traffic_ch4_sweep.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch_65536_walkers")
+            tj = json.load(open(tpath))
+            traffic = tj.get("bytes_per_launch_65536_walkers")
+            sweep_kernel = tj.get("kernel", sweep_kernel)
         except Exception:
             traffic = None
     # the sweep keeps its walkers in shared memory for all 64 sweeps: FP32 issue
@@ -575,7 +579,7 @@ def main():
     roofline = {"bound": "fp32_simt", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved_tf / fp32_peak if fp32_peak else None, "traffic": traffic,
                 "peak_source": "measured FMA-chain kernel on this GPU (qmc_ctx_measure_peaks)",
-                "kernel": "k_sweep_one<ShapeCH4Min,float,ONE_GAUSS,64>",
+                "kernel": sweep_kernel,
                 "flops_per_move": counts["sweep_flops_per_move"],
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch, one ncu capture "
                                   "(profiles/traffic_ch4_sweep.json)"}

@@ -109,3 +109,77 @@ def test_noalloc_sr_sums_match_allocating_entry_point():
             b.free()
         sysh.close()
         ctx.close()
+
+
+def test_noalloc_sr_sums_capture_and_replay():
+    """After one eager call (its set-up), further eager calls leave the device's
+    free memory unchanged, and the call records into a CUDA graph on a
+    non-blocking stream (global capture mode): replaying that graph with new
+    inputs in the same buffers gives the allocating entry point's sums."""
+    lib = Q.load_library()
+    ctx = Q.Context(0)
+    spec = Q.methane_minimal()
+    spec = spec.with_params(np.concatenate([spec.jas, [0.1, -0.2, 0.05, 0.3]]))
+    sysh = Q.System(ctx, spec)
+    rt = _cudart()
+    rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    rt.cudaStreamCreateWithFlags.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
+    rt.cudaStreamBeginCapture.argtypes = [C.c_void_p, C.c_int]
+    rt.cudaStreamEndCapture.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    rt.cudaGraphInstantiate.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_ulonglong]
+    rt.cudaGraphLaunch.argtypes = [C.c_void_p, C.c_void_p]
+    rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+    rt.cudaGraphExecDestroy.argtypes = [C.c_void_p]
+    rt.cudaGraphDestroy.argtypes = [C.c_void_p]
+    rt.cudaStreamDestroy.argtypes = [C.c_void_p]
+    P = sysh.num_params()
+    M = 2 + 2 * P + P * (P + 1) // 2
+    W = 2048
+    refs = [sysh.logderiv_batch(random_configs(spec, W, seed=s), sums=True) for s in (21, 22, 23)]
+    dE, dO, dS = DevBuf(rt, 8 * W), DevBuf(rt, 8 * W * P), DevBuf(rt, 8 * M)
+    dp = lambda b: C.cast(b.ptr, C.POINTER(C.c_double))
+
+    def free_bytes():
+        f, t = C.c_size_t(), C.c_size_t()
+        assert rt.cudaMemGetInfo(C.byref(f), C.byref(t)) == 0
+        return f.value
+
+    stream, graph, gexec = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    try:
+        O, E = refs[0][0], refs[0][1]
+        dE.put(E)
+        dO.put(O)
+        assert lib.qmc_sr_sums_noalloc(dp(dE), dp(dO), W, P, dp(dS), None) == L.QMC_OK   # set-up call
+        assert rt.cudaDeviceSynchronize() == 0
+        free0 = free_bytes()
+        for _ in range(3):
+            assert lib.qmc_sr_sums_noalloc(dp(dE), dp(dO), W, P, dp(dS), None) == L.QMC_OK
+        assert rt.cudaDeviceSynchronize() == 0
+        assert free_bytes() == free0
+        assert rt.cudaStreamCreateWithFlags(C.byref(stream), 1) == 0          # non-blocking
+        assert rt.cudaStreamBeginCapture(stream, 0) == 0                      # global mode
+        rc = lib.qmc_sr_sums_noalloc(dp(dE), dp(dO), W, P, dp(dS), stream)
+        assert rt.cudaStreamEndCapture(stream, C.byref(graph)) == 0
+        assert rc == L.QMC_OK
+        assert rt.cudaGraphInstantiate(C.byref(gexec), graph, 0) == 0
+        for O, E, S_ref, f_ref, em_ref in refs[1:]:
+            dE.put(E)
+            dO.put(O)
+            dS.put(np.full(M, np.nan))
+            assert rt.cudaGraphLaunch(gexec, stream) == 0
+            assert rt.cudaStreamSynchronize(stream) == 0
+            S, f, em = sums_to_sr(dS.get(M), W, P)
+            np.testing.assert_allclose(S, S_ref, rtol=1e-9, atol=1e-9 * np.abs(S_ref).max())
+            np.testing.assert_allclose(f, f_ref, rtol=1e-9, atol=1e-9 * np.abs(f_ref).max())
+            assert abs(em - em_ref) <= 1e-9 * max(1.0, abs(em_ref))
+    finally:
+        if gexec.value:
+            rt.cudaGraphExecDestroy(gexec)
+        if graph.value:
+            rt.cudaGraphDestroy(graph)
+        if stream.value:
+            rt.cudaStreamDestroy(stream)
+        for b in (dE, dO, dS):
+            b.free()
+        sysh.close()
+        ctx.close()

@@ -1207,6 +1207,9 @@ __device__ __forceinline__ V ld_state(const V* p) {
 // the previous chunk left them, [slot][Wcap], read instead of recomputed when
 // jc_load and written back when jc_store (recomputing them gives the same
 // values: the same expressions on the same positions).
+// CG (chunked sweeps): the inverse and the pair cache are already in the
+// thread's shared-memory columns (copied by the calling warp) and are written
+// back by it; the positions, sign and one-body terms are read at the L2 here.
 template <class SH, class T, int MOVE, int TPB, bool CG = false, class A, class C>
 __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd, A& a, C& c, int w,
                                              unsigned& acc_out, int& flg_out, T* jcache = nullptr,
@@ -1219,16 +1222,16 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
     for (int e = 0; e < SH::NE; ++e)
         P.set(e, ld_state<CG>(&a.pos[(size_t)(3 * e) * a.Wcap + w]), ld_state<CG>(&a.pos[(size_t)(3 * e + 1) * a.Wcap + w]),
               ld_state<CG>(&a.pos[(size_t)(3 * e + 2) * a.Wcap + w]));
+    if constexpr (!CG) {
 #pragma unroll
-    for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = ld_state<CG>(&a.dinv[(size_t)i * a.Wcap + w]);
+        for (int i = 0; i < 2 * NM * NM; ++i) sd[i * TPB + t] = a.dinv[(size_t)i * a.Wcap + w];
+    }
     T* pc = sd + 2 * NM * NM * TPB + t;
     // one-body terms of the electrons (thread-local; the pair cache fills the
     // shared-memory budget of a walker)
     T u1c[SH::NE];
     if constexpr (NPC > 0) {
         if (CG && jc_load) {
-#pragma unroll
-            for (int k = 0; k < NPC; ++k) pc[k * TPB] = __ldcg(&jcache[(size_t)k * a.Wcap + w]);
             if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll
                 for (int e = 0; e < SH::NE; ++e) u1c[e] = __ldcg(&jcache[(size_t)(NPC + e) * a.Wcap + w]);
@@ -1256,13 +1259,13 @@ __device__ __forceinline__ void sweep_walker(const SysT<SH, T>& S, T* sp, T* sd,
     for (int e = 0; e < SH::NE; ++e)
 #pragma unroll
         for (int c = 0; c < 3; ++c) a.pos[(size_t)(3 * e + c) * a.Wcap + w] = P(e, c);
+    if constexpr (!CG) {
 #pragma unroll
-    for (int i = 0; i < 2 * NM * NM; ++i) a.dinv[(size_t)i * a.Wcap + w] = sd[i * TPB + t];
+        for (int i = 0; i < 2 * NM * NM; ++i) a.dinv[(size_t)i * a.Wcap + w] = sd[i * TPB + t];
+    }
     a.sign[w] = sgn;
     if constexpr (NPC > 0) {
         if (CG && jc_store) {
-#pragma unroll
-            for (int k = 0; k < NPC; ++k) jcache[(size_t)k * a.Wcap + w] = pc[k * TPB];
             if (SH::JAS == JAS_PADE_EEN) {
 #pragma unroll
                 for (int e = 0; e < SH::NE; ++e) jcache[(size_t)(NPC + e) * a.Wcap + w] = u1c[e];
@@ -1295,6 +1298,27 @@ __global__ void __launch_bounds__(TPB, (sizeof(T) == 4 ? 512 : 256) / TPB) k_swe
     sweep_walker<SH, T, MOVE, TPB>(S, sp, sd, a, a, w, acc, flg);
     if (acc) atomicAdd(acc_out, (unsigned long long)acc);
     if (flg) atomicOr(flags, flg);
+}
+
+// 16-byte global -> shared copy at the L2 (cp.async.cg), and its completion.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Rows r of a warp's 32 walker columns, global [r][Wcap] from walker g0 <->
+// shared [r][TPB] from column c0: 16 bytes per lane, four rows per instruction.
+template <int TPB>
+__device__ __forceinline__ void warp_rows_in(float* sm, const float* gm, int rows, size_t Wcap, int lane) {
+    const int q = 4 * (lane & 7);
+    for (int r = lane >> 3; r < rows; r += 4) cp_async16(sm + (size_t)r * TPB + q, gm + (size_t)r * Wcap + q);
+}
+template <int TPB>
+__device__ __forceinline__ void warp_rows_out(float* gm, const float* sm, int rows, size_t Wcap, int lane) {
+    const int q = 4 * (lane & 7);
+    for (int r = lane >> 3; r < rows; r += 4)
+        *reinterpret_cast<float4*>(gm + (size_t)r * Wcap + q) = *reinterpret_cast<const float4*>(sm + (size_t)r * TPB + q);
 }
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
@@ -1347,6 +1371,15 @@ __global__ void __launch_bounds__(TPB, (MOVE == MOVE_ONE_GAUSS ? 16 : 12) * 32 /
         }
         const int w = g * 32 + lane;
         const int s0 = c * chunk, ns = min(chunk, n_sweeps - s0);
+        // the group's inverses (and, after its first chunk, pair caches) as whole
+        // rows of the warp's columns; the slots past W lie inside Wcap and
+        // travel unchanged
+        constexpr int NDI = 2 * SH::NMAX * SH::NMAX, NPC = sweep_pairs<SH, MOVE>();
+        T* sdw = sd + (threadIdx.x - lane);
+        warp_rows_in<TPB>(sdw, gdinv + (size_t)g * 32, NDI, (size_t)Wcap, lane);
+        if (NPC > 0 && c > 0) warp_rows_in<TPB>(sdw + NDI * TPB, jcache + (size_t)g * 32, NPC, (size_t)Wcap, lane);
+        cp_async_wait_all();
+        __syncwarp();
         unsigned acc = 0;
         int flg = 0;
         if (w < W) {
@@ -1354,6 +1387,9 @@ __global__ void __launch_bounds__(TPB, (MOVE == MOVE_ONE_GAUSS ? 16 : 12) * 32 /
                                  Wcap, ns, fixed_node};
             sweep_walker<SH, T, MOVE, TPB, true>(S, sp, sd, a, a, w, acc, flg, jcache, c > 0, c + 1 < n_chunks);
         }
+        __syncwarp();
+        warp_rows_out<TPB>(gdinv + (size_t)g * 32, sdw, NDI, (size_t)Wcap, lane);
+        if (NPC > 0 && c + 1 < n_chunks) warp_rows_out<TPB>(jcache + (size_t)g * 32, sdw + NDI * TPB, NPC, (size_t)Wcap, lane);
         acc = __reduce_add_sync(0xffffffffu, acc);
         flg = (int)__reduce_or_sync(0xffffffffu, (unsigned)flg);
         __syncwarp();                          // the lanes' state writes before lane 0's release

@@ -180,7 +180,8 @@ typedef struct {
     double acceptance_rate;
     double variance;
     int n_samples;
-    int status_flags;
+    int status_flags;            /* OR of: 1 singular, 2 non-finite, 4 DMC population collapse (re-initialised),
+                                    8 a bounded device wait of a sweep gave up */
     double avg_population;
     double final_step;           /* VMC: the step (all-electron / Gaussian) or tau (drift) after adaptation */
     double reserved[3];

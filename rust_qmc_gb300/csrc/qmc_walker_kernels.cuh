@@ -1350,6 +1350,7 @@ __global__ void __launch_bounds__(TPB, (MOVE == MOVE_ONE_GAUSS ? 16 : 12) * 32 /
     const __grid_constant__ SysT<SH, T> S, T* __restrict__ gpos, T* __restrict__ gdinv, int* __restrict__ gsign, int W,
     int Wcap, int n_sweeps, int chunk, uint64_t step0, T step, T tau, T maxd, uint64_t seed,
     unsigned long long* acc_out, int* flags, int fixed_node, unsigned* __restrict__ done, T* __restrict__ jcache) {
+    static_assert(std::is_same<T, float>::value, "the warp-row copies move 4-byte columns");
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sp = reinterpret_cast<T*>(smraw);
     T* sd = sp + 3 * SH::NE * TPB;

@@ -36,16 +36,27 @@ def _run(sysh, W, move, fixed_node=False):
     return acc, pos, sg, status
 
 
-@pytest.mark.parametrize("move", [L.QMC_MOVE_ONE_GAUSS, L.QMC_MOVE_ONE_DRIFT])
-def test_chunked_sweep_matches_one_warp_per_group(ctx, move):
-    sysh = Q.System(ctx, Q.methane_minimal())
+SYSTEMS = {
+    "ch4_min": (lambda: Q.methane_minimal(), 10),
+    "ch4_gto": (lambda: Q.methane_gto(), 10),
+    "li_ref": (lambda: Q.lithium_atom(reference_quirks=True), 3),
+    "h2": (lambda: Q.h2_mo(), 2),
+}
+
+
+@pytest.mark.parametrize("name,move", [("ch4_min", L.QMC_MOVE_ONE_GAUSS), ("ch4_min", L.QMC_MOVE_ONE_DRIFT),
+                                       ("ch4_gto", L.QMC_MOVE_ONE_GAUSS), ("li_ref", L.QMC_MOVE_ONE_GAUSS),
+                                       ("h2", L.QMC_MOVE_ONE_GAUSS)])
+def test_chunked_sweep_matches_one_warp_per_group(ctx, name, move):
+    build, n_elec = SYSTEMS[name]
+    sysh = Q.System(ctx, build())
     acc_b, pos_b, sg_b, st_b = _run(sysh, BIG, move)
     acc_s, pos_s, sg_s, st_s = _run(sysh, SMALL, move)
     assert st_b == 0 and st_s == 0, (st_b, st_s)          # no flag, no wait that gave up
     assert np.array_equal(pos_b[:SMALL], pos_s)
     assert np.array_equal(sg_b[:SMALL], sg_s)
     # acceptance of the two halves of the big set agree with the small set's rate
-    rate_b = acc_b / float(BIG * 10 * SWEEPS)
-    rate_s = acc_s / float(SMALL * 10 * SWEEPS)
+    rate_b = acc_b / float(BIG * n_elec * SWEEPS)
+    rate_s = acc_s / float(SMALL * n_elec * SWEEPS)
     assert abs(rate_b - rate_s) < 0.01, (rate_b, rate_s)
-    assert 0.2 < rate_b < 0.99
+    assert 0.05 < rate_b < 0.999
